@@ -1,0 +1,301 @@
+#!/usr/bin/env python3
+"""Benchmark of the stage-1 star x cluster screen on GB300 (one JSON line on stdout).
+
+Workload: one screening chunk of 20,000 synthetic stars x 4,087 synthetic clusters (phygas_gb300.synth "screen",
+seed 1001: the reference's stage-1 task size), chi2_max 25, n_samp 64, r_kernel 2.  A step screens the whole chunk:
+FP64 orbits + STM covariances of the 20,000 stars, the scan of all 81.7 M pairs, and the 512-draw probabilities of
+every kept pair, with the cluster table resident (built once, outside the timed region, as a serving process keeps
+it).
+
+  value     pairs/s of the mixed-precision screen, device time per chunk (CUDA events on the library's stream),
+            star inputs (nominal state + covariance of the draws) already in HBM; L2 flushed between steps
+  e2e       the same metric through the C-ABI call a user makes (pgx_draw_targets + pgx_screen): host star records
+            in, host rows out, host draws and host<->device copies inside the timed region
+  plain_fp64  the plain FP64 screen on the same chunk (the comparison the target is stated against)
+  roofline  the dominant kernel (the FP64 orbit integration): FP64 FLOP/s against the FP64 FMA peak measured in
+            this run by the library's probe kernel
+  cpu_baseline  the oracle (a pinned C restatement of the reference's CPU code) on all host cores, bounded sample
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun (N > 1) every rank screens its own chunk (weak scaling, no data exchange); rank 0 prints.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_STARS, N_CLUSTERS, SEED = 20000, 4087, 1001
+CHI2_MAX, N_SAMP, R_KERNEL = 25.0, 64, 2.0
+# FP64 flops of one body step (one KDK leapfrog step of one orbit: 9 FMA-class operations plus one force
+# evaluation), counted from the executed FP64 instructions of the orbit kernel (ncu sass op counters, FMA = 2;
+# profiles/stm_orbits_screen20k.md)
+FLOPS_PER_BODY_STEP = 236.0
+# DRAM traffic of one orbit-kernel launch on this chunk, from one ncu capture (same profile summary), bytes
+ORBIT_TRAFFIC_BYTES = None
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.p, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.p = None
+        return self
+
+    def _read(self):
+        for ln in self.p.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(tmp, rank):
+    from phygas_gb300 import synth
+    seed = SEED + 7919 * rank
+    cp, tp = synth.write_workload(tmp, "screen", N_STARS, seed)
+    return cp, tp
+
+
+def cpu_baseline(cp, tp, stars_per_proc=192, procs=None):
+    """Oracle screen on all host cores: P processes, each `stars_per_proc` stars x all clusters; pairs/s from the
+    per-target loop time (the per-cluster precompute, done once per task by the reference, is timed apart)."""
+    from tests import oracle_tools as ot
+    procs = procs or os.cpu_count() or 1
+    with open(tp) as f:
+        stars = f.readlines()
+    tmp = tempfile.mkdtemp(prefix="phygas_cpu_")
+    inp = os.path.join(tmp, "in")
+    with open(inp, "w") as f:
+        f.write("PHYGAS 1 screen %g %d %g 0\n" % (CHI2_MAX, N_SAMP, R_KERNEL))
+        f.writelines(stars[:stars_per_proc * procs])
+    t0 = time.time()
+    ps = [subprocess.Popen([ot.ORACLE_WU, cp, inp, str(p * stars_per_proc), str((p + 1) * stars_per_proc)],
+                           stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True) for p in range(procs)]
+    runs, preps = [], []
+    for p in ps:
+        err = p.communicate()[1]
+        if p.returncode:
+            raise RuntimeError("oracle_wu failed: " + err[-500:])
+        f = err.split("wu_time")[-1].split()
+        preps.append(float(f[1]))
+        runs.append(float(f[3]))
+    wall = time.time() - t0
+    pairs = stars_per_proc * procs * N_CLUSTERS
+    return {"value": pairs / max(runs), "unit": "pairs/s", "cores": procs, "kind": "port",
+            "sample": "%d stars x %d clusters on %d processes (%d stars each); per-target loop %.1f s, cluster "
+                      "precompute %.1f s per process (excluded), wall %.1f s" % (
+                          stars_per_proc * procs, N_CLUSTERS, procs, stars_per_proc, max(runs), max(preps), wall)}
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from phygas_gb300 import build as B
+    B.build_oracle()
+    with tempfile.TemporaryDirectory() as tmp:
+        cp, tp = make_inputs(tmp, 0)
+        vals = []
+        for i in range(args.warmup + args.steps):
+            r = cpu_baseline(cp, tp, stars_per_proc=32)
+            if i >= args.warmup:
+                vals.append(r)
+        v = statistics.median(x["value"] for x in vals)
+        base = dict(vals[-1])
+        base["value"] = v
+        print(json.dumps({"impl": "reference", "metric": "pairs/s", "value": v, "unit": "pairs/s",
+                          "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": config(args),
+                          "cpu_baseline": base,
+                          "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def config(args):
+    return {"workload": "screen: %d stars x %d clusters (synthetic, seed %d), chi2_max %g, n_samp %d, r_kernel %g"
+                        % (N_STARS, N_CLUSTERS, SEED, CHI2_MAX, N_SAMP, R_KERNEL),
+            "stars": N_STARS, "clusters": N_CLUSTERS, "pairs_per_step": N_STARS * N_CLUSTERS,
+            "l2": "flushed between steps (256 MiB write)", "cluster_table": "resident, built once outside timing",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import numpy as np
+    import torch
+    import phygas_gb300 as pg
+    import __graft_entry__
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    if rank == 0 or ws > 1:
+        __graft_entry__.build()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    tmp = tempfile.mkdtemp(prefix="phygas_bench_")
+    cp, tp = make_inputs(tmp, rank)
+    clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    tmax = max(c.tmax_myr for c in clusters)
+    ctx = pg.Context(local)
+    fp64_peak, fp32_peak = ctx.peaks()
+    t0 = time.time()
+    ctx.set_clusters(clusters, N_SAMP, R_KERNEL)
+    table_s = time.time() - t0
+    ps0, sig, pre = pg.draw_targets(stars, N_SAMP)
+    ctx.stage(ps0, sig, pre)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def run(precision, k, w):
+        for _ in range(w):
+            ctx.exec(tmax, CHI2_MAX, precision)
+        per, stats, rows = [], [], 0
+        barrier()
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize()
+            rows = ctx.exec(tmax, CHI2_MAX, precision)
+            s = ctx.stats()
+            per.append(s["ms_total"])
+            stats.append(s)
+        barrier()
+        return per, stats, rows
+
+    try:
+        run(pg.PGX_MIXED, 0, 1)
+        precision = pg.PGX_MIXED
+    except pg.GpuError as e:
+        log("mixed-precision screen unavailable (%s); timing the FP64 screen as the value" % e)
+        precision = pg.PGX_FP64
+    with Clocks(local) as clk:
+        per, stats, n_rows = run(precision, args.steps, args.warmup)
+    per64, stats64, n_rows64 = run(pg.PGX_FP64, max(2, min(args.steps, 3)), 1)
+    ms = statistics.mean(per)
+    ms64 = statistics.mean(per64)
+    if ws > 1:
+        t = torch.tensor([ms, ms64], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, ms64 = t.tolist()
+    pairs = N_STARS * N_CLUSTERS
+    value = ws * pairs / (ms * 1e-3)
+
+    # end to end through the C-ABI: host records -> host draws -> H2D -> device -> D2H rows
+    e2e_times = []
+    for i in range(max(2, args.steps // 2) + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        a, b, c = pg.draw_targets(stars, N_SAMP)
+        r = ctx.screen(a, b, c, tmax, CHI2_MAX, precision)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = statistics.median(e2e_times[1:])
+    h2d = N_STARS * (6 + 21 + 1) * 8
+    d2h = len(r) * pg.ROW_DTYPE.itemsize + 8
+
+    s = stats[-1]
+    orbit_ms = statistics.mean(x["ms_orbit"] for x in stats)
+    achieved = FLOPS_PER_BODY_STEP * s["body_steps"] / (orbit_ms * 1e-3)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(cp, tp)
+        except Exception as e:          # the baseline is reported, not required
+            log("cpu baseline failed: %s" % e)
+    if rank == 0:
+        out = {
+            "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64+f32" if precision == pg.PGX_MIXED else "f64", "data": "synthetic",
+            "precision": "mixed" if precision == pg.PGX_MIXED else "fp64",
+            "config": config(args),
+            "plain_fp64": {"value": ws * pairs / (ms64 * 1e-3), "unit": "pairs/s", "ms_per_step": ms64,
+                           "speedup_of_value": ms64 / ms},
+            "rows_per_step": n_rows, "rows_fp64": n_rows64,
+            "stages_ms": {k: statistics.mean(x[k] for x in stats) for k in
+                          ("ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish")},
+            "stages_ms_fp64": {k: statistics.mean(x[k] for x in stats64) for k in
+                               ("ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish")},
+            "e2e": {"value": ws * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "s_per_step": e2e_s},
+            "roofline": {"bound": "fp64", "kernel": "k_stm_orbits", "achieved": achieved / 1e12,
+                         "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                         "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
+                         "traffic": ORBIT_TRAFFIC_BYTES, "flops_per_body_step": FLOPS_PER_BODY_STEP,
+                         "body_steps_per_launch": s["body_steps"], "ms_per_launch": orbit_ms},
+            "fp32_peak_tflops": fp32_peak / 1e12,
+            "cluster_table_s": table_s,
+            "gpu_launches": int(sum(x["kernels"] for x in stats)),
+            "clocks": clk.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(out))
+    ctx.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

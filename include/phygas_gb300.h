@@ -1,0 +1,111 @@
+/* phygas_gb300.h -- batched C-ABI of libphygas_gb300 (GB300, sm_103a).
+ *
+ * The reference's per-pair API (phygas.h) cannot feed a GPU: every call is one star, one pair or one clone.  These
+ * entry points take whole chunks and keep their data on the device between stages.  They replace the reference's
+ * GPU backend interface, src/phygas_gpu.h:18-31 (pg_init, pg_alloc/put/get/free, pg_lin, pg_chi2, pg_finish,
+ * pg_pair), and the loops of its host layer that drive it, src/main_phygas_boinc.cpp:59-301 (gpu_screen, gpu_pair).
+ * Plain pointers and sizes only; host buffers in, host buffers out; every call is synchronous on return.
+ *
+ * Status codes: 0 ok; otherwise one of PGX_E_* below, with a message in pgx_last_error().  (The reference backend
+ * returns 0 / 1 with a message on stderr, src/phygas_cuda.cu:16-17.)
+ */
+#ifndef PHYGAS_GB300_H
+#define PHYGAS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include "phygas.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGX_OK 0
+#define PGX_E_ARG 1        /* a size or pointer is invalid */
+#define PGX_E_CUDA 2       /* a CUDA call or kernel failed */
+#define PGX_E_NOMEM 3      /* device memory exhausted */
+#define PGX_E_TIMEOUT 4    /* a bounded device-side wait ran out */
+#define PGX_E_LIMIT 5      /* beyond a documented size limit */
+#define PGX_E_NODEV 6      /* no usable GPU */
+
+#define PGX_FP64 0         /* the plain FP64 screen */
+#define PGX_MIXED 1        /* FP32 screen with FP64 rechecks (identical rows) */
+
+typedef struct PgxContext PgxContext;
+
+/* One device context per GPU: a stream, resident tables and work buffers.  Replaces pg_init
+ * (src/phygas_gpu.h:18).  device < 0 picks device 0. */
+int pgx_open(int device, PgxContext **ctx);
+void pgx_close(PgxContext *ctx);
+const char *pgx_last_error(const PgxContext *ctx);
+void pgx_free(void *p);              /* frees arrays the pgx_* calls return */
+
+/* State-transition tracks (reference lin_integrate, src/phygas.c:286-323; GPU pg_lin, src/phygas_gpu.h:25):
+ * for n objects, nominal phase space ps0[6n], 6x6 initial covariance sig[36n] (row-major), npts[n] points 0.5 Myr
+ * apart.  Outputs are the objects' points back to back (object i starts at point sum(npts[0..i-1])): pos[3*],
+ * vel[3*], S[6*] (xx xy xz yy yz zz). */
+int pgx_lin(PgxContext *ctx, int n, const double *ps0, const double *sig, const int *npts, double *pos, double *vel,
+            double *S);
+
+/* ---- stage-1 screen -------------------------------------------------------------------------------------------- */
+/* A kept pair (chi2 < chi2_max), in (star, cluster) order: the columns of the reference's rows
+ * (src/phygas_screen.c:60-61) plus the argmin point kb and segment fraction sb. */
+typedef struct {
+    int star, cluster, kb, pad;
+    double sb, chi2, t_myr, d_nom_pc, sig_pc, p_r50, p_rtot, vrel_kms;
+} PgxScreenRow;
+
+/* Resident cluster table: nominal orbit + 6 neighbours of each cluster integrated on the device (reference
+ * ph_lin_cluster, src/phygas.c:336-344); ps0/sig as in pgx_lin, tmax_myr sets each track's length; names (40 bytes
+ * each, NUL-terminated) seed the pairs' draws; r_kernel as ph_screen_r (0 = rtot). */
+int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double *sig, const double *tmax_myr,
+                        const double *r50_pc, const double *rtot_pc, const char *names, double r_kernel);
+
+/* Screen nt stars against the resident cluster table (reference ph_lin_target + ph_screen_chi2_cut +
+ * ph_screen_finish over every pair, src/phygas_screen.c:50-62; GPU pg_lin + pg_chi2 + pg_finish).
+ * ps0/sig as in pgx_lin; seed_prefix[i] = FNV-1a state after "id|" of star i (pgx_seed_prefix), so a pair's seed is
+ * ph_seed(id, cluster name); tmax_myr = the star tracks' length (the reference uses the longest cluster tmax).
+ * Returns a malloc'ed array of *n_rows rows (free with pgx_free). */
+int pgx_screen(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *seed_prefix,
+               double tmax_myr, double chi2_max, int precision, PgxScreenRow **rows, long *n_rows);
+
+/* The same in three steps, for callers that time the device part alone: stage (host -> device), exec (device
+ * only; returns the kept-pair count), fetch (device -> host, n rows into a caller buffer). */
+int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *seed_prefix);
+int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double chi2_max, int precision, long *n_rows);
+int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n);
+
+/* Host draws for the records API (reference ph_lin_target_init / the draws of ph_lin_cluster, src/phygas.c:274-344,
+ * seeds ph_seed("lin", id)), on `threads` host threads (<= 0: all cores). */
+int pgx_draw_targets(const PhTarget *t, int n, int n_samp, int threads, double *ps0, double *sig,
+                     uint64_t *seed_prefix);
+int pgx_draw_clusters(const PhCluster *c, int n, int n_samp, int threads, double *ps0, double *sig);
+uint64_t pgx_seed_prefix(const char *target_id);
+
+/* ---- pair Monte Carlo ------------------------------------------------------------------------------------------ */
+/* Trace every clone of n_pairs pairs back and reduce each pair (reference ph_pair_clone + ph_pair_reduce,
+ * src/phygas.c:200-238; GPU pg_pair + the host reduction of src/main_phygas_boinc.cpp:236-246).
+ * Clones of pair p are clone_off[p] .. clone_off[p+1]-1 (clone_off[n_pairs] = total, at most 1024 x 16 per pair);
+ * ps = 12 doubles per clone as ph_pair_draw writes them; steps/dt per pair as ph_pair_draw returns them;
+ * r50_pc/rtot_pc per pair.  res[n_pairs] gets the results; clone_out (NULL or 3 x total: best kpc, tbest Myr,
+ * vbest kpc/Myr, clone-major blocks) the per-clone closest approaches. */
+int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,
+             const double *dt, const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out);
+
+/* ---- measurement ------------------------------------------------------------------------------------------------ */
+/* Device times (CUDA events on the context's stream) and counts of the last pgx_screen_exec / pgx_pair call. */
+typedef struct {
+    double ms_total, ms_orbit, ms_cov, ms_scan, ms_select, ms_finish, ms_pair;
+    long pairs, kept, candidates, rechecked_points, rechecked_draws, clones, clone_steps, body_steps;
+    int kernels;                     /* kernel launches of the call */
+} PgxStats;
+int pgx_stats(const PgxContext *ctx, PgxStats *out);
+
+/* Measured peak FMA rates of this GPU, in FLOP/s (2 per fused multiply-add): the roofline denominators of the
+ * FP64-bound orbit stages and the FP32-bound filter.  Runs two short probe kernels (about 20 ms). */
+int pgx_peaks(PgxContext *ctx, double *fp64_flops, double *fp32_flops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -8,12 +8,21 @@
  *   in: line 1 "PHYGAS 1 screen <chi2_max> <n_samp> <r_kernel> <p_min>" or "PHYGAS 1 pair <n_clones> <dt_myr>",
  *       then one target per line (14 fields, optionally "clusters=NAME,...").
  *   Rows of targets [j0,j1) against clusters [i0,i1), in (target, cluster) order.  No "# done" line.
+ *   stderr: "wu_time prep <s> run <s>" -- the per-cluster precompute and the per-target loop, timed apart.
  */
+#define _POSIX_C_SOURCE 199309L
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include "phygas.h"
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + ts.tv_nsec * 1e-9;
+}
 
 static int listed(const char *name, const char *list) {
     size_t n = strlen(name);
@@ -69,10 +78,13 @@ int main(int argc, char **argv) {
     if (i1 > nc) i1 = nc;
     double tmax = 0;
     for (int i = 0; i < nc; i++) if (cl[i].tmax_myr > tmax) tmax = cl[i].tmax_myr;
+    double t_prep = 0, t_run = 0, t0 = now_s();
     if (!strcmp(mode, "screen")) {
         ph_screen_r = p3 > 0 ? p3 : 2.0;
         PhLin *cin = calloc(nc, sizeof(PhLin));
         for (int i = i0; i < i1; i++) ph_lin_cluster(&cl[i], (int)p2, ph_seed("lin", cl[i].name), &cin[i]);
+        t_prep = now_s() - t0;
+        t0 = now_s();
         for (int j = j0; j < j1; j++) {
             PhLin tl;
             ph_lin_target(&tg[j], tmax, (int)p2, ph_seed("lin", tg[j].id), &tl);
@@ -91,6 +103,8 @@ int main(int argc, char **argv) {
     } else if (!strcmp(mode, "pair")) {
         PhTrack *ctr = calloc(nc, sizeof(PhTrack));
         for (int i = i0; i < i1; i++) ph_track_cluster(&cl[i], 32, ph_seed("track", cl[i].name), &ctr[i]);
+        t_prep = now_s() - t0;
+        t0 = now_s();
         for (int j = j0; j < j1; j++) {
             PhTrack tt;
             ph_track_target(&tg[j], tmax, 32, ph_seed("track", tg[j].id), &tt);
@@ -108,5 +122,8 @@ int main(int argc, char **argv) {
         fprintf(stderr, "unknown mode %s\n", mode);
         return 1;
     }
+    t_run = now_s() - t0;
+    fflush(stdout);
+    fprintf(stderr, "wu_time prep %.6f run %.6f\n", t_prep, t_run);
     return 0;
 }

@@ -1,0 +1,285 @@
+"""phygas_gb300 -- Python access to libphygas_gb300 (the GB300 implementation of Phygas's screen and pair paths).
+
+The product is the C library and its two CLIs (phygas_screen, phygas_cli) under phygas_gb300/_lib; this module only
+binds the C-ABI (include/phygas.h, include/phygas_gb300.h) with ctypes for tests, benchmarks and Python callers.
+There is no Python or CPU fallback of the GPU stages: without the built library every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_DIR = os.path.join(HERE, "_lib")
+LIB_PATH = os.path.join(LIB_DIR, "libphygas_gb300.so")
+SCREEN_CLI = os.path.join(LIB_DIR, "phygas_screen")
+PAIR_CLI = os.path.join(LIB_DIR, "phygas_cli")
+
+PGX_FP64, PGX_MIXED = 0, 1
+ERRORS = {1: "bad argument", 2: "CUDA error", 3: "out of device memory", 4: "device wait timed out",
+          5: "size limit", 6: "no usable GPU"}
+
+
+class PhCluster(C.Structure):
+    _fields_ = [("name", C.c_char * 40), ("kind", C.c_char), ("ra", C.c_double), ("dec", C.c_double),
+                ("dist_pc", C.c_double), ("e_dist_pc", C.c_double), ("pmra", C.c_double), ("e_pmra", C.c_double),
+                ("pmdec", C.c_double), ("e_pmdec", C.c_double), ("rv", C.c_double), ("e_rv", C.c_double),
+                ("has_rv", C.c_int), ("r50_pc", C.c_double), ("rtot_pc", C.c_double), ("age16", C.c_double),
+                ("age50", C.c_double), ("age84", C.c_double), ("tmax_myr", C.c_double)]
+
+
+class PhTarget(C.Structure):
+    _fields_ = [("id", C.c_char * 40), ("kind", C.c_char), ("ra", C.c_double), ("dec", C.c_double),
+                ("plx", C.c_double), ("e_plx", C.c_double), ("dist_pc", C.c_double), ("e_lndist", C.c_double),
+                ("pmra", C.c_double), ("e_pmra", C.c_double), ("pmdec", C.c_double), ("e_pmdec", C.c_double),
+                ("rv", C.c_double), ("e_rv", C.c_double), ("has_rv", C.c_int)]
+
+
+class PhResult(C.Structure):
+    _fields_ = [("n", C.c_int)] + [(k, C.c_double) for k in (
+        "d05", "d50", "d95", "t05", "t50", "t95", "v05", "v50", "v95", "f_r50", "f_rtot")]
+
+
+class PgxScreenRow(C.Structure):
+    _fields_ = [("star", C.c_int), ("cluster", C.c_int), ("kb", C.c_int), ("pad", C.c_int)] + [
+        (k, C.c_double) for k in ("sb", "chi2", "t_myr", "d_nom_pc", "sig_pc", "p_r50", "p_rtot", "vrel_kms")]
+
+
+class PgxStats(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("ms_total", "ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish",
+                                          "ms_pair")] + [
+        (k, C.c_long) for k in ("pairs", "kept", "candidates", "rechecked_points", "rechecked_draws", "clones",
+                                "clone_steps", "body_steps")] + [("kernels", C.c_int)]
+
+
+ROW_DTYPE = np.dtype([("star", "i4"), ("cluster", "i4"), ("kb", "i4"), ("pad", "i4"), ("sb", "f8"), ("chi2", "f8"),
+                      ("t_myr", "f8"), ("d_nom_pc", "f8"), ("sig_pc", "f8"), ("p_r50", "f8"), ("p_rtot", "f8"),
+                      ("vrel_kms", "f8")])
+RESULT_DTYPE = np.dtype({"names": ["n", "d05", "d50", "d95", "t05", "t50", "t95", "v05", "v50", "v95", "f_r50",
+                                   "f_rtot"],
+                         "formats": ["i4"] + ["f8"] * 11, "offsets": [0] + [8 + 8 * i for i in range(11)],
+                         "itemsize": 96})
+
+_P = C.POINTER
+_D = _P(C.c_double)
+_I = _P(C.c_int)
+_U64 = _P(C.c_uint64)
+
+# (name, restype, argtypes) of every C-ABI entry point bound here
+SIGNATURES = [
+    ("pgx_open", C.c_int, [C.c_int, _P(C.c_void_p)]),
+    ("pgx_close", None, [C.c_void_p]),
+    ("pgx_last_error", C.c_char_p, [C.c_void_p]),
+    ("pgx_free", None, [C.c_void_p]),
+    ("pgx_lin", C.c_int, [C.c_void_p, C.c_int, _D, _D, _I, _D, _D, _D]),
+    ("pgx_screen_clusters", C.c_int, [C.c_void_p, C.c_int, _D, _D, _D, _D, _D, C.c_char_p, C.c_double]),
+    ("pgx_screen", C.c_int, [C.c_void_p, C.c_int, _D, _D, _U64, C.c_double, C.c_double, C.c_int,
+                             _P(_P(PgxScreenRow)), _P(C.c_long)]),
+    ("pgx_screen_stage", C.c_int, [C.c_void_p, C.c_int, _D, _D, _U64]),
+    ("pgx_screen_exec", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _P(C.c_long)]),
+    ("pgx_screen_fetch", C.c_int, [C.c_void_p, C.c_void_p, C.c_long]),
+    ("pgx_draw_targets", C.c_int, [_P(PhTarget), C.c_int, C.c_int, C.c_int, _D, _D, _U64]),
+    ("pgx_draw_clusters", C.c_int, [_P(PhCluster), C.c_int, C.c_int, C.c_int, _D, _D]),
+    ("pgx_seed_prefix", C.c_uint64, [C.c_char_p]),
+    ("pgx_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, C.c_void_p, _D]),
+    ("pgx_stats", C.c_int, [C.c_void_p, _P(PgxStats)]),
+    ("pgx_peaks", C.c_int, [C.c_void_p, _D, _D]),
+    ("ph_init", None, []),
+    ("ph_seed", C.c_uint64, [C.c_char_p, C.c_char_p]),
+    ("ph_read_clusters", C.c_int, [C.c_char_p, _P(_P(PhCluster))]),
+    ("ph_read_targets", C.c_int, [C.c_char_p, _P(_P(PhTarget))]),
+    ("ph_pair_draw", C.c_int, [_P(PhTarget), _P(PhCluster), C.c_int, C.c_double, C.c_uint64, _D, _I, _D]),
+    ("ph_lin_target_init", None, [_P(PhTarget), C.c_int, C.c_uint64, _D, _D]),
+]
+
+_lib = None
+
+
+def lib():
+    """The loaded library; raises if it has not been built (phygas_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libphygas_gb300.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        L.ph_init()
+        _lib = L
+    return _lib
+
+
+def _ptr(a, t=C.c_double):
+    return a.ctypes.data_as(_P(t))
+
+
+class GpuError(RuntimeError):
+    pass
+
+
+def read_clusters(path):
+    p = _P(PhCluster)()
+    n = lib().ph_read_clusters(path.encode(), C.byref(p))
+    if n < 0:
+        raise OSError("can't read " + path)
+    return (PhCluster * n).from_address(C.addressof(p.contents)) if n else (PhCluster * 0)()
+
+
+def read_targets(path):
+    p = _P(PhTarget)()
+    n = lib().ph_read_targets(path.encode(), C.byref(p))
+    if n < 0:
+        raise OSError("can't read " + path)
+    return (PhTarget * n).from_address(C.addressof(p.contents)) if n else (PhTarget * 0)()
+
+
+def as_array(seq, T):
+    """A ctypes array of records T from any sequence of T (ctypes slices are lists)."""
+    if isinstance(seq, C.Array) and seq._type_ is T:
+        return seq
+    return (T * len(seq))(*seq)
+
+
+def draw_targets(targets, n_samp=64, threads=0):
+    targets = as_array(targets, PhTarget)
+    n = len(targets)
+    ps0, sig, pre = np.zeros((n, 6)), np.zeros((n, 36)), np.zeros(n, np.uint64)
+    rc = lib().pgx_draw_targets(targets, n, n_samp, threads, _ptr(ps0), _ptr(sig), _ptr(pre, C.c_uint64))
+    if rc:
+        raise ValueError("pgx_draw_targets: %d" % rc)
+    return ps0, sig, pre
+
+
+def draw_clusters(clusters, n_samp=64, threads=0):
+    clusters = as_array(clusters, PhCluster)
+    n = len(clusters)
+    ps0, sig = np.zeros((n, 6)), np.zeros((n, 36))
+    rc = lib().pgx_draw_clusters(clusters, n, n_samp, threads, _ptr(ps0), _ptr(sig))
+    if rc:
+        raise ValueError("pgx_draw_clusters: %d" % rc)
+    return ps0, sig
+
+
+class Context:
+    """One GPU context (pgx_open).  Methods mirror the C-ABI; arrays are numpy."""
+
+    def __init__(self, device=0):
+        self.h = C.c_void_p()
+        rc = lib().pgx_open(device, C.byref(self.h))
+        if rc:
+            raise GpuError("pgx_open: %s" % ERRORS.get(rc, rc))
+
+    def close(self):
+        if self.h:
+            lib().pgx_close(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc:
+            raise GpuError("%s: %s: %s" % (what, ERRORS.get(rc, rc), lib().pgx_last_error(self.h).decode()))
+
+    def stats(self):
+        s = PgxStats()
+        self._check(lib().pgx_stats(self.h, C.byref(s)), "pgx_stats")
+        return {k: getattr(s, k) for k, _ in PgxStats._fields_}
+
+    def peaks(self):
+        """(FP64, FP32) FMA peaks of this GPU in FLOP/s, measured now by the library's probe kernels."""
+        a, b = C.c_double(), C.c_double()
+        self._check(lib().pgx_peaks(self.h, C.byref(a), C.byref(b)), "pgx_peaks")
+        return a.value, b.value
+
+    def lin(self, ps0, sig, npts):
+        ps0 = np.ascontiguousarray(ps0, np.float64)
+        sig = np.ascontiguousarray(sig, np.float64)
+        npts = np.ascontiguousarray(npts, np.int32)
+        tot = int(npts.sum())
+        pos, vel, S = np.zeros((tot, 3)), np.zeros((tot, 3)), np.zeros((tot, 6))
+        self._check(lib().pgx_lin(self.h, len(npts), _ptr(ps0), _ptr(sig), _ptr(npts, C.c_int), _ptr(pos),
+                                  _ptr(vel), _ptr(S)), "pgx_lin")
+        return pos, vel, S
+
+    def set_clusters(self, clusters, n_samp=64, r_kernel=2.0, draws=None):
+        clusters = as_array(clusters, PhCluster)
+        ps0, sig = draws if draws is not None else draw_clusters(clusters, n_samp)
+        n = len(clusters)
+        tmax = np.array([c.tmax_myr for c in clusters])
+        r50 = np.array([c.r50_pc for c in clusters])
+        rt = np.array([c.rtot_pc for c in clusters])
+        names = b"".join(bytes(c.name).ljust(40, b"\0")[:40] for c in clusters)
+        self._check(lib().pgx_screen_clusters(self.h, n, _ptr(np.ascontiguousarray(ps0)),
+                                              _ptr(np.ascontiguousarray(sig)), _ptr(tmax), _ptr(r50), _ptr(rt),
+                                              names, r_kernel), "pgx_screen_clusters")
+
+    def screen(self, ps0, sig, prefix, tmax, chi2_max=25.0, precision=PGX_MIXED):
+        rows = _P(PgxScreenRow)()
+        n = C.c_long()
+        ps0 = np.ascontiguousarray(ps0, np.float64)
+        sig = np.ascontiguousarray(sig, np.float64)
+        prefix = np.ascontiguousarray(prefix, np.uint64)
+        self._check(lib().pgx_screen(self.h, len(prefix), _ptr(ps0), _ptr(sig), _ptr(prefix, C.c_uint64), tmax,
+                                     chi2_max, precision, C.byref(rows), C.byref(n)), "pgx_screen")
+        out = np.zeros(n.value, ROW_DTYPE)
+        if n.value:
+            C.memmove(out.ctypes.data, rows, n.value * ROW_DTYPE.itemsize)
+        lib().pgx_free(rows)
+        return out
+
+    def stage(self, ps0, sig, prefix):
+        self._keep = (np.ascontiguousarray(ps0, np.float64), np.ascontiguousarray(sig, np.float64),
+                      np.ascontiguousarray(prefix, np.uint64))
+        p, s, q = self._keep
+        self._check(lib().pgx_screen_stage(self.h, len(q), _ptr(p), _ptr(s), _ptr(q, C.c_uint64)), "stage")
+
+    def exec(self, tmax, chi2_max=25.0, precision=PGX_MIXED):
+        n = C.c_long()
+        self._check(lib().pgx_screen_exec(self.h, tmax, chi2_max, precision, C.byref(n)), "exec")
+        return n.value
+
+    def fetch(self, n):
+        out = np.zeros(n, ROW_DTYPE)
+        self._check(lib().pgx_screen_fetch(self.h, out.ctypes.data, n), "fetch")
+        return out
+
+    def pair(self, clone_off, ps, steps, dt, r50_pc, rtot_pc, want_clones=False):
+        clone_off = np.ascontiguousarray(clone_off, np.int32)
+        ps = np.ascontiguousarray(ps, np.float64)
+        steps = np.ascontiguousarray(steps, np.int32)
+        dt = np.ascontiguousarray(dt, np.float64)
+        r50 = np.ascontiguousarray(r50_pc, np.float64)
+        rt = np.ascontiguousarray(rtot_pc, np.float64)
+        npairs = len(steps)
+        res = np.zeros(npairs, RESULT_DTYPE)
+        clones = np.zeros((3, int(clone_off[-1]))) if want_clones else None
+        self._check(lib().pgx_pair(self.h, npairs, _ptr(clone_off, C.c_int), _ptr(ps), _ptr(steps, C.c_int),
+                                   _ptr(dt), _ptr(r50), _ptr(rt), res.ctypes.data,
+                                   _ptr(clones) if want_clones else None), "pgx_pair")
+        return (res, clones) if want_clones else res
+
+
+def pair_draws(targets, clusters, pairs, n_clones, dt_myr=0.05):
+    """Host draws of ph_pair for a list of (target index, cluster index): clone_off, ps, steps, dt, r50, rtot."""
+    L = lib()
+    offs, chunks, steps, dts = [0], [], [], []
+    buf = np.zeros(12 * max(n_clones, 1))
+    st, dtv = C.c_int(), C.c_double()
+    for j, i in pairs:
+        t, c = targets[j], clusters[i]
+        seed = L.ph_seed(t.id, c.name)
+        m = L.ph_pair_draw(C.byref(t), C.byref(c), n_clones, dt_myr, seed, _ptr(buf), C.byref(st), C.byref(dtv))
+        chunks.append(buf[:12 * m].copy())
+        offs.append(offs[-1] + m)
+        steps.append(st.value)
+        dts.append(dtv.value)
+    ps = np.concatenate(chunks) if chunks else np.zeros(0)
+    r50 = np.array([clusters[i].r50_pc for _, i in pairs])
+    rt = np.array([clusters[i].rtot_pc for _, i in pairs])
+    return np.array(offs, np.int32), ps, np.array(steps, np.int32), np.array(dts), r50, rt

@@ -1,0 +1,792 @@
+// pgx_api.cu -- the C-ABI of libphygas_gb300 (include/phygas_gb300.h) and the GPU half of the drop-in API
+// (include/phygas.h): device context, resident tables, work buffers, and the stage sequences.
+//
+// Stage sequence of one screen chunk (all on the context's stream, no host round trip before the kept-pair count):
+//   k_stm_orbits -> k_stm_cov -> k_scan64 -> k_count_kept -> k_exclusive_scan -> [count to host] -> k_emit_kept
+//   -> k_finish_prep -> k_finish64            (the FP64 path; the mixed path replaces scan..finish, pgx_mixed.cu)
+// Pair Monte Carlo: one persistent k_pair_mc launch over a longest-first queue (+ k_pair_reduce_big).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "phygas_gb300.h"
+#include "pgx_kernels.h"
+#include "pgx_mixed.h"
+#include "../host/ph_host.h"
+
+static_assert(sizeof(pgx::PhResultDev) == sizeof(PhResult), "PhResult layout");
+static_assert(sizeof(pgx::ScreenRowDev) == sizeof(PgxScreenRow), "PgxScreenRow layout");
+
+namespace {
+
+struct Buf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+enum { EV_START, EV_ORBIT, EV_COV, EV_SCAN, EV_SELECT, EV_FINISH, EV_PAIR0, EV_PAIR1, EV_N };
+
+}  // namespace
+
+struct PgxContext {
+    int device = 0, sms = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[EV_N] = {};
+    std::string err;
+    // resident cluster table (original cluster order)
+    int nc = 0, ncp = 0;
+    Buf c64, c32, cn, cR2, cr50, crt, cname;
+    // the staged star chunk and the screen's work buffers
+    int nt = 0;
+    Buf s_ps0, s_sig21, s_prefix;
+    Buf opos, ovel, t64, t32;
+    Buf chi2T, kbT, sbT, cnt, off, total, kept, fin, rows;
+    pgx::MixedBufs mixed;
+    long n_rows = 0;
+    // pair Monte Carlo
+    Buf p_off, p_ps, p_steps, p_dt, p_r50, p_rt, p_items, p_q, p_done, p_cres, p_res;
+    // one-object helpers of the drop-in API
+    Buf x_ps0, x_sig21, x_npts, x_opos, x_ovel, x_t64, x_t32;
+    PgxStats stats = {};
+};
+
+namespace {
+
+int fail(PgxContext *c, int code, const char *fmt, ...) {
+    char b[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b, sizeof b, fmt, ap);
+    va_end(ap);
+    if (c) c->err = b;
+    return code;
+}
+
+#define CK(call)                                                                                             \
+    do {                                                                                                     \
+        cudaError_t e_ = (call);                                                                             \
+        if (e_ != cudaSuccess)                                                                               \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? PGX_E_NOMEM : PGX_E_CUDA, "%s: %s (%s:%d)", #call, \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                                         \
+    } while (0)
+#define CKL() CK(cudaGetLastError())
+#define RET(x)                  \
+    do {                        \
+        int r_ = (x);           \
+        if (r_) return r_;      \
+    } while (0)
+#define MRET(x)                                 \
+    do {                                        \
+        int r_ = (x);                           \
+        if (r_) {                               \
+            ctx->err = ctx->mixed.err;          \
+            return r_;                          \
+        }                                       \
+    } while (0)
+
+int ensure(PgxContext *ctx, Buf &b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.cap >= bytes) return 0;
+    if (b.p) CK(cudaFree(b.p));
+    b.p = nullptr;
+    b.cap = 0;
+    const size_t want = bytes + bytes / 4;
+    CK(cudaMalloc(&b.p, want));
+    b.cap = want;
+    return 0;
+}
+
+template <class T> T *P(Buf &b) { return reinterpret_cast<T *>(b.p); }
+
+int npts_of(double tmax) { return (int)std::ceil(tmax / PH_PRE_STEP_MYR) + 1; }
+
+// ps0 [n][6] -> [6][n]; sig [n][36] -> the 21 upper-triangle entries [21][n]
+void to_soa(int n, const double *ps0, const double *sig, std::vector<double> &p6, std::vector<double> &s21,
+            const int *order = nullptr) {
+    p6.resize((size_t)6 * n);
+    s21.resize((size_t)21 * n);
+    for (int slot = 0; slot < n; slot++) {
+        const int i = order ? order[slot] : slot;
+        for (int c = 0; c < 6; c++) p6[(size_t)c * n + slot] = ps0[(size_t)6 * i + c];
+        int q = 0;
+        for (int a = 0; a < 6; a++)
+            for (int b = a; b < 6; b++) s21[(size_t)q++ * n + slot] = sig[(size_t)36 * i + 6 * a + b];
+    }
+}
+
+// nominal + neighbour orbits of N objects (ps0 / sig21 device SoA, npts per slot or uniform) into t64 / t32
+int run_lin(PgxContext *ctx, int N, const double *d_ps0, const double *d_sig21, const int *d_npts, int nmax,
+            Buf &opos, Buf &ovel, double *t64, float4 *t32, bool timed) {
+    RET(ensure(ctx, opos, (size_t)nmax * 21 * N * sizeof(double)));
+    RET(ensure(ctx, ovel, (size_t)nmax * 3 * N * sizeof(double)));
+    dim3 g((N + 127) / 128, 7);
+    pgx::k_stm_orbits<<<g, 128, 0, ctx->st>>>(N, d_ps0, d_npts, nmax, P<double>(opos), P<double>(ovel));
+    CKL();
+    if (timed) CK(cudaEventRecord(ctx->ev[EV_ORBIT], ctx->st));
+    const size_t work = (size_t)N * nmax;
+    pgx::k_stm_cov<<<(unsigned)((work + 255) / 256), 256, 0, ctx->st>>>(N, nmax, d_npts, P<double>(opos),
+                                                                         P<double>(ovel), d_sig21, t64, t32);
+    CKL();
+    if (timed) CK(cudaEventRecord(ctx->ev[EV_COV], ctx->st));
+    ctx->stats.kernels += 2;
+    return 0;
+}
+
+pgx::ScreenTables tables(PgxContext *ctx, int ns) {
+    pgx::ScreenTables T;
+    T.nt = ctx->nt; T.ns = ns; T.nc = ctx->nc; T.ncp = ctx->ncp;
+    T.t64 = P<double>(ctx->t64); T.t32 = P<float4>(ctx->t32); T.seed_prefix = P<uint64_t>(ctx->s_prefix);
+    T.c64 = P<double>(ctx->c64); T.c32 = P<float4>(ctx->c32); T.cn = P<int>(ctx->cn);
+    T.R2 = P<double>(ctx->cR2); T.r50 = P<double>(ctx->cr50); T.rtot = P<double>(ctx->crt);
+    T.cname = P<char>(ctx->cname);
+    return T;
+}
+
+float elapsed(PgxContext *ctx, int a, int b) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]) != cudaSuccess) return 0.f;
+    return ms;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------------------------
+extern "C" {
+
+int pgx_open(int device, PgxContext **out) {
+    PgxContext *ctx = nullptr;
+    if (!out) return PGX_E_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return PGX_E_NODEV;
+    if (device < 0) device = 0;
+    if (device >= n) return PGX_E_ARG;
+    ctx = new PgxContext();
+    ctx->device = device;
+    int rc = 0;
+    {
+        auto init = [&]() -> int {
+            CK(cudaSetDevice(device));
+            CK(cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device));
+            CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+            for (auto &e : ctx->ev) CK(cudaEventCreate(&e));
+            return 0;
+        };
+        rc = init();
+    }
+    if (rc) {
+        pgx_close(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return 0;
+}
+
+void pgx_close(PgxContext *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    Buf *bufs[] = {&ctx->c64, &ctx->c32, &ctx->cn, &ctx->cR2, &ctx->cr50, &ctx->crt, &ctx->cname, &ctx->s_ps0,
+                   &ctx->s_sig21, &ctx->s_prefix, &ctx->opos, &ctx->ovel, &ctx->t64, &ctx->t32, &ctx->chi2T,
+                   &ctx->kbT, &ctx->sbT, &ctx->cnt, &ctx->off, &ctx->total, &ctx->kept, &ctx->fin, &ctx->rows,
+                   &ctx->p_off, &ctx->p_ps, &ctx->p_steps, &ctx->p_dt, &ctx->p_r50, &ctx->p_rt, &ctx->p_items,
+                   &ctx->p_q, &ctx->p_done, &ctx->p_cres, &ctx->p_res, &ctx->x_ps0, &ctx->x_sig21, &ctx->x_npts,
+                   &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32};
+    for (Buf *b : bufs)
+        if (b->p) cudaFree(b->p);
+    pgx::mixed_free(ctx->mixed);
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+}
+
+const char *pgx_last_error(const PgxContext *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+void pgx_free(void *p) { free(p); }
+
+uint64_t pgx_seed_prefix(const char *id) { return pgh_seed_prefix(id); }
+
+int pgx_draw_targets(const PhTarget *t, int n, int n_samp, int threads, double *ps0, double *sig, uint64_t *prefix) {
+    if (n < 0 || (n > 0 && (!t || !ps0 || !sig)) || n_samp < 0) return PGX_E_ARG;
+    pgh_draw_targets(t, n, n_samp, threads > 0 ? threads : pgh_default_threads(), ps0, sig, prefix);
+    return 0;
+}
+
+int pgx_draw_clusters(const PhCluster *c, int n, int n_samp, int threads, double *ps0, double *sig) {
+    if (n < 0 || (n > 0 && (!c || !ps0 || !sig)) || n_samp < 0) return PGX_E_ARG;
+    pgh_draw_clusters(c, n, n_samp, threads > 0 ? threads : pgh_default_threads(), ps0, sig);
+    return 0;
+}
+
+int pgx_stats(const PgxContext *ctx, PgxStats *out) {
+    if (!ctx || !out) return PGX_E_ARG;
+    *out = ctx->stats;
+    return 0;
+}
+
+int pgx_peaks(PgxContext *ctx, double *fp64, double *fp32) {
+    if (!ctx || !fp64 || !fp32) return PGX_E_ARG;
+    CK(cudaSetDevice(ctx->device));
+    const int blocks = ctx->sms * 8, threads = 256;
+    RET(ensure(ctx, ctx->x_opos, (size_t)blocks * threads * 8));
+    const int it64 = 2000, it32 = 32000;
+    for (int rep = 0; rep < 2; rep++) {      // the first round warms up
+        CK(cudaEventRecord(ctx->ev[EV_PAIR0], ctx->st));
+        pgx::k_peak_dfma<<<blocks, threads, 0, ctx->st>>>(P<double>(ctx->x_opos), it64, 1.0000001, 1e-9);
+        CKL();
+        CK(cudaEventRecord(ctx->ev[EV_PAIR1], ctx->st));
+        pgx::k_peak_ffma<<<blocks, threads, 0, ctx->st>>>(P<float>(ctx->x_opos), it32, 1.0000001f, 1e-9f);
+        CKL();
+        CK(cudaEventRecord(ctx->ev[EV_START], ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    }
+    const double n = (double)blocks * threads * 8 * 2;
+    *fp64 = n * it64 / (elapsed(ctx, EV_PAIR0, EV_PAIR1) * 1e-3);
+    *fp32 = n * it32 / (elapsed(ctx, EV_PAIR1, EV_START) * 1e-3);
+    return 0;
+}
+
+int pgx_lin(PgxContext *ctx, int n, const double *ps0, const double *sig, const int *npts, double *pos, double *vel,
+            double *S) {
+    if (!ctx) return PGX_E_ARG;
+    if (n < 0 || (n > 0 && (!ps0 || !sig || !npts || !pos || !vel || !S))) return fail(ctx, PGX_E_ARG, "pgx_lin: bad args");
+    if (n == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    int nmax = 0;
+    for (int i = 0; i < n; i++) {
+        if (npts[i] < 1) return fail(ctx, PGX_E_ARG, "pgx_lin: npts[%d] = %d", i, npts[i]);
+        nmax = std::max(nmax, npts[i]);
+    }
+    std::vector<double> p6, s21;
+    to_soa(n, ps0, sig, p6, s21);
+    RET(ensure(ctx, ctx->x_ps0, p6.size() * 8));
+    RET(ensure(ctx, ctx->x_sig21, s21.size() * 8));
+    RET(ensure(ctx, ctx->x_npts, (size_t)n * 4));
+    RET(ensure(ctx, ctx->x_t64, (size_t)nmax * 12 * n * 8));
+    RET(ensure(ctx, ctx->x_t32, (size_t)nmax * 3 * n * 16));
+    CK(cudaMemcpyAsync(ctx->x_ps0.p, p6.data(), p6.size() * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->x_sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->x_npts.p, npts, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->st));
+    ctx->stats = PgxStats();
+    RET(run_lin(ctx, n, P<double>(ctx->x_ps0), P<double>(ctx->x_sig21), P<int>(ctx->x_npts), nmax, ctx->x_opos,
+                ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), false));
+    std::vector<double> t((size_t)nmax * 12 * n);
+    CK(cudaMemcpyAsync(t.data(), ctx->x_t64.p, t.size() * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    size_t o = 0;
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < npts[i]; k++, o++) {
+            const double *T = t.data() + (size_t)k * 12 * n + i;
+            for (int c = 0; c < 3; c++) pos[3 * o + c] = T[(size_t)c * n];
+            for (int c = 0; c < 3; c++) vel[3 * o + c] = T[(size_t)(3 + c) * n];
+            for (int c = 0; c < 6; c++) S[6 * o + c] = T[(size_t)(6 + c) * n];
+        }
+    return 0;
+}
+
+int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double *sig, const double *tmax_myr,
+                        const double *r50_pc, const double *rtot_pc, const char *names, double r_kernel) {
+    if (!ctx) return PGX_E_ARG;
+    if (nc <= 0 || !ps0 || !sig || !tmax_myr || !r50_pc || !rtot_pc || !names)
+        return fail(ctx, PGX_E_ARG, "pgx_screen_clusters: bad args");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<int> npts(nc), order(nc), col(nc);
+    int nmax = 0;
+    for (int i = 0; i < nc; i++) {
+        npts[i] = npts_of(tmax_myr[i]);
+        if (npts[i] < 1) return fail(ctx, PGX_E_ARG, "pgx_screen_clusters: tmax %g", tmax_myr[i]);
+        nmax = std::max(nmax, npts[i]);
+        order[i] = i;
+    }
+    // integrate longest first, so the lanes of a warp carry tracks of similar length
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return npts[a] > npts[b]; });
+    std::vector<int> npts_slot(nc);
+    for (int s = 0; s < nc; s++) npts_slot[s] = npts[order[s]];
+    std::vector<double> p6, s21;
+    to_soa(nc, ps0, sig, p6, s21, order.data());
+    RET(ensure(ctx, ctx->x_ps0, p6.size() * 8));
+    RET(ensure(ctx, ctx->x_sig21, s21.size() * 8));
+    RET(ensure(ctx, ctx->x_npts, (size_t)nc * 4));
+    RET(ensure(ctx, ctx->x_t64, (size_t)nmax * 12 * nc * 8));
+    RET(ensure(ctx, ctx->x_t32, (size_t)nmax * 3 * nc * 16));
+    RET(ensure(ctx, ctx->c64, (size_t)nmax * 12 * nc * 8));
+    RET(ensure(ctx, ctx->c32, (size_t)nmax * 3 * nc * 16));
+    RET(ensure(ctx, ctx->cn, (size_t)nc * 4));
+    RET(ensure(ctx, ctx->cR2, (size_t)nc * 8));
+    RET(ensure(ctx, ctx->cr50, (size_t)nc * 8));
+    RET(ensure(ctx, ctx->crt, (size_t)nc * 8));
+    RET(ensure(ctx, ctx->cname, (size_t)nc * 40));
+    CK(cudaMemcpyAsync(ctx->x_ps0.p, p6.data(), p6.size() * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->x_sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->x_npts.p, npts_slot.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, ctx->st));
+    ctx->stats = PgxStats();
+    RET(run_lin(ctx, nc, P<double>(ctx->x_ps0), P<double>(ctx->x_sig21), P<int>(ctx->x_npts), nmax, ctx->x_opos,
+                ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), false));
+    // slot order -> cluster order (a column gather, once per table)
+    MRET(pgx::gather_columns(ctx->st, nc, nmax, order.data(), P<double>(ctx->x_t64), P<float4>(ctx->x_t32),
+                            P<double>(ctx->c64), P<float4>(ctx->c32), ctx->mixed));
+    std::vector<double> R2(nc), r50(nc), rt(nc);
+    for (int i = 0; i < nc; i++) {
+        double R = (r_kernel > 0 ? r_kernel * r50_pc[i] : rtot_pc[i]) / 1000.0;
+        R2[i] = R * R;
+        r50[i] = r50_pc[i] / 1000.0;
+        rt[i] = rtot_pc[i] / 1000.0;
+    }
+    CK(cudaMemcpyAsync(ctx->cn.p, npts.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->cR2.p, R2.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->cr50.p, r50.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->crt.p, rt.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->cname.p, names, (size_t)nc * 40, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->nc = nc;
+    ctx->ncp = nmax;
+    MRET(pgx::mixed_cluster_aux(ctx->st, nc, nmax, P<float4>(ctx->c32), P<int>(ctx->cn), P<double>(ctx->cR2),
+                               ctx->mixed));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *prefix) {
+    if (!ctx) return PGX_E_ARG;
+    if (nt <= 0 || !ps0 || !sig || !prefix) return fail(ctx, PGX_E_ARG, "pgx_screen_stage: bad args");
+    if (nt > (1 << 20)) return fail(ctx, PGX_E_LIMIT, "pgx_screen_stage: %d stars in one chunk (limit 2^20)", nt);
+    CK(cudaSetDevice(ctx->device));
+    std::vector<double> p6, s21;
+    to_soa(nt, ps0, sig, p6, s21);
+    RET(ensure(ctx, ctx->s_ps0, p6.size() * 8));
+    RET(ensure(ctx, ctx->s_sig21, s21.size() * 8));
+    RET(ensure(ctx, ctx->s_prefix, (size_t)nt * 8));
+    CK(cudaMemcpyAsync(ctx->s_ps0.p, p6.data(), p6.size() * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->s_sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->s_prefix.p, prefix, (size_t)nt * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->nt = nt;
+    return 0;
+}
+
+int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision, long *n_rows) {
+    if (!ctx) return PGX_E_ARG;
+    if (ctx->nc <= 0) return fail(ctx, PGX_E_ARG, "pgx_screen_exec: no cluster table (pgx_screen_clusters)");
+    if (ctx->nt <= 0) return fail(ctx, PGX_E_ARG, "pgx_screen_exec: no stars staged (pgx_screen_stage)");
+    if (!(tmax_myr > 0) || !(cut > 0)) return fail(ctx, PGX_E_ARG, "pgx_screen_exec: tmax %g chi2_max %g", tmax_myr, cut);
+    if (precision != PGX_FP64 && precision != PGX_MIXED) return fail(ctx, PGX_E_ARG, "precision %d", precision);
+    CK(cudaSetDevice(ctx->device));
+    const int nt = ctx->nt, nc = ctx->nc, ns = npts_of(tmax_myr);
+    ctx->stats = PgxStats();
+    RET(ensure(ctx, ctx->t64, (size_t)ns * 12 * nt * 8));
+    RET(ensure(ctx, ctx->t32, (size_t)ns * 3 * nt * 16));
+    CK(cudaEventRecord(ctx->ev[EV_START], ctx->st));
+    RET(run_lin(ctx, nt, P<double>(ctx->s_ps0), P<double>(ctx->s_sig21), nullptr, ns, ctx->opos, ctx->ovel,
+                P<double>(ctx->t64), P<float4>(ctx->t32), true));
+    pgx::ScreenTables T = tables(ctx, ns);
+    int total = 0;
+    if (precision == PGX_FP64) {
+        const size_t pairs = (size_t)nt * nc;
+        RET(ensure(ctx, ctx->chi2T, pairs * 8));
+        RET(ensure(ctx, ctx->kbT, pairs * 4));
+        RET(ensure(ctx, ctx->sbT, pairs * 8));
+        RET(ensure(ctx, ctx->cnt, (size_t)nt * 4));
+        RET(ensure(ctx, ctx->off, (size_t)nt * 4));
+        RET(ensure(ctx, ctx->total, 16));
+        dim3 g((nt + 127) / 128, std::min(nc, 65535));
+        pgx::k_scan64<<<g, 128, 0, ctx->st>>>(T, cut, P<double>(ctx->chi2T), P<int>(ctx->kbT), P<double>(ctx->sbT));
+        CKL();
+        CK(cudaEventRecord(ctx->ev[EV_SCAN], ctx->st));
+        pgx::k_count_kept<<<(nt + 127) / 128, 128, 0, ctx->st>>>(nt, nc, P<double>(ctx->chi2T), cut, P<int>(ctx->cnt));
+        CKL();
+        pgx::k_exclusive_scan<<<1, 1024, 0, ctx->st>>>(nt, P<int>(ctx->cnt), P<int>(ctx->off), P<int>(ctx->total));
+        CKL();
+        CK(cudaMemcpyAsync(&total, ctx->total.p, 4, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        RET(ensure(ctx, ctx->kept, (size_t)total * sizeof(pgx::KeptPair)));
+        if (total > 0) {
+            pgx::k_emit_kept<<<(nt + 127) / 128, 128, 0, ctx->st>>>(nt, nc, P<double>(ctx->chi2T), P<int>(ctx->kbT),
+                                                                    P<double>(ctx->sbT), cut, P<int>(ctx->off),
+                                                                    P<pgx::KeptPair>(ctx->kept));
+            CKL();
+        }
+        CK(cudaEventRecord(ctx->ev[EV_SELECT], ctx->st));
+        ctx->stats.kernels += 4;
+    } else {
+        MRET(pgx::mixed_select(ctx->st, T, cut, ctx->mixed, ctx->ev[EV_SCAN], &total, &ctx->stats));
+        CK(cudaEventRecord(ctx->ev[EV_SELECT], ctx->st));
+    }
+    RET(ensure(ctx, ctx->fin, (size_t)total * sizeof(pgx::FinishIn)));
+    RET(ensure(ctx, ctx->rows, (size_t)total * sizeof(pgx::ScreenRowDev)));
+    if (total > 0) {
+        const pgx::KeptPair *kp = precision == PGX_FP64 ? P<pgx::KeptPair>(ctx->kept) : pgx::mixed_kept(ctx->mixed);
+        pgx::k_finish_prep<<<(total + 127) / 128, 128, 0, ctx->st>>>(T, total, kp, P<pgx::FinishIn>(ctx->fin),
+                                                                     P<pgx::ScreenRowDev>(ctx->rows));
+        CKL();
+        if (precision == PGX_FP64) {
+            pgx::k_finish64<<<(unsigned)(((size_t)total * 32 + 255) / 256), 256, 0, ctx->st>>>(
+                total, P<pgx::FinishIn>(ctx->fin), P<pgx::ScreenRowDev>(ctx->rows));
+            CKL();
+        } else {
+            MRET(pgx::mixed_finish(ctx->st, total, P<pgx::FinishIn>(ctx->fin), P<pgx::ScreenRowDev>(ctx->rows),
+                                  ctx->mixed, &ctx->stats));
+        }
+        ctx->stats.kernels += 2;
+    }
+    CK(cudaEventRecord(ctx->ev[EV_FINISH], ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    PgxStats &S = ctx->stats;
+    S.ms_orbit = elapsed(ctx, EV_START, EV_ORBIT);
+    S.ms_cov = elapsed(ctx, EV_ORBIT, EV_COV);
+    S.ms_scan = elapsed(ctx, EV_COV, EV_SCAN);
+    S.ms_select = elapsed(ctx, EV_SCAN, EV_SELECT);
+    S.ms_finish = elapsed(ctx, EV_SELECT, EV_FINISH);
+    S.ms_total = elapsed(ctx, EV_START, EV_FINISH);
+    S.pairs = (long)nt * nc;
+    S.kept = total;
+    S.body_steps = (long)nt * 7 * (ns - 1) * PH_LIN_SUB;
+    ctx->n_rows = total;
+    if (n_rows) *n_rows = total;
+    return 0;
+}
+
+int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n) {
+    if (!ctx) return PGX_E_ARG;
+    if (n < 0 || n > ctx->n_rows || (n > 0 && !rows)) return fail(ctx, PGX_E_ARG, "pgx_screen_fetch: n %ld", n);
+    if (n == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(rows, ctx->rows.p, (size_t)n * sizeof(PgxScreenRow), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+int pgx_screen(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *prefix, double tmax,
+               double cut, int precision, PgxScreenRow **rows, long *n_rows) {
+    if (!ctx) return PGX_E_ARG;
+    if (!rows || !n_rows) return fail(ctx, PGX_E_ARG, "pgx_screen: bad args");
+    *rows = nullptr;
+    *n_rows = 0;
+    RET(pgx_screen_stage(ctx, nt, ps0, sig, prefix));
+    long n = 0;
+    RET(pgx_screen_exec(ctx, tmax, cut, precision, &n));
+    PgxScreenRow *r = (PgxScreenRow *)malloc(sizeof(PgxScreenRow) * (n > 0 ? n : 1));
+    if (!r) return fail(ctx, PGX_E_NOMEM, "pgx_screen: host allocation of %ld rows", n);
+    int rc = pgx_screen_fetch(ctx, r, n);
+    if (rc) {
+        free(r);
+        return rc;
+    }
+    *rows = r;
+    *n_rows = n;
+    return 0;
+}
+
+int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps, const double *dt,
+             const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out) {
+    if (!ctx) return PGX_E_ARG;
+    if (n_pairs < 0 || (n_pairs > 0 && (!clone_off || !steps || !dt || !r50_pc || !rtot_pc || !res)))
+        return fail(ctx, PGX_E_ARG, "pgx_pair: bad args");
+    if (n_pairs == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    const int M = clone_off[n_pairs];
+    if (clone_off[0] != 0 || M < 0 || (M > 0 && !ps)) return fail(ctx, PGX_E_ARG, "pgx_pair: clone_off");
+    std::vector<int4> items;
+    int big_n2 = 0;
+    long long clone_steps = 0;
+    for (int p = 0; p < n_pairs; p++) {
+        const int m = clone_off[p + 1] - clone_off[p];
+        if (m < 0) return fail(ctx, PGX_E_ARG, "pgx_pair: clone_off not ascending at %d", p);
+        if (m > 16384) return fail(ctx, PGX_E_LIMIT, "pgx_pair: pair %d has %d clones (limit 16384)", p, m);
+        if (steps[p] < 0) return fail(ctx, PGX_E_ARG, "pgx_pair: steps[%d] = %d", p, steps[p]);
+        if (m > 1024) {
+            int n2 = 1;
+            while (n2 < m) n2 <<= 1;
+            big_n2 = std::max(big_n2, n2);
+        }
+        for (int c0 = 0; c0 < m; c0 += 32) items.push_back(make_int4(p, clone_off[p] + c0, std::min(32, m - c0), 0));
+        clone_steps += (long long)m * steps[p];
+    }
+    std::stable_sort(items.begin(), items.end(), [&](const int4 &a, const int4 &b) { return steps[a.x] > steps[b.x]; });
+    RET(ensure(ctx, ctx->p_off, (size_t)(n_pairs + 1) * 4));
+    RET(ensure(ctx, ctx->p_ps, (size_t)M * 12 * 8));
+    RET(ensure(ctx, ctx->p_steps, (size_t)n_pairs * 4));
+    RET(ensure(ctx, ctx->p_dt, (size_t)n_pairs * 8));
+    RET(ensure(ctx, ctx->p_r50, (size_t)n_pairs * 8));
+    RET(ensure(ctx, ctx->p_rt, (size_t)n_pairs * 8));
+    RET(ensure(ctx, ctx->p_items, items.size() * sizeof(int4)));
+    RET(ensure(ctx, ctx->p_q, 16));
+    RET(ensure(ctx, ctx->p_done, (size_t)n_pairs * 4));
+    RET(ensure(ctx, ctx->p_cres, (size_t)M * 3 * 8));
+    RET(ensure(ctx, ctx->p_res, (size_t)n_pairs * sizeof(PhResult)));
+    CK(cudaMemcpyAsync(ctx->p_off.p, clone_off, (size_t)(n_pairs + 1) * 4, cudaMemcpyHostToDevice, ctx->st));
+    if (M > 0) CK(cudaMemcpyAsync(ctx->p_ps.p, ps, (size_t)M * 12 * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->p_steps.p, steps, (size_t)n_pairs * 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->p_dt.p, dt, (size_t)n_pairs * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->p_r50.p, r50_pc, (size_t)n_pairs * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->p_rt.p, rtot_pc, (size_t)n_pairs * 8, cudaMemcpyHostToDevice, ctx->st));
+    if (!items.empty())
+        CK(cudaMemcpyAsync(ctx->p_items.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctx->p_q.p, 0, 16, ctx->st));
+    CK(cudaMemsetAsync(ctx->p_done.p, 0, (size_t)n_pairs * 4, ctx->st));
+    pgx::McPairs Pp;
+    Pp.n_pairs = n_pairs; Pp.n_clones = M; Pp.n_items = (int)items.size();
+    Pp.clone_off = P<int>(ctx->p_off); Pp.ps = P<double>(ctx->p_ps); Pp.steps = P<int>(ctx->p_steps);
+    Pp.dt = P<double>(ctx->p_dt); Pp.r50_pc = P<double>(ctx->p_r50); Pp.rtot_pc = P<double>(ctx->p_rt);
+    Pp.items = P<int4>(ctx->p_items); Pp.qhead = P<int>(ctx->p_q); Pp.done = P<int>(ctx->p_done);
+    Pp.cres = P<double>(ctx->p_cres); Pp.res = P<pgx::PhResultDev>(ctx->p_res);
+    ctx->stats = PgxStats();
+    CK(cudaEventRecord(ctx->ev[EV_PAIR0], ctx->st));
+    if (!items.empty()) {
+        int per_sm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pgx::k_pair_mc, pgx::kMcThreads, 0));
+        const int warps_needed = (int)items.size();
+        int grid = std::max(1, ctx->sms * std::max(1, per_sm));
+        grid = std::min(grid, (warps_needed + pgx::kMcThreads / 32 - 1) / (pgx::kMcThreads / 32));
+        pgx::k_pair_mc<<<grid, pgx::kMcThreads, 0, ctx->st>>>(Pp);
+        CKL();
+        ctx->stats.kernels++;
+    }
+    const size_t smem = (size_t)big_n2 * 8;
+    if (smem > 48 * 1024)
+        CK(cudaFuncSetAttribute(pgx::k_pair_reduce_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pgx::k_pair_reduce_big<<<n_pairs, 256, smem, ctx->st>>>(Pp);
+    CKL();
+    ctx->stats.kernels++;
+    CK(cudaEventRecord(ctx->ev[EV_PAIR1], ctx->st));
+    CK(cudaMemcpyAsync(res, ctx->p_res.p, (size_t)n_pairs * sizeof(PhResult), cudaMemcpyDeviceToHost, ctx->st));
+    if (clone_out && M > 0)
+        CK(cudaMemcpyAsync(clone_out, ctx->p_cres.p, (size_t)M * 3 * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->stats.ms_pair = elapsed(ctx, EV_PAIR0, EV_PAIR1);
+    ctx->stats.ms_total = ctx->stats.ms_pair;
+    ctx->stats.clones = M;
+    ctx->stats.clone_steps = clone_steps;
+    ctx->stats.body_steps = 2 * clone_steps;
+    ctx->stats.pairs = n_pairs;
+    return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------------------
+// The GPU half of the drop-in API (include/phygas.h).  These per-object / per-pair calls keep the reference's
+// signatures and ownership rules; each one runs the same kernels as the batched entry points on a process-wide
+// default context.  The reference API has no error channel: a GPU failure here prints the cause and ends the
+// process with status 1, as the reference GPU application does (src/main_phygas_boinc.cpp:23-27).
+namespace {
+
+PgxContext *g_ctx = nullptr;
+std::mutex g_mu;
+
+[[noreturn]] void die(const char *what, const char *why) {
+    fprintf(stderr, "phygas_gb300: %s failed: %s\n", what, why);
+    fflush(stderr);
+    exit(1);
+}
+
+PgxContext *dctx() {
+    if (!g_ctx) {
+        int rc = pgx_open(-1, &g_ctx);
+        if (rc) die("pgx_open", rc == PGX_E_NODEV ? "no CUDA device" : "device set-up");
+    }
+    return g_ctx;
+}
+
+void lin_one(PgxContext *ctx, const double ps0[6], const double sig[36], double tmax, PhLin *out) {
+    int n = npts_of(tmax);
+    out->n = n;
+    out->pos = (Vec3 *)malloc(sizeof(Vec3) * n);
+    out->vel = (Vec3 *)malloc(sizeof(Vec3) * n);
+    out->S = (double(*)[6])malloc(sizeof(double[6]) * n);
+    if (pgx_lin(ctx, 1, ps0, sig, &n, &out->pos[0].x, &out->vel[0].x, &out->S[0][0])) die("ph_lin", ctx->err.c_str());
+}
+
+// one (star, cluster) pair as a 1 x 1 screen
+int pair_tables(PgxContext *ctx, const PhLin *tl, const PhLin *cl, const PhCluster *c, uint64_t seed,
+                pgx::ScreenTables &T) {
+    const int nmax = std::max(tl->n, cl->n);
+    std::vector<double> h((size_t)2 * nmax * 12, 0.0);
+    auto pack = [&](const PhLin *l, double *dst) {
+        for (int k = 0; k < l->n; k++) {
+            double *o = dst + (size_t)k * 12;
+            o[0] = l->pos[k].x; o[1] = l->pos[k].y; o[2] = l->pos[k].z;
+            o[3] = l->vel[k].x; o[4] = l->vel[k].y; o[5] = l->vel[k].z;
+            for (int i = 0; i < 6; i++) o[6 + i] = l->S[k][i];
+        }
+    };
+    pack(tl, h.data());
+    pack(cl, h.data() + (size_t)nmax * 12);
+    const double R = (ph_screen_r > 0 ? ph_screen_r * c->r50_pc : c->rtot_pc) / 1000.0;
+    struct {
+        double R2, r50, rt;
+        uint64_t seed;
+        int cn, pad;
+        char name[40];
+    } aux = {R * R, c->r50_pc / 1000.0, c->rtot_pc / 1000.0, seed, cl->n, 0, {0}};
+    RET(ensure(ctx, ctx->x_t64, h.size() * 8 + sizeof aux));
+    char *base = P<char>(ctx->x_t64);
+    CK(cudaMemcpyAsync(base, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(base + h.size() * 8, &aux, sizeof aux, cudaMemcpyHostToDevice, ctx->st));
+    const char *a = base + h.size() * 8;
+    T.nt = 1; T.ns = tl->n; T.nc = 1; T.ncp = cl->n;
+    T.t64 = (const double *)base;
+    T.c64 = (const double *)base + (size_t)nmax * 12;
+    T.t32 = nullptr; T.c32 = nullptr;
+    T.R2 = (const double *)a; T.r50 = (const double *)(a + 8); T.rtot = (const double *)(a + 16);
+    T.seed_prefix = (const uint64_t *)(a + 24); T.cn = (const int *)(a + 32); T.cname = a + 40;
+    return 0;
+}
+
+int chi2_one(PgxContext *ctx, const PhLin *tl, const PhLin *cl, const PhCluster *c, double cut, int *kb, double *sb,
+             double *chi2) {
+    pgx::ScreenTables T;
+    RET(pair_tables(ctx, tl, cl, c, 0, T));
+    RET(ensure(ctx, ctx->x_opos, 32));
+    double *o = P<double>(ctx->x_opos);
+    pgx::k_scan64<<<dim3(1, 1), 32, 0, ctx->st>>>(T, cut, o, (int *)(o + 2), o + 1);
+    CKL();
+    double hb[3];
+    CK(cudaMemcpyAsync(hb, o, sizeof hb, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    *chi2 = hb[0];
+    *sb = hb[1];
+    memcpy(kb, &hb[2], sizeof(int));
+    return 0;
+}
+
+int finish_one(PgxContext *ctx, const PhLin *tl, const PhLin *cl, const PhCluster *c, uint64_t seed, double chi2,
+               int kb, double sb, PhScreen *res) {
+    pgx::ScreenTables T;
+    RET(pair_tables(ctx, tl, cl, c, seed, T));
+    RET(ensure(ctx, ctx->x_opos, sizeof(pgx::KeptPair) + sizeof(pgx::FinishIn) + sizeof(pgx::ScreenRowDev)));
+    char *b = P<char>(ctx->x_opos);
+    pgx::KeptPair kp = {0, 0, kb, 0, sb, chi2};
+    CK(cudaMemcpyAsync(b, &kp, sizeof kp, cudaMemcpyHostToDevice, ctx->st));
+    pgx::FinishIn *fin = (pgx::FinishIn *)(b + sizeof kp);
+    pgx::ScreenRowDev *row = (pgx::ScreenRowDev *)(b + sizeof kp + sizeof(pgx::FinishIn));
+    pgx::k_finish_prep<<<1, 32, 0, ctx->st>>>(T, 1, (const pgx::KeptPair *)b, fin, row);
+    CKL();
+    pgx::k_finish64<<<1, 32, 0, ctx->st>>>(1, fin, row);
+    CKL();
+    pgx::ScreenRowDev r;
+    CK(cudaMemcpyAsync(&r, row, sizeof r, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    memset(res, 0, sizeof *res);
+    res->chi2 = chi2; res->t = r.t_myr; res->d_nom_pc = r.d_nom_pc; res->sig_pc = r.sig_pc;
+    res->p_r50 = r.p_r50; res->p_rtot = r.p_rtot; res->vrel = r.vrel_kms;
+    return 0;
+}
+
+int reduce_only(PgxContext *ctx, int m, const double *best, const double *tbest, const double *vbest, double r50,
+                double rt, PhResult *res) {
+    const int off[2] = {0, m};
+    RET(ensure(ctx, ctx->p_off, 8));
+    RET(ensure(ctx, ctx->p_cres, (size_t)3 * (m > 0 ? m : 1) * 8));
+    RET(ensure(ctx, ctx->p_r50, 8));
+    RET(ensure(ctx, ctx->p_rt, 8));
+    RET(ensure(ctx, ctx->p_res, sizeof(PhResult)));
+    CK(cudaMemcpyAsync(ctx->p_off.p, off, 8, cudaMemcpyHostToDevice, ctx->st));
+    if (m > 0) {
+        CK(cudaMemcpyAsync(P<double>(ctx->p_cres), best, (size_t)m * 8, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaMemcpyAsync(P<double>(ctx->p_cres) + m, tbest, (size_t)m * 8, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaMemcpyAsync(P<double>(ctx->p_cres) + 2 * (size_t)m, vbest, (size_t)m * 8, cudaMemcpyHostToDevice, ctx->st));
+    }
+    CK(cudaMemcpyAsync(ctx->p_r50.p, &r50, 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ctx->p_rt.p, &rt, 8, cudaMemcpyHostToDevice, ctx->st));
+    pgx::McPairs Pp = {};
+    Pp.n_pairs = 1; Pp.n_clones = m; Pp.clone_off = P<int>(ctx->p_off); Pp.cres = P<double>(ctx->p_cres);
+    Pp.r50_pc = P<double>(ctx->p_r50); Pp.rtot_pc = P<double>(ctx->p_rt); Pp.res = P<pgx::PhResultDev>(ctx->p_res);
+    pgx::k_pair_reduce_only<<<1, pgx::kMcThreads, 0, ctx->st>>>(Pp);
+    CKL();
+    int n2 = 1;
+    while (n2 < m) n2 <<= 1;
+    const size_t smem = m > 1024 ? (size_t)n2 * 8 : 0;
+    if (m > 16384) return fail(ctx, PGX_E_LIMIT, "ph_pair_reduce: %d clones (limit 16384)", m);
+    if (smem > 48 * 1024)
+        CK(cudaFuncSetAttribute(pgx::k_pair_reduce_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    pgx::k_pair_reduce_big<<<1, 256, smem, ctx->st>>>(Pp);
+    CKL();
+    CK(cudaMemcpyAsync(res, ctx->p_res.p, sizeof(PhResult), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void ph_lin_target(const PhTarget *t, double tmax, int n_samp, uint64_t seed, PhLin *out) {
+    double ps0[6], sig[36];
+    pgh_target_init(t, n_samp, seed, ps0, sig);
+    std::lock_guard<std::mutex> lk(g_mu);
+    lin_one(dctx(), ps0, sig, tmax, out);
+}
+
+void ph_lin_cluster(const PhCluster *c, int n_samp, uint64_t seed, PhLin *out) {
+    double ps0[6], sig[36];
+    pgh_cluster_init(c, n_samp, seed, ps0, sig);
+    std::lock_guard<std::mutex> lk(g_mu);
+    lin_one(dctx(), ps0, sig, c->tmax_myr, out);
+}
+
+void ph_lin_free(PhLin *l) {
+    free(l->pos); free(l->vel); free(l->S);
+    l->pos = l->vel = nullptr; l->S = nullptr; l->n = 0;
+}
+
+double ph_screen_chi2_cut(const PhLin *tl, const PhLin *cl, const PhCluster *c, double cut, int *kb, double *sb) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    PgxContext *ctx = dctx();
+    double chi2;
+    if (chi2_one(ctx, tl, cl, c, cut, kb, sb, &chi2)) die("ph_screen_chi2", ctx->err.c_str());
+    return chi2;
+}
+
+double ph_screen_chi2(const PhLin *tl, const PhLin *cl, const PhCluster *c, int *kb, double *sb) {
+    return ph_screen_chi2_cut(tl, cl, c, INFINITY, kb, sb);
+}
+
+void ph_screen_finish(const PhLin *tl, const PhLin *cl, const PhCluster *c, uint64_t seed, double chi2, int kb,
+                      double sb, PhScreen *res) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    PgxContext *ctx = dctx();
+    if (finish_one(ctx, tl, cl, c, seed, chi2, kb, sb, res)) die("ph_screen_finish", ctx->err.c_str());
+}
+
+void ph_screen(const PhLin *tl, const PhLin *cl, const PhCluster *c, uint64_t seed, PhScreen *res) {
+    int kb;
+    double sb, chi2 = ph_screen_chi2(tl, cl, c, &kb, &sb);
+    ph_screen_finish(tl, cl, c, seed, chi2, kb, sb, res);
+}
+
+void ph_pair_clone(const double *ps, int steps, double dt, double *best, double *tbest, double *vbest) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    PgxContext *ctx = dctx();
+    const int off[2] = {0, 1};
+    const double r = 0.0;
+    PhResult res;
+    double out[3];
+    if (pgx_pair(ctx, 1, off, ps, &steps, &dt, &r, &r, &res, out)) die("ph_pair_clone", ctx->err.c_str());
+    *best = out[0]; *tbest = out[1]; *vbest = out[2];
+}
+
+void ph_pair_reduce(const PhCluster *c, int m, const double *best, const double *tbest, const double *vbest,
+                    PhResult *res) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    PgxContext *ctx = dctx();
+    if (reduce_only(ctx, m, best, tbest, vbest, c->r50_pc, c->rtot_pc, res)) die("ph_pair_reduce", ctx->err.c_str());
+}
+
+void ph_pair(const PhTarget *t, const PhCluster *c, int n_clones, double dt_myr, uint64_t seed, PhResult *res) {
+    std::vector<double> ps((size_t)12 * (n_clones > 0 ? n_clones : 1));
+    int steps;
+    double dt;
+    const int m = ph_pair_draw(t, c, n_clones, dt_myr, seed, ps.data(), &steps, &dt);
+    const int off[2] = {0, m};
+    std::lock_guard<std::mutex> lk(g_mu);
+    PgxContext *ctx = dctx();
+    if (pgx_pair(ctx, 1, off, ps.data(), &steps, &dt, &c->r50_pc, &c->rtot_pc, res, nullptr))
+        die("ph_pair", ctx->err.c_str());
+}
+
+}  // extern "C"

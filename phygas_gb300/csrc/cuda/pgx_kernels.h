@@ -1,0 +1,81 @@
+// pgx_kernels.h -- kernels of libphygas_gb300 and the device-side argument records they take (internal header).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pgx {
+
+// layout-identical to PhResult (include/phygas.h); checked by a static_assert in pgx_api.cu
+struct PhResultDev {
+    int n;
+    double d05, d50, d95, t05, t50, t95, v05, v50, v95, f_r50, f_rtot;
+};
+
+constexpr int kMcThreads = 128;
+
+// Clone Monte Carlo work: clones of pair p are [clone_off[p], clone_off[p+1]); ps = 12 doubles per clone
+struct McPairs {
+    int n_pairs, n_clones, n_items;
+    const int *clone_off;     // n_pairs + 1
+    const double *ps;         // n_clones * 12
+    const int *steps;         // per pair
+    const double *dt;         // per pair (negative)
+    const double *r50_pc, *rtot_pc;
+    const int4 *items;        // (pair, first clone, count <= 32, -)
+    int *qhead;               // queue head (zeroed before launch)
+    int *done;                // per pair, clones finished (zeroed before launch)
+    double *cres;             // [3][n_clones]: best (kpc), tbest (Myr), vbest (kpc/Myr)
+    PhResultDev *res;         // per pair
+};
+
+// The screen's device tables.  Star tracks: FP64 t64[k][12][nt] (pos, vel, S) and FP32 t32[k][nt][3] float4
+// (pos hi, pos lo, S).  Cluster table: the same two layouts over nc, plus per cluster its point count, kernel
+// radius^2, r50 and rtot (kpc) and its name (for the pair seeds).
+struct ScreenTables {
+    int nt, ns;                      // stars, points per star track
+    int nc, ncp;                     // clusters, points of the longest cluster track
+    const double *t64;
+    const float4 *t32;
+    const uint64_t *seed_prefix;     // per star: FNV-1a state after "id|"
+    const double *c64;
+    const float4 *c32;
+    const int *cn;
+    const double *R2, *r50, *rtot;
+    const char *cname;               // nc * 40 bytes
+};
+
+// one pair kept past the chi2 cut, in (star, cluster) order
+struct KeptPair {
+    int s, c, kb, pad;
+    double sb, chi2;
+};
+
+// what the 512-draw stage needs of a kept pair, and the row it fills
+struct FinishIn {
+    double mx, my, mz, l00, l10, l20, l11, l21, l22, r50, rt;
+    uint64_t seed;
+};
+struct ScreenRowDev {                // layout-identical to PgxScreenRow (include/phygas_gb300.h)
+    int star, cluster, kb, pad;
+    double sb, chi2, t_myr, d_nom_pc, sig_pc, p_r50, p_rtot, vrel_kms;
+};
+
+// ---- kernels ------------------------------------------------------------------------------------------------------
+__global__ void k_stm_orbits(int N, const double *ps0, const int *npts, int nmax, double *opos, double *ovel);
+__global__ void k_stm_cov(int N, int nmax, const int *npts, const double *opos, const double *ovel,
+                          const double *sig21, double *t64, float4 *t32);
+__global__ void k_pair_mc(McPairs P);
+__global__ void k_pair_reduce_big(McPairs P);
+__global__ void k_pair_reduce_only(McPairs P);
+__global__ void k_peak_dfma(double *out, int iters, double a, double b);
+__global__ void k_peak_ffma(float *out, int iters, float a, float b);
+
+__global__ void k_scan64(ScreenTables T, double cut, double *chi2T, int *kbT, double *sbT);
+__global__ void k_count_kept(int nt, int nc, const double *chi2T, double cut, int *cnt);
+__global__ void k_exclusive_scan(int n, const int *in, int *out, int *total);
+__global__ void k_emit_kept(int nt, int nc, const double *chi2T, const int *kbT, const double *sbT, double cut,
+                            const int *off, KeptPair *out);
+__global__ void k_finish_prep(ScreenTables T, int n, const KeptPair *kp, FinishIn *fin, ScreenRowDev *rows);
+__global__ void k_finish64(int n, const FinishIn *fin, ScreenRowDev *rows);
+
+}  // namespace pgx

@@ -1,0 +1,34 @@
+// pgx_mixed.h -- the mixed-precision screen stages and the cluster-table helpers (internal header).
+#pragma once
+#include <string>
+#include "pgx_kernels.h"
+#include "phygas_gb300.h"
+
+namespace pgx {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+// work buffers of the mixed-precision screen, owned by the context
+struct MixedBufs {
+    DevBuf order, ub, flag, cnt, off, total, kept, cand, cand_off, ent, entq, aux;
+    std::string err;
+};
+
+void mixed_free(MixedBufs &m);
+// slot-ordered tracks (longest first) -> cluster-ordered table columns
+int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, const double *t64_slot,
+                   const float4 *t32_slot, double *c64, float4 *c32, MixedBufs &m);
+// per-cluster quantities the FP32 filter reads (kept resident with the table)
+int mixed_cluster_aux(cudaStream_t st, int nc, int nmax, const float4 *c32, const int *cn, const double *R2,
+                      MixedBufs &m);
+// FP32 filter + FP64 recheck: the kept pairs in (star, cluster) order, identical to the FP64 path's
+int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &m, cudaEvent_t ev_scan, int *total,
+                 PgxStats *stats);
+const KeptPair *mixed_kept(MixedBufs &m);
+// FP32 draws with an FP64 guard band: counts identical to the FP64 path's
+int mixed_finish(cudaStream_t st, int n, const FinishIn *fin, ScreenRowDev *rows, MixedBufs &m, PgxStats *stats);
+
+}  // namespace pgx

@@ -1,0 +1,427 @@
+// pgx_orbit.cu -- FP64 orbit kernels of libphygas_gb300: the state-transition tracks of the linear screen and the
+// clone Monte Carlo of ph_pair with its quantile reduction.
+//
+//   k_stm_orbits   one thread per orbit: an object's nominal orbit and its 6 neighbours (+1e-5 on one phase-space
+//                  axis) are 7 independent threads, so a warp is 32 orbits with identical work and no barrier
+//                  (reference lin_integrate, src/phygas.c:286-323)
+//   k_stm_cov      one thread per (object, point): A = (neighbour - nominal) / eps, S = A Sigma0 A^T, and the two
+//                  track layouts the screen reads (FP64 for the exact stages, split FP32 for the filter)
+//   k_pair_mc      persistent: warps take items of <= 32 clones of one pair from a device queue (longest first),
+//                  trace them back with KDK leapfrog and the segment closest approach (reference ph_pair_clone,
+//                  src/phygas.c:200-216); the warp that finishes a pair's last item reduces it in registers
+//                  with warp shuffles (reference ph_pair_reduce, src/phygas.c:218-238)
+//   k_pair_reduce_big  the same reduction for pairs of more than 1024 clones, one CTA per pair in shared memory
+#include "pgx_internal.cuh"
+#include "pgx_kernels.h"
+
+namespace pgx {
+
+// npts == nullptr: every object has nmax points
+__global__ void __launch_bounds__(128) k_stm_orbits(int N, const double *__restrict__ ps0, const int *__restrict__ npts,
+                                                    int nmax, double *__restrict__ opos, double *__restrict__ ovel) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= N) return;
+    const size_t NN = N;
+    Orbit o;
+    o.x = ps0[i]; o.y = ps0[NN + i]; o.z = ps0[2 * NN + i];
+    o.vx = ps0[3 * NN + i]; o.vy = ps0[4 * NN + i]; o.vz = ps0[5 * NN + i];
+    switch (j) {
+        case 1: o.x += kEps; break;
+        case 2: o.y += kEps; break;
+        case 3: o.z += kEps; break;
+        case 4: o.vx += kEps; break;
+        case 5: o.vy += kEps; break;
+        case 6: o.vz += kEps; break;
+        default: break;
+    }
+    o.init();
+    const int n = npts ? npts[i] : nmax;
+    constexpr double dt = -kStepMyr / kSub, h = 0.5 * dt;
+    for (int k = 0; k < n; k++) {
+        if (k > 0) {
+#pragma unroll 1
+            for (int s = 0; s < kSub; s++) o.kdk(dt, h);
+        }
+        double *p = opos + (size_t)(k * 7 + j) * 3 * NN + i;
+        p[0] = o.x; p[NN] = o.y; p[2 * NN] = o.z;
+        if (j == 0) {
+            double *v = ovel + (size_t)k * 3 * NN + i;
+            v[0] = o.vx; v[NN] = o.vy; v[2 * NN] = o.vz;
+        }
+    }
+}
+
+// sig21: the 21 distinct entries of the symmetric 6x6 Sigma0, [21][N], upper triangle row by row
+__global__ void __launch_bounds__(256) k_stm_cov(int N, int nmax, const int *__restrict__ npts,
+                                                 const double *__restrict__ opos, const double *__restrict__ ovel,
+                                                 const double *__restrict__ sig21, double *__restrict__ t64,
+                                                 float4 *__restrict__ t32) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t NN = N;
+    if (idx >= NN * nmax) return;
+    const int i = (int)(idx % NN), k = (int)(idx / NN);
+    if (npts && k >= npts[i]) return;
+    const double *P = opos + (size_t)k * 21 * NN + i;
+    const double x0 = P[0], y0 = P[NN], z0 = P[2 * NN];
+    double A[3][6];
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        const double *Q = P + (size_t)(j + 1) * 3 * NN;
+        A[0][j] = (Q[0] - x0) * 1e5;
+        A[1][j] = (Q[NN] - y0) * 1e5;
+        A[2][j] = (Q[2 * NN] - z0) * 1e5;
+    }
+    double sg[6][6];
+    {
+        int q = 0;
+#pragma unroll
+        for (int a = 0; a < 6; a++)
+#pragma unroll
+            for (int b = a; b < 6; b++) { sg[a][b] = sg[b][a] = sig21[(size_t)q * NN + i]; q++; }
+    }
+    double AS[3][6];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int b = 0; b < 6; b++) {
+            double acc = 0.0;
+#pragma unroll
+            for (int a = 0; a < 6; a++) acc = fma(A[r][a], sg[a][b], acc);
+            AS[r][b] = acc;
+        }
+    double S[6];
+    const int rr[6] = {0, 0, 0, 1, 1, 2}, ss[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int b = 0; b < 6; b++) acc = fma(AS[rr[q]][b], A[ss[q]][b], acc);
+        S[q] = acc;
+    }
+    const double *V = ovel + (size_t)k * 3 * NN + i;
+    double *T = t64 + (size_t)k * 12 * NN + i;
+    const double vals[12] = {x0, y0, z0, V[0], V[NN], V[2 * NN], S[0], S[1], S[2], S[3], S[4], S[5]};
+#pragma unroll
+    for (int f = 0; f < 12; f++) T[(size_t)f * NN] = vals[f];
+    const float hx = (float)x0, hy = (float)y0, hz = (float)z0;
+    float4 *o = t32 + ((size_t)k * NN + i) * 3;
+    o[0] = make_float4(hx, hy, hz, (float)(x0 - (double)hx));
+    o[1] = make_float4((float)(y0 - (double)hy), (float)(z0 - (double)hz), (float)S[0], (float)S[1]);
+    o[2] = make_float4((float)S[2], (float)S[3], (float)S[4], (float)S[5]);
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// clone Monte Carlo
+
+// closest approach of one clone (ps: target pos/vel, cluster pos/vel); results in kpc, Myr, kpc/Myr
+__device__ __forceinline__ void trace_clone(const double *__restrict__ ps, int steps, double dt, double &best_o,
+                                            double &tbest_o, double &vbest_o) {
+    Orbit a, b;
+    a.x = ps[0]; a.y = ps[1]; a.z = ps[2]; a.vx = ps[3]; a.vy = ps[4]; a.vz = ps[5];
+    b.x = ps[6]; b.y = ps[7]; b.z = ps[8]; b.vx = ps[9]; b.vy = ps[10]; b.vz = ps[11];
+    a.init();
+    b.init();
+    double r0x = a.x - b.x, r0y = a.y - b.y, r0z = a.z - b.z;
+    double r0s = r0x * r0x + r0y * r0y + r0z * r0z;
+    double best = sqrt(r0s), best2 = r0s, tbest = 0.0;
+    double ux = a.vx - b.vx, uy = a.vy - b.vy, uz = a.vz - b.vz;
+    double vbest = sqrt(ux * ux + uy * uy + uz * uz);
+    const double h = 0.5 * dt;
+#pragma unroll 1
+    for (int i = 1; i <= steps; i++) {
+        a.kdk(dt, h);
+        b.kdk(dt, h);
+        const double r1x = a.x - b.x, r1y = a.y - b.y, r1z = a.z - b.z;
+        const double dx = r1x - r0x, dy = r1y - r0y, dz = r1z - r0z;
+        const double dd = dx * dx + dy * dy + dz * dz;
+        const double an = r0x * dx + r0y * dy + r0z * dz;
+        const double r1s = r1x * r1x + r1y * r1y + r1z * r1z;
+        // squared distance of the segment r0 -> r1 from the origin, times dd (no division): the cheap pre-test
+        double near2dd;
+        if (!(dd > 0) || an >= 0) near2dd = r0s * dd;
+        else if (-an >= dd) near2dd = r1s * dd;
+        else near2dd = r0s * dd - an * an;
+        if (near2dd < best2 * dd * (1.0 + 1e-12) || (!(dd > 0) && r0s < best2 * (1.0 + 1e-12))) {
+            // the reference's segment minimum (seg_min, src/phygas.c:147-156) and its strict comparison
+            double s = 0.0;
+            if (dd > 0) {
+                s = -an / dd;
+                s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+            }
+            const double mx = fma(dx, s, r0x), my = fma(dy, s, r0y), mz = fma(dz, s, r0z);
+            const double dm = sqrt(mx * mx + my * my + mz * mz);
+            if (dm < best) {
+                best = dm;
+                best2 = dm * dm;
+                tbest = ((double)(i - 1) + s) * -dt;
+                const double wx = a.vx - b.vx, wy = a.vy - b.vy, wz = a.vz - b.vz;
+                vbest = sqrt(wx * wx + wy * wy + wz * wz);
+            }
+        }
+        r0x = r1x; r0y = r1y; r0z = r1z;
+        r0s = r1s;
+    }
+    best_o = best;
+    tbest_o = tbest;
+    vbest_o = vbest;
+}
+
+// ---- reduction of one pair (m clones) ---------------------------------------------------------------------------
+// All sorted quantities are non-negative doubles, whose IEEE bit patterns order like their values, so the sort
+// runs on 64-bit integer keys (the integer pipe; a double compare would occupy the scarce FP64 pipe).
+__device__ __forceinline__ unsigned long long kmin(unsigned long long a, unsigned long long b) { return a < b ? a : b; }
+__device__ __forceinline__ unsigned long long kmax(unsigned long long a, unsigned long long b) { return a < b ? b : a; }
+
+// bitonic sort of 32*R keys held by one warp, element e = 32*r + lane in register r: stages whose partner distance
+// j is below 32 exchange across lanes with shuffles, the others swap registers within a lane
+template <int R>
+__device__ __forceinline__ void warp_bitonic(unsigned long long (&a)[R], int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+                const int jr = j >> 5;
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    if (r & jr) continue;
+                    const bool asc = ((32 * r) & k) == 0;
+                    const unsigned long long lo = kmin(a[r], a[r | jr]), hi = kmax(a[r], a[r | jr]);
+                    a[r] = asc ? lo : hi;
+                    a[r | jr] = asc ? hi : lo;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const unsigned long long p = __shfl_xor_sync(0xffffffffu, a[r], j);
+                    const bool asc = ((32 * r + lane) & k) == 0, lower = (lane & j) == 0;
+                    a[r] = (asc == lower) ? kmin(a[r], p) : kmax(a[r], p);
+                }
+            }
+        }
+    }
+}
+
+// linear-interpolated quantile of a sorted array (reference quantile, src/phygas.c:175-180), without contraction
+__device__ __forceinline__ double interp_q(const double *v, int n, double q) {
+    const double pos = __dmul_rn(q, (double)(n - 1));
+    const int i = (int)pos;
+    if (i >= n - 1) return v[n - 1];
+    return __dadd_rn(v[i], __dmul_rn(__dsub_rn(pos, (double)i), __dsub_rn(v[i + 1], v[i])));
+}
+
+// one warp reduces one pair: cres holds best/tbest/vbest of its m clones (m <= 32*R)
+template <int R>
+__device__ void warp_reduce_pair(const double *__restrict__ best, const double *__restrict__ tbest,
+                                 const double *__restrict__ vbest, int m, double r50_pc, double rtot_pc,
+                                 double *smem_w, PhResultDev *out, int lane) {
+    unsigned long long a[R];
+    int in50 = 0, intot = 0;
+    double res[9];
+#pragma unroll 1
+    for (int which = 0; which < 3; which++) {
+        const double *src = which == 0 ? best : (which == 1 ? tbest : vbest);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int e = 32 * r + lane;
+            double v = 0.0;
+            if (e < m) {
+                v = __ldcg(src + e);
+                if (which == 0) {
+                    v = __dmul_rn(v, 1000.0);
+                    in50 += v < r50_pc;
+                    intot += v < rtot_pc;
+                } else if (which == 2) {
+                    v = __dmul_rn(v, kKms);
+                }
+            }
+            a[r] = e < m ? (unsigned long long)__double_as_longlong(v) : 0x7ff0000000000000ULL;
+        }
+        warp_bitonic<R>(a, lane);
+#pragma unroll
+        for (int r = 0; r < R; r++) smem_w[32 * r + lane] = __longlong_as_double((long long)a[r]);
+        __syncwarp();
+        if (lane == 0) {
+            res[3 * which + 0] = interp_q(smem_w, m, 0.05);
+            res[3 * which + 1] = interp_q(smem_w, m, 0.5);
+            res[3 * which + 2] = interp_q(smem_w, m, 0.95);
+        }
+        __syncwarp();
+    }
+    in50 = __reduce_add_sync(0xffffffffu, in50);
+    intot = __reduce_add_sync(0xffffffffu, intot);
+    if (lane == 0) {
+        PhResultDev o;
+        o.n = m;
+        o.d05 = res[0]; o.d50 = res[1]; o.d95 = res[2];
+        o.t05 = res[3]; o.t50 = res[4]; o.t95 = res[5];
+        o.v05 = res[6]; o.v50 = res[7]; o.v95 = res[8];
+        o.f_r50 = m > 0 ? __ddiv_rn((double)in50, (double)m) : 0.0;
+        o.f_rtot = m > 0 ? __ddiv_rn((double)intot, (double)m) : 0.0;
+        if (m <= 0) { o.d05 = o.d50 = o.d95 = o.t05 = o.t50 = o.t95 = o.v05 = o.v50 = o.v95 = 0.0; }
+        *out = o;
+    }
+}
+
+__device__ void reduce_dispatch(const McPairs &P, int p, double *smem_w, int lane) {
+    const int m = P.clone_off[p + 1] - P.clone_off[p];
+    const size_t o = P.clone_off[p];
+    const double *b = P.cres + o, *t = P.cres + P.n_clones + o, *v = P.cres + 2 * (size_t)P.n_clones + o;
+    PhResultDev *out = P.res + p;
+    const double r50 = P.r50_pc[p], rt = P.rtot_pc[p];
+    if (m <= 32) warp_reduce_pair<1>(b, t, v, m, r50, rt, smem_w, out, lane);
+    else if (m <= 64) warp_reduce_pair<2>(b, t, v, m, r50, rt, smem_w, out, lane);
+    else if (m <= 128) warp_reduce_pair<4>(b, t, v, m, r50, rt, smem_w, out, lane);
+    else if (m <= 256) warp_reduce_pair<8>(b, t, v, m, r50, rt, smem_w, out, lane);
+    else if (m <= 512) warp_reduce_pair<16>(b, t, v, m, r50, rt, smem_w, out, lane);
+    else warp_reduce_pair<32>(b, t, v, m, r50, rt, smem_w, out, lane);
+}
+
+// Persistent clone kernel.  items[q] = (pair, first clone, count <= 32), longest trace first.  No warp ever waits
+// for another: a warp takes the next item with one atomic, and the warp whose item completes a pair's count (an
+// atomic per item, after a fence) reduces that pair.
+__global__ void __launch_bounds__(kMcThreads) k_pair_mc(McPairs P) {
+    __shared__ double smem[kMcThreads / 32][1024];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (;;) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(P.qhead, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= P.n_items) break;
+        const int4 it = P.items[q];   // x = pair, y = first clone, z = count
+        const int p = it.x;
+        if (lane < it.z) {
+            const int c = it.y + lane;
+            double best, tbest, vbest;
+            trace_clone(P.ps + (size_t)c * 12, P.steps[p], P.dt[p], best, tbest, vbest);
+            P.cres[c] = best;
+            P.cres[P.n_clones + c] = tbest;
+            P.cres[2 * (size_t)P.n_clones + c] = vbest;
+        }
+        __threadfence();
+        __syncwarp();
+        int last = 0;
+        if (lane == 0) {
+            const int m = P.clone_off[p + 1] - P.clone_off[p];
+            last = atomicAdd(P.done + p, it.z) + it.z == m;
+        }
+        last = __shfl_sync(0xffffffffu, last, 0);
+        if (last) {
+            __threadfence();
+            const int m = P.clone_off[p + 1] - P.clone_off[p];
+            if (m <= 1024) reduce_dispatch(P, p, smem[w], lane);
+        }
+    }
+}
+
+// reduction alone, one warp per pair, for results traced elsewhere (the drop-in ph_pair_reduce)
+__global__ void __launch_bounds__(kMcThreads) k_pair_reduce_only(McPairs P) {
+    __shared__ double smem[kMcThreads / 32][1024];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int p = blockIdx.x * (kMcThreads / 32) + w;
+    if (p >= P.n_pairs) return;
+    const int m = P.clone_off[p + 1] - P.clone_off[p];
+    if (m > 0 && m <= 1024) reduce_dispatch(P, p, smem[w], lane);
+}
+
+// pairs of 0 clones never get an item: their (empty) result is written here, with the big-pair reduction
+__global__ void k_pair_reduce_big(McPairs P) {
+    extern __shared__ double sm[];
+    const int p = blockIdx.x;
+    const int m = P.clone_off[p + 1] - P.clone_off[p];
+    if (m > 0 && m <= 1024) return;
+    PhResultDev *out = P.res + p;
+    if (m <= 0) {
+        if (threadIdx.x == 0) {
+            PhResultDev o;
+            o.n = 0;
+            o.d05 = o.d50 = o.d95 = o.t05 = o.t50 = o.t95 = o.v05 = o.v50 = o.v95 = o.f_r50 = o.f_rtot = 0.0;
+            *out = o;
+        }
+        return;
+    }
+    int n2 = 1;
+    while (n2 < m) n2 <<= 1;
+    unsigned long long *key = reinterpret_cast<unsigned long long *>(sm);
+    const size_t o = P.clone_off[p];
+    __shared__ int c50, ctot;
+    __shared__ double res[9];
+    if (threadIdx.x == 0) { c50 = 0; ctot = 0; }
+    __syncthreads();
+    for (int which = 0; which < 3; which++) {
+        const double *src = P.cres + (size_t)which * P.n_clones + o;
+        int l50 = 0, ltot = 0;
+        for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+            double v = 0.0;
+            if (e < m) {
+                v = src[e];
+                if (which == 0) { v = __dmul_rn(v, 1000.0); l50 += v < P.r50_pc[p]; ltot += v < P.rtot_pc[p]; }
+                else if (which == 2) v = __dmul_rn(v, kKms);
+            }
+            key[e] = e < m ? (unsigned long long)__double_as_longlong(v) : 0x7ff0000000000000ULL;
+        }
+        if (which == 0) { atomicAdd(&c50, l50); atomicAdd(&ctot, ltot); }
+        __syncthreads();
+        for (int k = 2; k <= n2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int e = threadIdx.x; e < n2; e += blockDim.x) {
+                    const int f = e ^ j;
+                    if (f > e) {
+                        const unsigned long long x = key[e], y = key[f];
+                        const bool asc = (e & k) == 0;
+                        if ((x > y) == asc) { key[e] = y; key[f] = x; }
+                    }
+                }
+                __syncthreads();
+            }
+        if (threadIdx.x == 0) {
+            const double *v = reinterpret_cast<const double *>(key);
+            res[3 * which] = interp_q(v, m, 0.05);
+            res[3 * which + 1] = interp_q(v, m, 0.5);
+            res[3 * which + 2] = interp_q(v, m, 0.95);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        PhResultDev r;
+        r.n = m;
+        r.d05 = res[0]; r.d50 = res[1]; r.d95 = res[2];
+        r.t05 = res[3]; r.t50 = res[4]; r.t95 = res[5];
+        r.v05 = res[6]; r.v50 = res[7]; r.v95 = res[8];
+        r.f_r50 = __ddiv_rn((double)c50, (double)m);
+        r.f_rtot = __ddiv_rn((double)ctot, (double)m);
+        *out = r;
+    }
+}
+
+}  // namespace pgx
+
+namespace pgx {
+// Peak-rate probes for the roofline denominators (FP64 and FP32 are not in the driver's measured peaks): long
+// independent FMA chains, 8 per thread; the result is stored so nothing is eliminated.
+__global__ void k_peak_dfma(double *out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = threadIdx.x * 1e-3 + i;
+    for (int it = 0; it < iters; it++)
+#pragma unroll
+        for (int i = 0; i < 8; i++) x[i] = fma(x[i], a, b);
+    double s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += x[i];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+__global__ void k_peak_ffma(float *out, int iters, float a, float b) {
+    float x[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = threadIdx.x * 1e-3f + i;
+    for (int it = 0; it < iters; it++)
+#pragma unroll
+        for (int i = 0; i < 8; i++) x[i] = fmaf(x[i], a, b);
+    float s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; i++) s += x[i];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace pgx

@@ -1,0 +1,31 @@
+/* ph_host.h -- internal host helpers of libphygas_gb300 (not part of the public C-ABI). */
+#ifndef PH_HOST_H
+#define PH_HOST_H
+#include <stdint.h>
+#include <unistd.h>
+#include "phygas.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ph_lin_target_init / the cluster counterpart with the covariance as 36 doubles, row-major */
+void pgh_target_init(const PhTarget *t, int n_samp, uint64_t seed, double ps0[6], double sig[36]);
+void pgh_cluster_init(const PhCluster *c, int n_samp, uint64_t seed, double ps0[6], double sig[36]);
+/* the same for n objects on `threads` host threads (seeds ph_seed("lin", id|name)); prefix may be NULL */
+void pgh_draw_targets(const PhTarget *t, int n, int n_samp, int threads, double *ps0, double *sig, uint64_t *prefix);
+void pgh_draw_clusters(const PhCluster *c, int n, int n_samp, int threads, double *ps0, double *sig);
+/* FNV-1a: state after "target_id|", and its continuation over a string (ph_seed = continue(prefix(a), b)) */
+uint64_t pgh_seed_prefix(const char *target_id);
+uint64_t pgh_fnv_continue(uint64_t h, const char *s);
+int pgh_default_threads(void);
+/* fn(arg, i0, i1) over [0, n) in chunks, on `threads` host threads */
+void pgh_parallel_for(int n, int threads, int chunk, void (*fn)(void *, int, int), void *arg);
+/* ph_pair_draw for n_pairs pairs (clones of pair i at ps + 12 * n_clones * i; m, steps, dt per pair) */
+void pgh_draw_pairs(int n_pairs, const PhTarget *const *t, const PhCluster *const *c, int n_clones, double dt_myr,
+                    const uint64_t *seed, int threads, double *ps, int *m, int *steps, double *dt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -77,7 +77,7 @@ def main():
                 rows = [ln for ln in f if not ln.startswith("#")]
             h, n = rows_hash(rows), len(rows)
             if (h, n) != PUBLISHED[prof]:
-                sys.exit("%s: reference app gives %s / %d rows, published %s / %d" % (prof, h, n) + PUBLISHED[prof])
+                sys.exit("%s: reference app gives %s / %d rows, published %s / %d" % ((prof, h, n) + PUBLISHED[prof]))
             info["published"][prof] = {"sha1_12": h, "rows": n, "header": p["header"]}
             with open(os.path.join(d, "in"), "rb") as f:
                 write_gz(os.path.join(HERE, prof + "_in.txt.gz"), f.read())

@@ -1,0 +1,135 @@
+"""GPU parity of the pair Monte Carlo: per-clone closest approaches, the warp-shuffle quantile reduction (bit-exact
+on identical inputs), the 1 pulsar x 64 cluster x 200 clone x 400 step workload, and the reference's published row
+hash on its own `pulsar` profile through the drop-in CLI."""
+import ctypes as C
+import gzip
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import phygas_gb300 as pg
+from phygas_gb300 import synth
+from tests import oracle_tools as ot
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(built):
+    c = pg.Context(0)
+    yield c
+    c.close()
+
+
+def ref_pairs(name):
+    with gzip.open(os.path.join(ot.GOLDEN, "ref_dump_%s.txt.gz" % name), "rt") as f:
+        return ot.parse_pair_dump(f.read())
+
+
+def test_reduction_bit_exact(built, golden):
+    """ph_pair_reduce on the GPU, fed the reference's own per-clone results: the reference's PhResult bit for bit
+    (sorted quantiles with linear interpolation, strict < fractions)."""
+    L = pg.lib()
+    L.ph_pair_reduce.argtypes = [C.POINTER(pg.PhCluster), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double), C.POINTER(pg.PhResult)]
+    clusters = pg.read_clusters(golden["clusters"])
+    for name in ("pair_pulsar", "pair_star"):
+        for p in ref_pairs(name):
+            cl = np.array(p["clones"]).reshape(-1, 3)
+            b, t, v = (np.ascontiguousarray(cl[:, q]) for q in range(3))
+            res = pg.PhResult()
+            L.ph_pair_reduce(C.byref(clusters[p["cluster"]]), p["m"], pg._ptr(b), pg._ptr(t), pg._ptr(v),
+                             C.byref(res))
+            assert res.n == p["res"]["n"]
+            for k, want in p["res"].items():
+                assert getattr(res, k) == want, (name, p["cluster"], k)
+
+
+def test_reduction_large_pairs(ctx):
+    """Pairs of 1,000 (one warp, registers and shuffles) and 3,000 clones (shared-memory path) reduce exactly like a
+    sort on the host."""
+    rng = np.random.default_rng(5)
+    for m in (1, 31, 200, 1000, 1024, 1025, 3000):
+        cl = np.abs(rng.normal(size=(3, m))) * np.array([[1e-3], [10.0], [0.05]])
+        b, t, v = cl
+        L = pg.lib()
+        L.ph_pair_reduce.argtypes = [C.POINTER(pg.PhCluster), C.c_int, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(pg.PhResult)]
+        c = pg.PhCluster()
+        c.r50_pc, c.rtot_pc = 0.5, 1.5
+        res = pg.PhResult()
+        L.ph_pair_reduce(C.byref(c), m, pg._ptr(np.ascontiguousarray(b)), pg._ptr(np.ascontiguousarray(t)),
+                         pg._ptr(np.ascontiguousarray(v)), C.byref(res))
+        O = C.CDLL(ot.ORACLE_LIB)
+        O.ph_pair_reduce.argtypes = L.ph_pair_reduce.argtypes
+        want = pg.PhResult()
+        O.ph_pair_reduce(C.byref(c), m, pg._ptr(np.ascontiguousarray(b)), pg._ptr(np.ascontiguousarray(t)),
+                         pg._ptr(np.ascontiguousarray(v)), C.byref(want))
+        for k, _ in pg.PhResult._fields_:
+            assert getattr(res, k) == getattr(want, k), (m, k)
+
+
+def _check_pairs(res, clones, pairs, off):
+    worst = 0.0
+    for q, p in enumerate(pairs):
+        o = p["res"]
+        r = res[q]
+        assert r["n"] == o["n"]
+        for k in ("f_r50", "f_rtot"):
+            assert abs(r[k] - o[k]) <= ot.PROB_TOL, (q, k, r[k], o[k])
+        for k in ("d05", "d50", "d95", "t05", "t50", "t95", "v05", "v50", "v95"):
+            worst = max(worst, ot.rel_err(r[k], o[k]) if o[k] else abs(r[k]))
+        if clones is not None:
+            ref = np.array(p["clones"])
+            got = clones[:, off[q]:off[q + 1]].T
+            assert np.all(np.abs(got[:, 0] - ref[:, 0]) <= ot.REL_TOL * ref[:, 0] + 1e-12), q
+    return worst
+
+
+def test_clones_match_oracle(ctx):
+    """The reference's own clone draws traced on the GPU: closest approach, time and speed per clone and the
+    quantiles within 1e-6 relative, fractions identical."""
+    for name in ("pair_pulsar", "pair_star"):
+        pairs = ref_pairs(name)
+        off = np.concatenate([[0], np.cumsum([p["m"] for p in pairs])]).astype(np.int32)
+        ps = np.concatenate([np.array(p["ps"]).ravel() for p in pairs])
+        steps = np.array([p["steps"] for p in pairs], np.int32)
+        dt = np.array([p["dt"] for p in pairs])
+        cls = pg.read_clusters(ot.golden_inputs()["clusters"])
+        r50 = np.array([cls[p["cluster"]].r50_pc for p in pairs])
+        rt = np.array([cls[p["cluster"]].rtot_pc for p in pairs])
+        res, clones = ctx.pair(off, ps, steps, dt, r50, rt, want_clones=True)
+        worst = _check_pairs(res, clones, pairs, off)
+        assert worst <= ot.REL_TOL, (name, worst)
+
+
+def test_pair64_workload_matches_oracle(ctx):
+    """1 synthetic pulsar x 64 clusters x 200 clones x 400 steps (the plain FP64 ph_pair configuration)."""
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "pair64", 1, 1000)
+        out = ot.run([ot.ORACLE_DUMP, "pair", cp, tp, "0", "0", "64", "200", "0.05"])
+        pairs = ot.parse_pair_dump(out)
+        targets, clusters = pg.read_targets(tp), pg.read_clusters(cp)
+        off, ps, steps, dt, r50, rt = pg.pair_draws(targets, clusters, [(0, i) for i in range(64)], 200)
+    assert all(s == 400 for s in steps)
+    for q, p in enumerate(pairs):
+        assert np.array_equal(ps[12 * off[q]:12 * off[q + 1]], np.array(p["ps"]).ravel())
+    res, clones = ctx.pair(off, ps, steps, dt, r50, rt, want_clones=True)
+    worst = _check_pairs(res, clones, pairs, off)
+    assert worst <= ot.REL_TOL, worst
+    st = ctx.stats()
+    assert st["clone_steps"] == 64 * 200 * 400 and st["kernels"] >= 1
+
+
+def test_pulsar_profile_published_hash_via_cli(built, golden):
+    """phygas_cli (the drop-in CLI) on the reference's `pulsar` profile: the published hash 73bd8776bd66."""
+    out = subprocess.run([pg.PAIR_CLI, golden["clusters"], golden["pulsar"], "100", "0.05"], stdout=subprocess.PIPE,
+                         stderr=subprocess.PIPE, text=True, check=True).stdout
+    rows = [" ".join(ln.split()[:15]) + "\n" for ln in out.splitlines()]
+    gold = ot.golden_rows("pulsar")
+    if (ot.rows_hash(rows), len(rows)) != ot.PUBLISHED["pulsar"]:
+        diff = [(a, b) for a, b in zip(rows, gold) if a != b][:5]
+        pytest.fail("rows %d vs %d; first differences %r" % (len(rows), len(gold), diff))

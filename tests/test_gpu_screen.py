@@ -1,0 +1,123 @@
+"""GPU parity of the screen: STM tracks, the chi2 scan, the 512-draw probabilities, the kept-pair sets, and the
+reference's published row hash on its own `screen` profile -- for the FP64 path and the mixed-precision path."""
+import numpy as np
+import pytest
+
+import phygas_gb300 as pg
+from tests import oracle_tools as ot
+
+pytestmark = pytest.mark.gpu
+PRECISIONS = [pg.PGX_FP64, pg.PGX_MIXED]
+
+
+@pytest.fixture(scope="module")
+def ctx(built):
+    c = pg.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def data(golden):
+    return dict(clusters=pg.read_clusters(golden["clusters"]), stars=pg.read_targets(golden["screen"]))
+
+
+def _tracks_close(got, ref, keyfn, n_points):
+    worst = np.zeros(3)
+    for (i, k), v in ref.items():
+        g = got[keyfn(i, k)]
+        v = np.array(v)
+        worst[0] = max(worst[0], np.max(np.abs(g[:3] - v[:3])))                      # kpc
+        worst[1] = max(worst[1], np.max(np.abs(g[3:6] - v[3:6]) / np.abs(v[3:6]).max()))
+        worst[2] = max(worst[2], np.max(np.abs(g[6:] - v[6:])) / max(np.abs(v[6:]).max(), 1e-300))
+    return worst
+
+
+def test_stm_tracks_match_oracle(ctx, data, golden):
+    """pgx_lin (nominal + 6 neighbour orbits in FP64, S = A Sigma0 A^T) against the oracle's ph_lin_cluster /
+    ph_lin_target: positions within 1e-9 kpc, velocities and covariances within 1e-6 relative."""
+    for which, objs, n in (("c", data["clusters"], 24), ("t", data["stars"], 3)):
+        ref = ot.oracle_lin(golden["clusters"], golden["screen"], which, 0, n)
+        if which == "c":
+            ps0, sig = pg.draw_clusters(objs[:n])
+            npts = np.array([int(np.ceil(o.tmax_myr / 0.5)) + 1 for o in objs[:n]], np.int32)
+        else:
+            ps0, sig, _ = pg.draw_targets(objs[:n])
+            tmax = max(c.tmax_myr for c in data["clusters"])
+            npts = np.full(n, int(np.ceil(tmax / 0.5)) + 1, np.int32)
+        pos, vel, S = ctx.lin(ps0, sig, npts)
+        start = np.concatenate([[0], np.cumsum(npts)[:-1]])
+        got = {}
+        for i in range(n):
+            for k in range(npts[i]):
+                r = start[i] + k
+                got[(i, k)] = np.concatenate([pos[r], vel[r], S[r]])
+        assert len(got) == len(ref)
+        w = _tracks_close(got, ref, lambda i, k: (i, k), npts)
+        assert w[0] < 1e-9 and w[1] < 1e-6 and w[2] < 1e-6, (which, w)
+
+
+def _compare_rows(rows, ref, cut=25.0):
+    got = {(int(r["star"]), int(r["cluster"])): r for r in rows}
+    only_g = set(got) - set(ref)
+    only_r = set(ref) - set(got)
+    for key in only_g:
+        assert abs(got[key]["chi2"] - cut) <= ot.REL_TOL * cut, ("extra pair", key, got[key]["chi2"])
+    for key in only_r:
+        assert abs(ref[key]["chi2"] - cut) <= ot.REL_TOL * cut, ("missing pair", key, ref[key]["chi2"])
+    n_kb = 0
+    worst = {}
+    for key in set(got) & set(ref):
+        g, o = got[key], ref[key]
+        if g["kb"] != o["kb"]:
+            n_kb += 1
+            continue
+        for f in ("chi2", "t_myr", "d_nom_pc", "sig_pc", "vrel_kms"):
+            e = ot.rel_err(g[f], o[f]) if o[f] != 0 else abs(g[f])
+            worst[f] = max(worst.get(f, 0.0), e)
+        for f in ("p_r50", "p_rtot"):
+            assert abs(g[f] - o[f]) <= ot.PROB_TOL, (key, f, g[f], o[f])
+    return len(set(got) & set(ref)), n_kb, worst
+
+
+@pytest.mark.parametrize("precision", PRECISIONS, ids=["fp64", "mixed"])
+def test_screen_rows_match_oracle(ctx, data, golden, precision):
+    """8 stars x 4,087 clusters: same kept pairs, chi2 / t / d / sigma / vrel within 1e-6 relative, identical
+    p_r50 and p_rtot (counts out of 512), same argmin point."""
+    ctx.set_clusters(data["clusters"])
+    ps0, sig, pre = pg.draw_targets(data["stars"][:8])
+    tmax = max(c.tmax_myr for c in data["clusters"])
+    rows = ctx.screen(ps0, sig, pre, tmax, 25.0, precision)
+    ref = ot.oracle_screen(golden["clusters"], golden["screen"], 0, 8)
+    n, n_kb, worst = _compare_rows(rows, ref)
+    assert n > 500
+    assert n_kb == 0, n_kb
+    for f, e in worst.items():
+        assert e <= ot.REL_TOL, (f, e)
+
+
+def boinc_rows(rows, data, p_min=0.001):
+    out = []
+    for r in rows:
+        if r["p_r50"] < p_min:
+            continue
+        t, c = data["stars"][r["star"]], data["clusters"][r["cluster"]]
+        out.append("%s %s %s %.3f %.3f %.2f %.2f %.4f %.4f %.2f\n" % (
+            t.id.decode(), c.name.decode(), c.kind.decode(), r["chi2"], r["t_myr"], r["d_nom_pc"], r["sig_pc"],
+            r["p_r50"], r["p_rtot"], r["vrel_kms"]))
+    return out
+
+
+@pytest.mark.parametrize("precision", PRECISIONS, ids=["fp64", "mixed"])
+def test_screen_profile_published_hash(ctx, data, precision):
+    """The reference's `screen` benchmark profile (2,000 stars x 4,087 clusters, PHYGAS 1 screen 25 64 2 0.001):
+    the GPU rows hash to the published 3e860a4f0e51 (6,387 rows)."""
+    ctx.set_clusters(data["clusters"])
+    ps0, sig, pre = pg.draw_targets(data["stars"])
+    tmax = max(c.tmax_myr for c in data["clusters"])
+    rows = ctx.screen(ps0, sig, pre, tmax, 25.0, precision)
+    lines = boinc_rows(rows, data)
+    gold = ot.golden_rows("screen")
+    if (ot.rows_hash(lines), len(lines)) != ot.PUBLISHED["screen"]:
+        diff = [(a, b) for a, b in zip(lines, gold) if a != b][:5]
+        pytest.fail("rows %d vs %d; first differences %r" % (len(lines), len(gold), diff))

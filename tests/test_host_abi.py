@@ -1,0 +1,208 @@
+"""CPU checks of libphygas_gb300: it loads without a GPU, exports every entry point its headers declare, its
+records have the C layouts, and its host half (draws, seeds, readers, tracks, prefilter) equals the oracle bit for
+bit -- the GPU stages then start from the reference's own inputs."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import phygas_gb300 as pg
+from tests import oracle_tools as ot
+
+HEADERS = [os.path.join(ot.REPO, "include", h) for h in ("phygas.h", "phygas_gb300.h")]
+
+
+def declared_symbols():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names.update(re.findall(r"\b((?:ph|pgx)_\w+)\s*\(", text))
+        names.update(re.findall(r"extern\s+(?:const\s+)?\w+\s+(\w+)\s*;", text))
+    return sorted(names)
+
+
+def test_library_loads_and_exports_every_declared_symbol(built):
+    L = C.CDLL(pg.LIB_PATH)
+    missing = [n for n in declared_symbols() if not hasattr(L, n)]
+    assert not missing, missing
+    assert len(declared_symbols()) >= 40
+
+
+LAYOUT_PROBE = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "phygas_gb300.h"
+#define S(T) printf(#T " %zu\n", sizeof(T));
+#define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
+int main(void) {
+  S(PhCluster) S(PhTarget) S(PhResult) S(PgxScreenRow) S(PgxStats) S(PhLin) S(PhTrack) S(PhScreen)
+  O(PhCluster, kind) O(PhCluster, has_rv) O(PhCluster, r50_pc) O(PhCluster, tmax_myr)
+  O(PhTarget, kind) O(PhTarget, has_rv) O(PhTarget, e_rv)
+  O(PhResult, d05) O(PhResult, f_rtot) O(PgxScreenRow, sb) O(PgxScreenRow, vrel_kms)
+  O(PgxStats, pairs) O(PgxStats, kernels)
+  return 0;
+}
+"""
+
+
+def test_record_layouts_match_bindings(built):
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "p.c"), os.path.join(d, "p")
+        open(src, "w").write(LAYOUT_PROBE)
+        subprocess.check_call(["gcc", "-I", os.path.join(ot.REPO, "include"), src, "-o", exe])
+        got = dict(ln.split() for ln in subprocess.check_output([exe], text=True).splitlines())
+    for name, cls in (("PhCluster", pg.PhCluster), ("PhTarget", pg.PhTarget), ("PhResult", pg.PhResult),
+                      ("PgxScreenRow", pg.PgxScreenRow), ("PgxStats", pg.PgxStats)):
+        assert int(got[name]) == C.sizeof(cls), name
+    for key, val in got.items():
+        if "." in key:
+            t, f = key.split(".")
+            assert getattr(getattr(pg, t), f).offset == int(val), key
+    assert int(got["PgxScreenRow"]) == pg.ROW_DTYPE.itemsize
+    assert int(got["PhResult"]) == pg.RESULT_DTYPE.itemsize
+
+
+@pytest.fixture(scope="module")
+def both(built):
+    O = C.CDLL(ot.ORACLE_LIB)
+    O.ph_init()
+    return pg.lib(), O
+
+
+def test_readers_identical(both, golden):
+    P, O = both
+    for path, T, fn in ((golden["clusters"], pg.PhCluster, "ph_read_clusters"),
+                        (golden["screen"], pg.PhTarget, "ph_read_targets"),
+                        (golden["pulsar"], pg.PhTarget, "ph_read_targets")):
+        pa, pb = C.POINTER(T)(), C.POINTER(T)()
+        na = getattr(P, fn)(path.encode(), C.byref(pa))
+        getattr(O, fn).argtypes = [C.c_char_p, C.POINTER(C.POINTER(T))]
+        nb = getattr(O, fn)(path.encode(), C.byref(pb))
+        assert na == nb > 0
+        for i in range(na):      # field by field: padding and the bytes after a name's NUL are undefined
+            for f, ft in T._fields_:
+                va, vb = getattr(pa[i], f), getattr(pb[i], f)
+                if ft is C.c_double:
+                    va, vb = np.float64(va).tobytes(), np.float64(vb).tobytes()
+                assert va == vb, (path, i, f)
+
+
+def test_seeds_identical(both):
+    P, O = both
+    O.ph_seed.restype = C.c_uint64
+    O.ph_seed.argtypes = [C.c_char_p, C.c_char_p]
+    for a, b in ((b"lin", b"SYN_00001"), (b"4000000000000000007", b"SYN_04086"), (b"", b""), (b"x" * 39, b"y")):
+        assert P.ph_seed(a, b) == O.ph_seed(a, b)
+        assert P.ph_seed(a, b) == pg.lib().ph_seed(a, b)
+
+
+def test_target_draws_identical(both, golden):
+    """ph_lin_target_init (64 draws + 6-D covariance) and the threaded batch draws: bit-identical to the oracle."""
+    P, O = both
+    stars = pg.read_targets(golden["screen"])[:64]
+    ps0, sig, pre = pg.draw_targets(stars, 64, threads=4)
+    O.ph_lin_target_init.argtypes = [C.POINTER(pg.PhTarget), C.c_int, C.c_uint64, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]
+    O.ph_seed.restype = C.c_uint64
+    O.ph_seed.argtypes = [C.c_char_p, C.c_char_p]
+    for j, t in enumerate(stars):
+        a, s = np.zeros(6), np.zeros(36)
+        O.ph_lin_target_init(C.byref(t), 64, O.ph_seed(b"lin", t.id), pg._ptr(a), pg._ptr(s))
+        assert np.array_equal(a, ps0[j]) and np.array_equal(s, sig[j]), j
+        assert pre[j] == pg.lib().pgx_seed_prefix(t.id)
+
+
+def test_cluster_draws_identical(both, golden):
+    """pgx_draw_clusters equals the oracle's draws (ph_sample_cluster) and its covariance arithmetic."""
+    P, O = both
+
+    class Rng(C.Structure):
+        _fields_ = [("state", C.c_uint64)]
+
+    class PS(C.Structure):
+        _fields_ = [("v", C.c_double * 6)]
+
+    O.ph_sample_cluster.argtypes = [C.POINTER(pg.PhCluster), C.POINTER(Rng), C.POINTER(PS)]
+    O.ph_seed.restype = C.c_uint64
+    O.ph_seed.argtypes = [C.c_char_p, C.c_char_p]
+    clusters = pg.read_clusters(golden["clusters"])
+    pick = [0, 1, 2, 5, 17, 400, 4086] + [i for i in range(4087) if not clusters[i].has_rv][:5]
+    sel = (pg.PhCluster * len(pick))(*[clusters[i] for i in pick])
+    ps0, sig = pg.draw_clusters(sel, 64, threads=3)
+    for q, c in enumerate(sel):
+        nom = PS()
+        O.ph_sample_cluster(C.byref(c), None, C.byref(nom))
+        g = Rng(O.ph_seed(b"lin", c.name))
+        draws = []
+        for _ in range(64):
+            d = PS()
+            if O.ph_sample_cluster(C.byref(c), C.byref(g), C.byref(d)) == 0:
+                draws.append(list(d.v))
+        cov = [[0.0] * 6 for _ in range(6)]
+        for d in draws:
+            e = [d[i] - nom.v[i] for i in range(6)]
+            for a in range(6):
+                for b in range(6):
+                    cov[a][b] += e[a] * e[b]
+        cov = [[v / len(draws) for v in row] for row in cov]
+        assert list(nom.v) == list(ps0[q])
+        assert np.array_equal(np.array(cov).ravel(), sig[q]), pick[q]
+
+
+def test_pair_draws_identical(both, golden):
+    """ph_pair_draw (clone start states, steps, dt): bit-identical, for the pulsar and for stars."""
+    P, O = both
+    clusters = pg.read_clusters(golden["clusters"])
+    for tfile, js in ((golden["pulsar"], [0]), (golden["screen"], [3, 11])):
+        targets = pg.read_targets(tfile)
+        for j in js:
+            for i in (0, 7, 123, 4000):
+                t, c = targets[j], clusters[i]
+                seed = P.ph_seed(t.id, c.name)
+                out = []
+                for L in (P, O):
+                    L.ph_pair_draw.argtypes = [C.POINTER(pg.PhTarget), C.POINTER(pg.PhCluster), C.c_int,
+                                               C.c_double, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                               C.POINTER(C.c_double)]
+                    ps, st, dt = np.zeros(12 * 50), C.c_int(), C.c_double()
+                    m = L.ph_pair_draw(C.byref(t), C.byref(c), 50, 0.05, seed, pg._ptr(ps), C.byref(st),
+                                       C.byref(dt))
+                    out.append((m, st.value, dt.value, ps[:12 * m].tobytes()))
+                assert out[0] == out[1], (j, i)
+
+
+def test_tracks_and_prefilter_identical(both, golden):
+    """ph_track_target / ph_track_cluster / ph_prefilter (host): identical tracks and decisions."""
+    P, O = both
+
+    class Track(C.Structure):
+        _fields_ = [("n", C.c_int), ("pos", C.POINTER(C.c_double)), ("sig_pos", C.c_double),
+                    ("sig_vel", C.c_double)]
+
+    clusters = pg.read_clusters(golden["clusters"])
+    pulsar = pg.read_targets(golden["pulsar"])[0]
+    for L in (P, O):
+        L.ph_track_target.argtypes = [C.POINTER(pg.PhTarget), C.c_double, C.c_int, C.c_uint64, C.POINTER(Track)]
+        L.ph_track_cluster.argtypes = [C.POINTER(pg.PhCluster), C.c_int, C.c_uint64, C.POINTER(Track)]
+        L.ph_prefilter.argtypes = [C.POINTER(Track), C.POINTER(Track), C.POINTER(pg.PhCluster)]
+        L.ph_seed.restype = C.c_uint64
+        L.ph_seed.argtypes = [C.c_char_p, C.c_char_p]
+    tt = [Track(), Track()]
+    for L, t in zip((P, O), tt):
+        L.ph_track_target(C.byref(pulsar), 100.0, 32, L.ph_seed(b"track", pulsar.id), C.byref(t))
+    assert tt[0].n == tt[1].n and (tt[0].sig_pos, tt[0].sig_vel) == (tt[1].sig_pos, tt[1].sig_vel)
+    assert C.string_at(tt[0].pos, 24 * tt[0].n) == C.string_at(tt[1].pos, 24 * tt[1].n)
+    for i in range(0, 4087, 97):
+        c = clusters[i]
+        ct = [Track(), Track()]
+        dec = []
+        for L, t, x in zip((P, O), ct, tt):
+            L.ph_track_cluster(C.byref(c), 32, L.ph_seed(b"track", c.name), C.byref(t))
+            dec.append(L.ph_prefilter(C.byref(x), C.byref(t), C.byref(c)))
+        assert C.string_at(ct[0].pos, 24 * ct[0].n) == C.string_at(ct[1].pos, 24 * ct[1].n), i
+        assert dec[0] == dec[1], i

@@ -105,6 +105,14 @@ int pgx_stats(const PgxContext *ctx, PgxStats *out);
  * FP64-bound orbit stages and the FP32-bound filter.  Runs two short probe kernels (about 20 ms). */
 int pgx_peaks(PgxContext *ctx, double *fp64_flops, double *fp32_flops);
 
+/* Self-check of the mixed-precision screen's error bounds (no counterpart in the reference): for n points given in
+ * FP64 -- pos[12n] = star and cluster positions at the point and at the next (t0 c0 t1 c1), S[12n] = the star's and
+ * the cluster's covariance (xx xy xz yy yz zz), R2[n] -- returns the FP64 point chi2 (v64; -1 singular, +inf
+ * rejected by the trace bound) and the FP32 filter's bounds lb <= v64 <= ub, or rej = 1 where the filter rejects
+ * the point (then v64 >= chi2_max). */
+int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S, const double *R2, double chi2_max,
+                     double *v64, float *lb, float *ub, int *rej);
+
 #ifdef __cplusplus
 }
 #endif

@@ -84,6 +84,8 @@ SIGNATURES = [
     ("pgx_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, C.c_void_p, _D]),
     ("pgx_stats", C.c_int, [C.c_void_p, _P(PgxStats)]),
     ("pgx_peaks", C.c_int, [C.c_void_p, _D, _D]),
+    ("pgx_check_bounds", C.c_int, [C.c_void_p, C.c_int, _D, _D, _D, C.c_double, _D, _P(C.c_float),
+                                   _P(C.c_float), _I]),
     ("ph_init", None, []),
     ("ph_seed", C.c_uint64, [C.c_char_p, C.c_char_p]),
     ("ph_read_clusters", C.c_int, [C.c_char_p, _P(_P(PhCluster))]),
@@ -196,6 +198,18 @@ class Context:
         a, b = C.c_double(), C.c_double()
         self._check(lib().pgx_peaks(self.h, C.byref(a), C.byref(b)), "pgx_peaks")
         return a.value, b.value
+
+    def check_bounds(self, pos, S, R2, chi2_max=25.0):
+        """FP64 point chi2 and the FP32 filter's bounds for n points (see pgx_check_bounds)."""
+        pos = np.ascontiguousarray(pos, np.float64)
+        S = np.ascontiguousarray(S, np.float64)
+        R2 = np.ascontiguousarray(R2, np.float64)
+        n = len(R2)
+        v, lb, ub, rej = np.zeros(n), np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(n, np.int32)
+        self._check(lib().pgx_check_bounds(self.h, n, _ptr(pos), _ptr(S), _ptr(R2), chi2_max, _ptr(v),
+                                           _ptr(lb, C.c_float), _ptr(ub, C.c_float), _ptr(rej, C.c_int)),
+                    "pgx_check_bounds")
+        return v, lb, ub, rej
 
     def lin(self, ps0, sig, npts):
         ps0 = np.ascontiguousarray(ps0, np.float64)

@@ -251,6 +251,29 @@ int pgx_peaks(PgxContext *ctx, double *fp64, double *fp32) {
     return 0;
 }
 
+int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S, const double *R2, double cut,
+                     double *v64, float *lb, float *ub, int *rej) {
+    if (!ctx) return PGX_E_ARG;
+    if (n <= 0 || !pos || !S || !R2 || !v64 || !lb || !ub || !rej) return fail(ctx, PGX_E_ARG, "pgx_check_bounds");
+    CK(cudaSetDevice(ctx->device));
+    const size_t in = (size_t)n * (12 + 12 + 1) * 8, out = (size_t)n * (8 + 4 + 4 + 4);
+    RET(ensure(ctx, ctx->x_opos, in + out + 64));
+    char *b = P<char>(ctx->x_opos);
+    double *dp = (double *)b, *dS = dp + (size_t)12 * n, *dR = dS + (size_t)12 * n, *dv = dR + n;
+    float *dl = (float *)(dv + n), *du = dl + n;
+    int *dj = (int *)(du + n);
+    CK(cudaMemcpyAsync(dp, pos, (size_t)12 * n * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(dS, S, (size_t)12 * n * 8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(dR, R2, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->st));
+    MRET(pgx::mixed_check_bounds(ctx->st, n, dp, dS, dR, cut, dv, dl, du, dj, ctx->mixed.err));
+    CK(cudaMemcpyAsync(v64, dv, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(lb, dl, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(ub, du, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(rej, dj, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
 int pgx_lin(PgxContext *ctx, int n, const double *ps0, const double *sig, const int *npts, double *pos, double *vel,
             double *S) {
     if (!ctx) return PGX_E_ARG;

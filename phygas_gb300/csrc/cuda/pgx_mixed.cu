@@ -1,4 +1,24 @@
-// pgx_mixed.cu -- mixed-precision screen of libphygas_gb300 and the cluster-table column gather.
+// pgx_mixed.cu -- the mixed-precision screen of libphygas_gb300, and the cluster-table column gather.
+//
+// The orbits and state-transition matrices stay FP64 (pgx_orbit.cu).  The scan over every (star, cluster, point)
+// and the 512 draws per kept pair run in FP32 on cluster-relative coordinates (star and cluster positions carried
+// as FP32 hi + lo pairs, so m = (t_hi - c_hi) + (t_lo - c_lo) keeps FP64-level accuracy of the separation), each
+// FP32 value with a rigorous error bound.  Only what the bound cannot decide is recomputed with the FP64 path's own
+// functions (pgx_screen_math.cuh), so the rows are the FP64 path's rows bit for bit:
+//
+//   k_mx_scan32      FP32 filter, one thread per pair (warp = 32 stars x one cluster).  Per point: the reference's
+//                    trace bound (chi2 >= dist^2 / trace M), then bounds LB <= chi2_64 <= UB on the FP64 path's
+//                    value (a Rayleigh lower bound that needs no inversion, and an LDL^T solve where it is well
+//                    conditioned).  Per pair: may it be kept (some LB < cut), and its smallest UB.
+//   k_mx_count / k_mx_emit   stable compaction, per star, of the pairs that may be kept
+//   k_mx_cand        those pairs again: the points that can be the FP64 minimum (LB_k <= min UB, LB_k < cut),
+//                    counted, then written in point order after a scan
+//   k_mx_eval64      one thread per candidate point: the FP64 point chi2 (full warps on the scarce FP64 pipe)
+//   k_mx_best        per possible pair: FP64 argmin over its candidates, strict < in point order
+//   k_mx_kept_*      stable compaction of the pairs under the cut
+//   k_mx_finish32    one warp per kept pair: the 512 draws in FP32 with a per-draw error bound; a draw whose
+//                    distance is within the bound of r50 or rtot is redone in FP64
+#include <algorithm>
 #include <vector>
 #include "pgx_internal.cuh"
 #include "pgx_mixed.h"
@@ -26,6 +46,7 @@ int check(cudaError_t e, std::string &err, const char *what) {
     err = std::string(what) + ": " + cudaGetErrorString(e);
     return PGX_E_CUDA;
 }
+template <class T> T *Pb(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
 }  // namespace
 
 void mixed_free(MixedBufs &m) {
@@ -35,6 +56,7 @@ void mixed_free(MixedBufs &m) {
         if (b->p) { cudaFree(b->p); b->p = nullptr; b->cap = 0; }
 }
 
+// ---- cluster table: slot order (longest track first) -> cluster order ------------------------------------------
 __global__ void k_gather_cols(int nc, int nmax, const int *__restrict__ order, const double *__restrict__ s64,
                               const float4 *__restrict__ s32, double *__restrict__ d64, float4 *__restrict__ d32) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -54,23 +76,596 @@ int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, con
     if ((rc = check(cudaMemsetAsync(c64, 0, (size_t)nmax * 12 * nc * 8, st), m.err, "memset"))) return rc;
     if ((rc = check(cudaMemsetAsync(c32, 0, (size_t)nmax * 3 * nc * 16, st), m.err, "memset"))) return rc;
     const size_t work = (size_t)nc * nmax;
-    k_gather_cols<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(nc, nmax, (const int *)m.order.p, t64_slot, t32_slot,
+    k_gather_cols<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(nc, nmax, Pb<int>(m.order), t64_slot, t32_slot,
                                                                    c64, c32);
     if ((rc = check(cudaGetLastError(), m.err, "k_gather_cols"))) return rc;
-    // the host order array must outlive the async copy
     return check(cudaStreamSynchronize(st), m.err, "gather sync");
 }
 
 int mixed_cluster_aux(cudaStream_t, int, int, const float4 *, const int *, const double *, MixedBufs &) { return 0; }
 
-int mixed_select(cudaStream_t, const ScreenTables &, double, MixedBufs &m, cudaEvent_t, int *, PgxStats *) {
-    m.err = "mixed-precision screen not built in this version";
-    return PGX_E_ARG;
-}
-const KeptPair *mixed_kept(MixedBufs &m) { return (const KeptPair *)m.kept.p; }
-int mixed_finish(cudaStream_t, int, const FinishIn *, ScreenRowDev *, MixedBufs &m, PgxStats *) {
-    m.err = "mixed-precision finish not built in this version";
-    return PGX_E_ARG;
+// ---- the FP32 point evaluation with its error bounds ------------------------------------------------------------
+constexpr float kEps32 = 5.9604645e-8f;      // 2^-24
+constexpr float kC1 = 48.f, kC2 = 32.f;
+// relative error of the FP64 path's adjugate form m^T adj(M) m / det(M) (pgx_screen_math.cuh): cofactors, det
+// and numerator each lose at most a few hundred ulps of T^3 / det, T = trace(M) (all |M_ij| <= T); 256 eps_64
+constexpr float kAdj64 = 2.85e-14f;
+
+struct Bound {
+    float lb, ub;          // lb <= the FP64 path's point chi2 <= ub (ub = +inf: no upper bound)
+};
+
+// m^T (L D L^T)^-1 m with the factors of one point
+__device__ __forceinline__ float ldl_form(float l10, float l20, float l21, float i1, float i2, float i3, float x,
+                                          float y, float z) {
+    const float y1 = fmaf(-l10, x, y);
+    const float y2 = fmaf(-l21, y1, fmaf(-l20, x, z));
+    return fmaf(y2 * y2, i3, fmaf(y1 * y1, i2, x * x * i1));
 }
 
+// Bounds on the FP64 path's point chi2 (the smaller of the forms at m0 and at the segment's nearest point to the
+// origin, pgx_screen_math.cuh point_chi2_64) from FP32 data.  Returns false when the point is rejected by the
+// reference's trace bound with a margin, i.e. when the FP64 path rejects it as well and never uses its value.
+//
+// Lower bound, robust to any conditioning: for every x on the segment and u = its nearest point to the origin,
+// u.x >= |u|^2, and by Cauchy-Schwarz x^T M^-1 x >= (u.x)^2 / u^T M u, so the whole segment's forms are
+// >= |u|^4 / u^T M u (u^T M u needs no inversion and no cancellation bound beyond 10 eps (sum sqrt(M_ii)|u_i|)^2;
+// u's own FP32 error is taken off |u|).
+// Upper and lower bound from an FP32 LDL^T solve, when it is well conditioned: the computed form is exact for a
+// matrix within C1 eps tr(M) of M (storage, the two additions, the backward error of the factorization), and since
+// lambda_min(M) >= R^2 (both covariances are positive semi-definite), rho = C1 eps tr(M) / R^2 bounds the relative
+// change; plus C2 eps for the separations and the sums.  Used when rho <= 1/4.
+// Both are bounds on the exact form; the FP64 path's adjugate evaluation adds its own relative error
+// <= kAdj64 T^3 / det(M), with det(M) >= R^4 tr(M) / 3 (eigenvalues >= R^2, the largest >= tr/3), or from the FP32
+// pivots when rho <= 1/4.
+__device__ __forceinline__ bool point_bound32(const float (&St)[6], const float (&Sc)[6], float R2, const float (&m0)[3],
+                                              const float (&m1)[3], bool more, float cut, Bound &b) {
+    const float inf = __int_as_float(0x7f800000);
+    const float M0 = St[0] + Sc[0] + R2, M1 = St[1] + Sc[1], M2 = St[2] + Sc[2];
+    const float M3 = St[3] + Sc[3] + R2, M4 = St[4] + Sc[4], M5 = St[5] + Sc[5] + R2;
+    const float tr = M0 + M3 + M5;
+    const float thr = 2.f * cut * tr;
+    const float dx = m1[0] - m0[0], dy = m1[1] - m0[1], dz = m1[2] - m0[2];
+    const float a = fmaf(m0[0], dx, fmaf(m0[1], dy, m0[2] * dz));
+    const float dd = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float m00 = fmaf(m0[0], m0[0], fmaf(m0[1], m0[1], m0[2] * m0[2]));
+    const float m11 = fmaf(m1[0], m1[0], fmaf(m1[1], m1[1], m1[2] * m1[2]));
+    // Rejected points: the exact distance satisfies dist^2 > 1.5 cut tr(M) (the FP32 test has a factor 2 and its
+    // cancellation is limited by the m00 guard), so the exact chi2 > 1.5 cut, and the FP64 path's value -- rejected
+    // by its own test, or evaluated with relative error < 1/3 (the tr / R^2 guard, see kAdj64) -- is above the cut:
+    // the point can be neither the minimum of a kept pair nor bring a pair under the cut.
+    const float thr_m = thr * (1.f + 1e-5f);
+    bool far;
+    if (a >= 0.f) far = m00 > thr_m;
+    else if (-a >= dd) far = m11 > thr_m;
+    else far = (fmaf(m00, dd, -a * a) > thr_m * dd) && (m00 * (8.f * kEps32) < cut * tr);
+    if (far && tr < 1.8e6f * R2) return false;
+    // nearest point of the segment (FP32) and its error bound
+    float s = 0.f;
+    if (more && dd > 0.f) s = fminf(fmaxf(-a / dd, 0.f), 1.f);
+    const float ux = fmaf(dx, s, m0[0]), uy = fmaf(dy, s, m0[1]), uz = fmaf(dz, s, m0[2]);
+    const float big = sqrtf(fmaxf(m00, m11));
+    const float du = 8.f * kEps32 * big + 1e-12f;
+    const float uu = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
+    // Rayleigh lower bound
+    const float uMu = fmaf(M0, ux * ux, fmaf(M3, uy * uy, fmaf(M5, uz * uz,
+                      2.f * fmaf(M1, ux * uy, fmaf(M2, ux * uz, M4 * uy * uz)))));
+    const float sw = sqrtf(M0) * fabsf(ux) + sqrtf(M3) * fabsf(uy) + sqrtf(M5) * fabsf(uz);
+    const float uMu_ub = fmaxf(uMu, 0.f) + 10.f * kEps32 * sw * sw;
+    const float un = fmaxf(sqrtf(uu) - du, 0.f);
+    const float g = fmaxf(fmaf(un, un, -du * big), 0.f);
+    float lb = uMu_ub > 0.f ? g * g / uMu_ub * (1.f - 8.f * kEps32) : 0.f;
+    float ub = inf;
+    // LDL^T
+    const float lam = R2 * (1.f - 4.f * kEps32);
+    const float rho = kC1 * kEps32 * tr / lam;
+    const float D1 = M0;
+    const float i1 = 1.f / D1;
+    const float l10 = M1 * i1, l20 = M2 * i1;
+    const float D2 = fmaf(-l10, M1, M3);
+    const float i2 = 1.f / D2;
+    const float u = fmaf(-l20, M1, M4);
+    const float l21 = u * i2;
+    const float D3 = fmaf(-l21, u, fmaf(-l20, M2, M5));
+    const float i3 = 1.f / D3;
+    const bool ldl = D1 > 0.f && D2 > 0.f && D3 > 0.f && rho <= 0.25f && lam > 0.f;
+    // det(M) lower bound -> the FP64 path's own error
+    const float T = tr * (1.f + 4.f * kEps32);
+    float det_lb = lam * lam * tr * (1.f / 3.f) * (1.f - 8.f * kEps32);
+    if (ldl) {
+        const float r1 = rho / (1.f - rho);
+        const float f = 1.f - r1;
+        det_lb = fmaxf(det_lb, D1 * D2 * D3 * (f * f * f) * (1.f - 8.f * kEps32));
+    }
+    const float r64 = det_lb > 0.f ? kAdj64 * (T * T) * (T / det_lb) : inf;
+    if (ldl) {
+        // a point that differs from the FP64 path's by <= d moves the form by <= 2 sqrt(q / lam) d + d^2 / lam,
+        // whatever the direction: the FP32 separation m0 (hi/lo rounding, <= 3 eps |m0|) and the segment point (du)
+        const float rel = 2.f * rho + kC2 * kEps32;
+        const float il = 1.f / lam;
+        const float q0 = ldl_form(l10, l20, l21, i1, i2, i3, m0[0], m0[1], m0[2]);
+        const float d0 = 3.f * kEps32 * sqrtf(m00) + 1e-12f;
+        const float e0 = 2.f * sqrtf(q0 * (1.f + rel) * il) * d0 + d0 * d0 * il;
+        float lo = fmaf(q0, -rel, q0) - e0, hi = fmaf(q0, rel, q0) + e0;
+        if (more) {
+            const float qs = ldl_form(l10, l20, l21, i1, i2, i3, ux, uy, uz);
+            const float ea = 2.f * sqrtf(qs * (1.f + rel) * il) * du + du * du * il;
+            lo = fminf(lo, fmaf(qs, -rel, qs) - ea);
+            hi = fminf(hi, fmaf(qs, rel, qs) + ea);
+        }
+        lb = fmaxf(lb, lo);
+        ub = hi;
+    }
+    if (!(r64 < 0.5f)) {
+        b.lb = 0.f;
+        b.ub = inf;
+        return true;
+    }
+    b.lb = fmaxf(lb * (1.f - r64), 0.f);
+    b.ub = ub < inf ? ub * (1.f + r64) * (1.f + 4.f * kEps32) : inf;
+    return true;
+}
+
+// separation of star and cluster at one point from the split FP32 positions
+__device__ __forceinline__ void sep32(const float4 &t0, const float4 &t1, const float4 &c0, const float4 &c1,
+                                      float (&m)[3]) {
+    m[0] = (t0.x - c0.x) + (t0.w - c0.w);
+    m[1] = (t0.y - c0.y) + (t1.x - c1.x);
+    m[2] = (t0.z - c0.z) + (t1.y - c1.y);
+}
+
+// Walks the points of one (star, cluster) pair in order, calling f(k, bound) for every point the trace bound keeps.
+template <class F>
+__device__ __forceinline__ void walk32(const ScreenTables &T, int s, int c, float cut, F &&f) {
+    const size_t NT = T.nt, NC = T.nc;
+    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
+    const float R2 = (float)T.R2[c];
+    const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
+    const size_t tstride = NT * 3, cstride = NC * 3;
+    float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
+    float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2);
+    float mcur[3];
+    sep32(t0, t1, c0, c1, mcur);
+    for (int k = 0; k < n; k++) {
+        const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+        const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
+        const bool more = k + 1 < n;
+        float mnext[3] = {mcur[0], mcur[1], mcur[2]};
+        if (more) {
+            const float4 *tn = tp + (size_t)(k + 1) * tstride, *cn = cp + (size_t)(k + 1) * cstride;
+            t0 = tn[0]; t1 = tn[1]; t2 = tn[2];
+            c0 = __ldg(cn); c1 = __ldg(cn + 1); c2 = __ldg(cn + 2);
+            sep32(t0, t1, c0, c1, mnext);
+        }
+        Bound b;
+        if (point_bound32(St, Sc, R2, mcur, mnext, more, cut, b)) f(k, b);
+        mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
+    }
+}
+
+// ---- K1: FP32 filter over every pair -------------------------------------------------------------------------
+// ubmin[c][s] = the smallest upper bound over the pair's points (+inf if none); flag[c][s] = 1 when some point's
+// lower bound is under the cut (the pair may be kept), else 0.
+__global__ void __launch_bounds__(128) k_mx_scan32(ScreenTables T, float cut, unsigned char *__restrict__ flag,
+                                                   float *__restrict__ ubmin) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= T.nt) return;
+    for (int c = blockIdx.y; c < T.nc; c += gridDim.y) {
+        float ub = __int_as_float(0x7f800000), lb = ub;
+        walk32(T, s, c, cut, [&](int, const Bound &b) {
+            ub = fminf(ub, b.ub);
+            lb = fminf(lb, b.lb);
+        });
+        const size_t o = (size_t)c * T.nt + s;
+        flag[o] = lb < cut;
+        ubmin[o] = ub;
+    }
+}
+
+// ---- multi-block exclusive scan of int counts --------------------------------------------------------------------
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ int block_incl_scan(int v, int *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += t;
+    }
+    if (lane == 31) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int x = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, x, d);
+            if (lane >= d) x += t;
+        }
+        sh[lane] = x;
+    }
+    __syncthreads();
+    if (w > 0) v += sh[w - 1];
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_partials(int n, const int *__restrict__ in, int *__restrict__ part) {
+    __shared__ int sh[32];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const int v = i < n ? in[i] : 0;
+    const int incl = block_incl_scan(v, sh);
+    if (threadIdx.x == kScanBlock - 1) part[blockIdx.x] = incl;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_top(int nb, int *__restrict__ part, int *__restrict__ total) {
+    __shared__ int sh[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nb; base += kScanBlock) {
+        const int i = base + threadIdx.x;
+        const int v = i < nb ? part[i] : 0;
+        const int incl = block_incl_scan(v, sh);
+        if (i < nb) part[i] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == kScanBlock - 1) carry += incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kScanBlock) k_scan_apply(int n, const int *__restrict__ in,
+                                                           const int *__restrict__ part, int *__restrict__ out) {
+    __shared__ int sh[32];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const int v = i < n ? in[i] : 0;
+    const int incl = block_incl_scan(v, sh);
+    if (i < n) out[i] = part[blockIdx.x] + incl - v;
+}
+
+// exclusive scan of n ints into out, total into *total (device); part: ceil(n / 1024) ints of scratch
+int exclusive_scan(cudaStream_t st, int n, const int *in, int *out, int *part, int *total, std::string &err) {
+    const int nb = (n + kScanBlock - 1) / kScanBlock;
+    if (n <= 0) return check(cudaMemsetAsync(total, 0, 4, st), err, "scan total");
+    k_scan_partials<<<nb, kScanBlock, 0, st>>>(n, in, part);
+    k_scan_top<<<1, kScanBlock, 0, st>>>(nb, part, total);
+    k_scan_apply<<<nb, kScanBlock, 0, st>>>(n, in, part, out);
+    return check(cudaGetLastError(), err, "scan");
+}
+
+// ---- K2: possible pairs in (star, cluster) order --------------------------------------------------------------
+struct PossPair {
+    int s, c;
+    float ubmin;
+    int pad;
+};
+
+__global__ void k_mx_count(int nt, int nc, const unsigned char *__restrict__ flag, int *__restrict__ npair) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nt) return;
+    int a = 0;
+    for (int c = 0; c < nc; c++) a += flag[(size_t)c * nt + s];
+    npair[s] = a;
+}
+
+__global__ void k_mx_emit(int nt, int nc, const unsigned char *__restrict__ flag, const float *__restrict__ ubmin,
+                          const int *__restrict__ opair, PossPair *__restrict__ P) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nt) return;
+    int p = opair[s];
+    for (int c = 0; c < nc; c++) {
+        const size_t o = (size_t)c * nt + s;
+        if (!flag[o]) continue;
+        PossPair r;
+        r.s = s; r.c = c; r.ubmin = ubmin[o]; r.pad = 0;
+        P[p++] = r;
+    }
+}
+
+// ---- K3: candidate points of the possible pairs (counted, then written in point order) ------------------------
+// a point can be its pair's FP64 minimum only if lb_k <= (the pair's smallest ub) and lb_k < cut
+__global__ void k_mx_cand(ScreenTables T, float cut, int np, const PossPair *__restrict__ P, int *__restrict__ cnt,
+                          const int *__restrict__ off, int2 *__restrict__ E) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const PossPair r = P[p];
+    if (!E) {
+        int n = 0;
+        walk32(T, r.s, r.c, cut, [&](int, const Bound &b) { n += (b.lb < cut && b.lb <= r.ubmin); });
+        cnt[p] = n;
+    } else {
+        int e = off[p];
+        walk32(T, r.s, r.c, cut, [&](int k, const Bound &b) {
+            if (b.lb < cut && b.lb <= r.ubmin) E[e++] = make_int2(p, k);
+        });
+    }
+}
+
+// ---- K4..K6: FP64 rechecks --------------------------------------------------------------------------------------
+__device__ __forceinline__ double point64_at(const ScreenTables &T, int s, int c, int k, double cut, double &sv) {
+    const size_t NT = T.nt, NC = T.nc;
+    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
+    const double *tk = T.t64 + (size_t)k * 12 * NT + s, *ck = T.c64 + (size_t)k * 12 * NC + c;
+    double M[6], m0[3], m1[3];
+#pragma unroll
+    for (int i = 0; i < 6; i++) M[i] = tk[(6 + i) * NT] + ck[(6 + i) * NC];
+#pragma unroll
+    for (int i = 0; i < 3; i++) m0[i] = tk[i * NT] - ck[i * NC];
+    const bool more = k + 1 < n;
+    if (more) {
+#pragma unroll
+        for (int i = 0; i < 3; i++) m1[i] = tk[(12 + i) * NT] - ck[(12 + i) * NC];
+    } else {
+        m1[0] = m0[0]; m1[1] = m0[1]; m1[2] = m0[2];
+    }
+    return point_chi2_64(M, T.R2[c], m0, m1, more, cut, sv);
+}
+
+__global__ void k_mx_eval64(ScreenTables T, double cut, int ne, const PossPair *__restrict__ P,
+                            const int2 *__restrict__ E, double *__restrict__ ev, double *__restrict__ es) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int2 pk = E[e];
+    const PossPair p = P[pk.x];
+    double sv;
+    ev[e] = point64_at(T, p.s, p.c, pk.y, cut, sv);
+    es[e] = sv;
+}
+
+struct PairBest {
+    double chi2, sb;
+    int kb, pad;
+};
+
+// FP64 argmin over a pair's candidates (in point order: strict <, the first of equal minima wins)
+__global__ void k_mx_best(int np, const int *__restrict__ off, const int *__restrict__ cnt,
+                          const int2 *__restrict__ E, const double *__restrict__ ev, const double *__restrict__ es,
+                          PairBest *__restrict__ B) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    double best = kInf, sb = 0.0;
+    int kb = 0;
+    const int e0 = off[p], n = cnt[p];
+    for (int q = 0; q < n; q++) {
+        const double v = ev[e0 + q];
+        if (v >= 0 && v < best) { best = v; kb = E[e0 + q].y; sb = es[e0 + q]; }
+    }
+    PairBest o;
+    o.chi2 = best; o.sb = sb; o.kb = kb; o.pad = 0;
+    B[p] = o;
+}
+
+__global__ void k_mx_kept_flags(int np, const PairBest *__restrict__ B, double cut, int *__restrict__ f) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < np) f[p] = B[p].chi2 < cut;
+}
+
+__global__ void k_mx_kept_emit(int np, const PossPair *__restrict__ P, const PairBest *__restrict__ B, double cut,
+                               const int *__restrict__ off, KeptPair *__restrict__ K) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const PairBest b = B[p];
+    if (!(b.chi2 < cut)) return;
+    KeptPair k;
+    k.s = P[p].s; k.c = P[p].c; k.kb = b.kb; k.pad = 0; k.sb = b.sb; k.chi2 = b.chi2;
+    K[off[p]] = k;
+}
+
+// entries beyond this are screened by the FP64 selection instead (identical rows; bounds the work buffers)
+constexpr long long kMaxEntries = 400000000LL;
+
+int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &m, cudaEvent_t ev_scan, int *total,
+                 PgxStats *stats) {
+    std::string &err = m.err;
+    const int nt = T.nt, nc = T.nc;
+    const size_t pairs = (size_t)nt * nc;
+    int rc, launches = 0;
+    const int nbs = nt / kScanBlock + 2;
+    if ((rc = grow(m.flag, pairs, err)) || (rc = grow(m.ub, pairs * 4, err)) ||
+        (rc = grow(m.cnt, (size_t)nt * 4, err)) || (rc = grow(m.off, (size_t)nt * 4, err)) ||
+        (rc = grow(m.total, 64, err)) || (rc = grow(m.aux, (size_t)nbs * 4 + 64, err)))
+        return rc;
+    int *cnt = Pb<int>(m.cnt), *off = Pb<int>(m.off), *tot = Pb<int>(m.total), *part = Pb<int>(m.aux);
+    dim3 g((nt + 127) / 128, std::min(nc, 65535));
+    const float cutf = (float)cut;
+    k_mx_scan32<<<g, 128, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub));
+    if ((rc = check(cudaGetLastError(), err, "k_mx_scan32"))) return rc;
+    if ((rc = check(cudaEventRecord(ev_scan, st), err, "event"))) return rc;
+    k_mx_count<<<(nt + 127) / 128, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), cnt);
+    if ((rc = exclusive_scan(st, nt, cnt, off, part, tot, err))) return rc;
+    launches += 2 + 3;
+    int np = 0;
+    if ((rc = check(cudaMemcpyAsync(&np, tot, 4, cudaMemcpyDeviceToHost, st), err, "counts")) ||
+        (rc = check(cudaStreamSynchronize(st), err, "counts sync")))
+        return rc;
+    const int nbp = np / kScanBlock + 2;
+    if ((rc = grow(m.cand, (size_t)np * sizeof(PossPair) + 64, err)) ||
+        (rc = grow(m.cand_off, ((size_t)np * 2 + nbp) * 4 + 64, err)) ||
+        (rc = grow(m.entq, (size_t)np * (sizeof(PairBest) + 8) + 64, err)))
+        return rc;
+    PossPair *P = Pb<PossPair>(m.cand);
+    int *pc = Pb<int>(m.cand_off), *po = pc + np, *ppart = po + np;
+    PairBest *B = Pb<PairBest>(m.entq);
+    int *kf = reinterpret_cast<int *>(B + np), *ko = kf + np;
+    k_mx_emit<<<(nt + 127) / 128, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), Pb<float>(m.ub), off, P);
+    launches += 1;
+    int ne = 0;
+    if (np > 0) {
+        k_mx_cand<<<(np + 127) / 128, 128, 0, st>>>(T, cutf, np, P, pc, nullptr, nullptr);
+        if ((rc = exclusive_scan(st, np, pc, po, ppart, tot + 1, err))) return rc;
+        if ((rc = check(cudaMemcpyAsync(&ne, tot + 1, 4, cudaMemcpyDeviceToHost, st), err, "entries")) ||
+            (rc = check(cudaStreamSynchronize(st), err, "entries sync")))
+            return rc;
+        launches += 4;
+    }
+    if ((long long)ne > kMaxEntries) {
+        err = "mixed precision: too many candidate points for the work buffers";
+        return PGX_E_LIMIT;
+    }
+    if ((rc = grow(m.ent, (size_t)ne * (sizeof(int2) + 16) + 64, err))) return rc;
+    int2 *E = Pb<int2>(m.ent);
+    double *ev = reinterpret_cast<double *>(E + ne), *es = ev + ne;
+    int nk = 0;
+    if (np > 0) {
+        if (ne > 0) {
+            k_mx_cand<<<(np + 127) / 128, 128, 0, st>>>(T, cutf, np, P, pc, po, E);
+            k_mx_eval64<<<(ne + 127) / 128, 128, 0, st>>>(T, cut, ne, P, E, ev, es);
+            launches += 2;
+        }
+        k_mx_best<<<(np + 127) / 128, 128, 0, st>>>(np, po, pc, E, ev, es, B);
+        k_mx_kept_flags<<<(np + 255) / 256, 256, 0, st>>>(np, B, cut, kf);
+        if ((rc = exclusive_scan(st, np, kf, ko, ppart, tot + 3, err))) return rc;
+        if ((rc = check(cudaMemcpyAsync(&nk, tot + 3, 4, cudaMemcpyDeviceToHost, st), err, "kept")) ||
+            (rc = check(cudaStreamSynchronize(st), err, "kept sync")))
+            return rc;
+        if ((rc = grow(m.kept, (size_t)nk * sizeof(KeptPair) + 16, err))) return rc;
+        if (nk > 0) k_mx_kept_emit<<<(np + 255) / 256, 256, 0, st>>>(np, P, B, cut, ko, Pb<KeptPair>(m.kept));
+        if ((rc = check(cudaGetLastError(), err, "k_mx_kept_emit"))) return rc;
+        launches += 2 + 3 + (nk > 0);
+    } else if ((rc = grow(m.kept, 16, err))) {
+        return rc;
+    }
+    *total = nk;
+    if (stats) {
+        stats->candidates = np;
+        stats->rechecked_points = ne;
+        stats->kernels += launches;
+    }
+    return 0;
+}
+
+const KeptPair *mixed_kept(MixedBufs &m) { return (const KeptPair *)m.kept.p; }
+
+// ---- the 512 draws in FP32 --------------------------------------------------------------------------------------
+// Box-Muller radius^2 = -2 ln u1 and cos(2 pi u2) in FP32 from the 53-bit integers: ln u1 by log1pf(-v) with
+// v = 1 - u1 exact in integers when u1 >= 1/2 (no cancellation near u1 = 1), by logf otherwise (1 ulp each, plus
+// the rounding of u1 or v to FP32): relative error of the radius <= 1.6e-7; the cosine by cospif(2 u2) with absolute
+// error <= 3.1e-7 (pi x the rounding of 2 u2 to FP32, plus 1 ulp).  So |z - z_64| <= 5.3e-7 * radius, and with the
+// roundings of L, m and the three fused multiply-adds of x = m + L z, |x_i - x_i,64| <= 4 eps |m| + 16 eps |L| radius.
+__device__ __forceinline__ void gauss32(uint64_t a, uint64_t b, float &z, float &rad) {
+    const uint64_t k1 = a >> 11, k2 = b >> 11;
+    float r2;
+    if (k1 == 0) {
+        r2 = 88.7228391f;                               // -2 ln 2^-64, the reference's floor for u1 = 0
+    } else if (k1 >= (1ull << 52)) {
+        const float v = (float)(int64_t)((1ull << 53) - k1) * 1.1102230246251565e-16f;
+        r2 = -2.f * log1pf(-v);
+    } else {
+        r2 = -2.f * logf((float)(int64_t)k1 * 1.1102230246251565e-16f);
+    }
+    rad = sqrtf(r2);
+    z = rad * cospif(2.f * ((float)(int64_t)k2 * 1.1102230246251565e-16f));
+}
+
+struct Fin32 {
+    float mx, my, mz, l00, l10, l20, l11, l21, l22, r50s, rts, mabs, lsum, e50, etot;
+};
+
+__global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__restrict__ fin,
+                                                     ScreenRowDev *__restrict__ rows, int *__restrict__ nrecheck) {
+    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (h >= n) return;
+    const FinishIn f = fin[h];
+    Fin32 g;
+    g.mx = (float)f.mx; g.my = (float)f.my; g.mz = (float)f.mz;
+    g.l00 = (float)f.l00; g.l10 = (float)f.l10; g.l20 = (float)f.l20;
+    g.l11 = (float)f.l11; g.l21 = (float)f.l21; g.l22 = (float)f.l22;
+    g.r50s = (float)(f.r50 * f.r50); g.rts = (float)(f.rt * f.rt);
+    g.mabs = fabsf(g.mx) + fabsf(g.my) + fabsf(g.mz);
+    g.lsum = fabsf(g.l00) + fabsf(g.l10) + fabsf(g.l20) + fabsf(g.l11) + fabsf(g.l21) + fabsf(g.l22);
+    g.e50 = 8.f * kEps32 * g.r50s;                 // rounding of r50^2 and of the comparison
+    g.etot = 8.f * kEps32 * g.rts;
+    int in50 = 0, intot = 0, rechecks = 0;
+#pragma unroll 1
+    for (int q = 0; q < 16; q++) {
+        const int i = lane + 32 * q;
+        const uint64_t nn = 6ull * (uint64_t)i;
+        float z0, z1, z2, a0, a1, a2;
+        gauss32(splitmix_at(f.seed, nn + 1), splitmix_at(f.seed, nn + 2), z0, a0);
+        gauss32(splitmix_at(f.seed, nn + 3), splitmix_at(f.seed, nn + 4), z1, a1);
+        gauss32(splitmix_at(f.seed, nn + 5), splitmix_at(f.seed, nn + 6), z2, a2);
+        const float x = fmaf(g.l00, z0, g.mx);
+        const float y = fmaf(g.l11, z1, fmaf(g.l10, z0, g.my));
+        const float z = fmaf(g.l22, z2, fmaf(g.l21, z1, fmaf(g.l20, z0, g.mz)));
+        const float r2 = fmaf(x, x, fmaf(y, y, z * z));
+        // |x_i - x_i,64| <= ex for every component: 4 eps (|m| + |L||z|) plus |L| times the Gaussians' error
+        const float amax = fmaxf(a0, fmaxf(a1, a2));
+        const float ex = 4.f * kEps32 * g.mabs + (16.f * kEps32) * g.lsum * amax;
+        const float x1 = fabsf(x) + fabsf(y) + fabsf(z);
+        const float er = 3.f * kEps32 * r2 + 2.f * x1 * ex + 3.f * ex * ex;
+        const float d50 = r2 - g.r50s, dt = r2 - g.rts;
+        if (fabsf(d50) > er + g.e50 && fabsf(dt) > er + g.etot) {
+            in50 += d50 < 0.f;
+            intot += dt < 0.f;
+        } else {
+            const int v = draw_inside64(f, i);             // the FP64 path's own draw
+            in50 += v & 1;
+            intot += v >> 1;
+            rechecks++;
+        }
+    }
+    in50 = __reduce_add_sync(0xffffffffu, in50);
+    intot = __reduce_add_sync(0xffffffffu, intot);
+    rechecks = __reduce_add_sync(0xffffffffu, rechecks);
+    if (lane == 0) {
+        rows[h].p_r50 = (double)in50 / 512.0;
+        rows[h].p_rtot = (double)intot / 512.0;
+        if (rechecks) atomicAdd(nrecheck, rechecks);
+    }
+}
+
+int mixed_finish(cudaStream_t st, int n, const FinishIn *fin, ScreenRowDev *rows, MixedBufs &m, PgxStats *stats) {
+    int rc;
+    if ((rc = grow(m.total, 64, m.err))) return rc;
+    int *cnt = Pb<int>(m.total) + 8;
+    if ((rc = check(cudaMemsetAsync(cnt, 0, 4, st), m.err, "memset"))) return rc;
+    k_mx_finish32<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(n, fin, rows, cnt);
+    if (stats) stats->kernels += 0;     // counted with the finish prep by the caller
+    if ((rc = check(cudaGetLastError(), m.err, "k_mx_finish32"))) return rc;
+    int h = 0;
+    if ((rc = check(cudaMemcpyAsync(&h, cnt, 4, cudaMemcpyDeviceToHost, st), m.err, "rechecks"))) return rc;
+    if ((rc = check(cudaStreamSynchronize(st), m.err, "finish sync"))) return rc;
+    if (stats) stats->rechecked_draws = h;
+    return 0;
+}
+
+}  // namespace pgx
+
+namespace pgx {
+// Self-check of point_bound32: n independent points given in FP64 (star and cluster positions at the point and at
+// the next one, the two covariances, R^2), evaluated as the screen evaluates them -- the FP32 bounds from split
+// positions and FP32 covariances, and the FP64 point chi2.  rej[i] = 1 when FP32 rejects the point by the bound.
+__global__ void k_mx_check_bounds(int n, const double *__restrict__ pos, const double *__restrict__ S,
+                                  const double *__restrict__ R2, double cut, double *__restrict__ v64,
+                                  float *__restrict__ lb, float *__restrict__ ub, int *__restrict__ rej) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *p = pos + (size_t)i * 12;          // t0 c0 t1 c1, 3 each
+    const double *s = S + (size_t)i * 12;            // S_t, S_c
+    float4 q[4][2];
+    for (int a = 0; a < 4; a++) {
+        const float hx = (float)p[3 * a], hy = (float)p[3 * a + 1], hz = (float)p[3 * a + 2];
+        q[a][0] = make_float4(hx, hy, hz, (float)(p[3 * a] - (double)hx));
+        q[a][1] = make_float4((float)(p[3 * a + 1] - (double)hy), (float)(p[3 * a + 2] - (double)hz), 0.f, 0.f);
+    }
+    float m0[3], m1[3], St[6], Sc[6];
+    sep32(q[0][0], q[0][1], q[1][0], q[1][1], m0);
+    sep32(q[2][0], q[2][1], q[3][0], q[3][1], m1);
+    for (int j = 0; j < 6; j++) { St[j] = (float)s[j]; Sc[j] = (float)s[6 + j]; }
+    Bound b;
+    const bool dec = point_bound32(St, Sc, (float)R2[i], m0, m1, true, (float)cut, b);
+    double M[6], d0[3], d1[3], sv;
+    for (int j = 0; j < 6; j++) M[j] = s[j] + s[6 + j];
+    for (int j = 0; j < 3; j++) { d0[j] = p[j] - p[3 + j]; d1[j] = p[6 + j] - p[9 + j]; }
+    v64[i] = point_chi2_64(M, R2[i], d0, d1, true, cut, sv);
+    lb[i] = dec ? b.lb : 0.f;
+    ub[i] = dec ? b.ub : 0.f;
+    rej[i] = dec ? 0 : 1;
+}
+
+int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *S, const double *R2, double cut,
+                       double *v64, float *lb, float *ub, int *rej, std::string &err) {
+    k_mx_check_bounds<<<(n + 127) / 128, 128, 0, st>>>(n, pos, S, R2, cut, v64, lb, ub, rej);
+    return check(cudaGetLastError(), err, "k_mx_check_bounds");
+}
 }  // namespace pgx

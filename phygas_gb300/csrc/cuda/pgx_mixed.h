@@ -31,4 +31,8 @@ const KeptPair *mixed_kept(MixedBufs &m);
 // FP32 draws with an FP64 guard band: counts identical to the FP64 path's
 int mixed_finish(cudaStream_t st, int n, const FinishIn *fin, ScreenRowDev *rows, MixedBufs &m, PgxStats *stats);
 
+// self-check of the FP32 point bounds (pgx_check_bounds)
+int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *S, const double *R2, double cut,
+                       double *v64, float *lb, float *ub, int *rej, std::string &err);
+
 }  // namespace pgx

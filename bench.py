@@ -34,10 +34,10 @@ sys.path.insert(0, REPO)
 
 N_STARS, N_CLUSTERS, SEED = 20000, 4087, 1001
 CHI2_MAX, N_SAMP, R_KERNEL = 25.0, 64, 2.0
-# FP64 flops of one body step (one KDK leapfrog step of one orbit: 9 FMA-class operations plus one force
-# evaluation), counted from the executed FP64 instructions of the orbit kernel (ncu sass op counters, FMA = 2;
-# profiles/stm_orbits_screen20k.md)
-FLOPS_PER_BODY_STEP = 236.0
+# FP64 flops of one body step (one kick-drift-kick step of one orbit, its force evaluation included), from the
+# executed FP64 instructions of k_stm_orbits per body step: 40.4 DFMA + 7.5 DADD + 19.9 DMUL (ncu sass op counters,
+# FMA = 2 flops; profiles/k_stm_orbits.md)
+FLOPS_PER_BODY_STEP = 108.0
 # DRAM traffic of one orbit-kernel launch on this chunk, from one ncu capture (same profile summary), bytes
 ORBIT_TRAFFIC_BYTES = None
 

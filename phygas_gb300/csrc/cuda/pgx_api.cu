@@ -41,18 +41,18 @@ struct PgxContext {
     std::string err;
     // resident cluster table (original cluster order)
     int nc = 0, ncp = 0;
-    Buf c64, c32, cn, cR2, cr50, crt, cname;
+    Buf c64, c32, clm, cn, cR2, cr50, crt, cname;
     // the staged star chunk and the screen's work buffers
     int nt = 0;
     Buf s_ps0, s_sig21, s_prefix;
-    Buf opos, ovel, t64, t32;
+    Buf opos, ovel, t64, t32, tlm;
     Buf chi2T, kbT, sbT, cnt, off, total, kept, fin, rows;
     pgx::MixedBufs mixed;
     long n_rows = 0;
     // pair Monte Carlo
     Buf p_off, p_ps, p_steps, p_dt, p_r50, p_rt, p_items, p_q, p_done, p_cres, p_res;
     // one-object helpers of the drop-in API
-    Buf x_ps0, x_sig21, x_npts, x_opos, x_ovel, x_t64, x_t32;
+    Buf x_ps0, x_sig21, x_npts, x_opos, x_ovel, x_t64, x_t32, x_lm;
     PgxStats stats = {};
 };
 
@@ -122,7 +122,7 @@ void to_soa(int n, const double *ps0, const double *sig, std::vector<double> &p6
 
 // nominal + neighbour orbits of N objects (ps0 / sig21 device SoA, npts per slot or uniform) into t64 / t32
 int run_lin(PgxContext *ctx, int N, const double *d_ps0, const double *d_sig21, const int *d_npts, int nmax,
-            Buf &opos, Buf &ovel, double *t64, float4 *t32, bool timed) {
+            Buf &opos, Buf &ovel, double *t64, float4 *t32, float *lm, bool timed) {
     RET(ensure(ctx, opos, (size_t)nmax * 21 * N * sizeof(double)));
     RET(ensure(ctx, ovel, (size_t)nmax * 3 * N * sizeof(double)));
     dim3 g((N + 127) / 128, 7);
@@ -131,7 +131,7 @@ int run_lin(PgxContext *ctx, int N, const double *d_ps0, const double *d_sig21, 
     if (timed) CK(cudaEventRecord(ctx->ev[EV_ORBIT], ctx->st));
     const size_t work = (size_t)N * nmax;
     pgx::k_stm_cov<<<(unsigned)((work + 255) / 256), 256, 0, ctx->st>>>(N, nmax, d_npts, P<double>(opos),
-                                                                         P<double>(ovel), d_sig21, t64, t32);
+                                                                         P<double>(ovel), d_sig21, t64, t32, lm);
     CKL();
     if (timed) CK(cudaEventRecord(ctx->ev[EV_COV], ctx->st));
     ctx->stats.kernels += 2;
@@ -141,8 +141,9 @@ int run_lin(PgxContext *ctx, int N, const double *d_ps0, const double *d_sig21, 
 pgx::ScreenTables tables(PgxContext *ctx, int ns) {
     pgx::ScreenTables T;
     T.nt = ctx->nt; T.ns = ns; T.nc = ctx->nc; T.ncp = ctx->ncp;
-    T.t64 = P<double>(ctx->t64); T.t32 = P<float4>(ctx->t32); T.seed_prefix = P<uint64_t>(ctx->s_prefix);
-    T.c64 = P<double>(ctx->c64); T.c32 = P<float4>(ctx->c32); T.cn = P<int>(ctx->cn);
+    T.t64 = P<double>(ctx->t64); T.t32 = P<float4>(ctx->t32); T.lm_t = P<float>(ctx->tlm);
+    T.seed_prefix = P<uint64_t>(ctx->s_prefix);
+    T.c64 = P<double>(ctx->c64); T.c32 = P<float4>(ctx->c32); T.lm_c = P<float>(ctx->clm); T.cn = P<int>(ctx->cn);
     T.R2 = P<double>(ctx->cR2); T.r50 = P<double>(ctx->cr50); T.rtot = P<double>(ctx->crt);
     T.cname = P<char>(ctx->cname);
     return T;
@@ -191,7 +192,7 @@ int pgx_open(int device, PgxContext **out) {
 void pgx_close(PgxContext *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
-    Buf *bufs[] = {&ctx->c64, &ctx->c32, &ctx->cn, &ctx->cR2, &ctx->cr50, &ctx->crt, &ctx->cname, &ctx->s_ps0,
+    Buf *bufs[] = {&ctx->c64, &ctx->c32, &ctx->clm, &ctx->tlm, &ctx->x_lm, &ctx->cn, &ctx->cR2, &ctx->cr50, &ctx->crt, &ctx->cname, &ctx->s_ps0,
                    &ctx->s_sig21, &ctx->s_prefix, &ctx->opos, &ctx->ovel, &ctx->t64, &ctx->t32, &ctx->chi2T,
                    &ctx->kbT, &ctx->sbT, &ctx->cnt, &ctx->off, &ctx->total, &ctx->kept, &ctx->fin, &ctx->rows,
                    &ctx->p_off, &ctx->p_ps, &ctx->p_steps, &ctx->p_dt, &ctx->p_r50, &ctx->p_rt, &ctx->p_items,
@@ -292,12 +293,13 @@ int pgx_lin(PgxContext *ctx, int n, const double *ps0, const double *sig, const 
     RET(ensure(ctx, ctx->x_npts, (size_t)n * 4));
     RET(ensure(ctx, ctx->x_t64, (size_t)nmax * 12 * n * 8));
     RET(ensure(ctx, ctx->x_t32, (size_t)nmax * 3 * n * 16));
+    RET(ensure(ctx, ctx->x_lm, (size_t)nmax * n * 4));
     CK(cudaMemcpyAsync(ctx->x_ps0.p, p6.data(), p6.size() * 8, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->x_sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->x_npts.p, npts, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->st));
     ctx->stats = PgxStats();
     RET(run_lin(ctx, n, P<double>(ctx->x_ps0), P<double>(ctx->x_sig21), P<int>(ctx->x_npts), nmax, ctx->x_opos,
-                ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), false));
+                ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), P<float>(ctx->x_lm), false));
     std::vector<double> t((size_t)nmax * 12 * n);
     CK(cudaMemcpyAsync(t.data(), ctx->x_t64.p, t.size() * 8, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
@@ -337,8 +339,10 @@ int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double
     RET(ensure(ctx, ctx->x_npts, (size_t)nc * 4));
     RET(ensure(ctx, ctx->x_t64, (size_t)nmax * 12 * nc * 8));
     RET(ensure(ctx, ctx->x_t32, (size_t)nmax * 3 * nc * 16));
+    RET(ensure(ctx, ctx->x_lm, (size_t)nmax * nc * 4));
     RET(ensure(ctx, ctx->c64, (size_t)nmax * 12 * nc * 8));
     RET(ensure(ctx, ctx->c32, (size_t)nmax * 3 * nc * 16));
+    RET(ensure(ctx, ctx->clm, (size_t)nmax * nc * 4));
     RET(ensure(ctx, ctx->cn, (size_t)nc * 4));
     RET(ensure(ctx, ctx->cR2, (size_t)nc * 8));
     RET(ensure(ctx, ctx->cr50, (size_t)nc * 8));
@@ -349,10 +353,11 @@ int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double
     CK(cudaMemcpyAsync(ctx->x_npts.p, npts_slot.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, ctx->st));
     ctx->stats = PgxStats();
     RET(run_lin(ctx, nc, P<double>(ctx->x_ps0), P<double>(ctx->x_sig21), P<int>(ctx->x_npts), nmax, ctx->x_opos,
-                ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), false));
+                ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), P<float>(ctx->x_lm), false));
     // slot order -> cluster order (a column gather, once per table)
     MRET(pgx::gather_columns(ctx->st, nc, nmax, order.data(), P<double>(ctx->x_t64), P<float4>(ctx->x_t32),
-                            P<double>(ctx->c64), P<float4>(ctx->c32), ctx->mixed));
+                            P<float>(ctx->x_lm), P<double>(ctx->c64), P<float4>(ctx->c32), P<float>(ctx->clm),
+                            ctx->mixed));
     std::vector<double> R2(nc), r50(nc), rt(nc);
     for (int i = 0; i < nc; i++) {
         double R = (r_kernel > 0 ? r_kernel * r50_pc[i] : rtot_pc[i]) / 1000.0;
@@ -403,9 +408,10 @@ int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision,
     ctx->stats = PgxStats();
     RET(ensure(ctx, ctx->t64, (size_t)ns * 12 * nt * 8));
     RET(ensure(ctx, ctx->t32, (size_t)ns * 3 * nt * 16));
+    RET(ensure(ctx, ctx->tlm, (size_t)ns * nt * 4));
     CK(cudaEventRecord(ctx->ev[EV_START], ctx->st));
     RET(run_lin(ctx, nt, P<double>(ctx->s_ps0), P<double>(ctx->s_sig21), nullptr, ns, ctx->opos, ctx->ovel,
-                P<double>(ctx->t64), P<float4>(ctx->t32), true));
+                P<double>(ctx->t64), P<float4>(ctx->t32), P<float>(ctx->tlm), true));
     pgx::ScreenTables T = tables(ctx, ns);
     int total = 0;
     if (precision == PGX_FP64) {
@@ -654,7 +660,7 @@ int pair_tables(PgxContext *ctx, const PhLin *tl, const PhLin *cl, const PhClust
     T.nt = 1; T.ns = tl->n; T.nc = 1; T.ncp = cl->n;
     T.t64 = (const double *)base;
     T.c64 = (const double *)base + (size_t)nmax * 12;
-    T.t32 = nullptr; T.c32 = nullptr;
+    T.t32 = nullptr; T.c32 = nullptr; T.lm_t = nullptr; T.lm_c = nullptr;
     T.R2 = (const double *)a; T.r50 = (const double *)(a + 8); T.rtot = (const double *)(a + 16);
     T.seed_prefix = (const uint64_t *)(a + 24); T.cn = (const int *)(a + 32); T.cname = a + 40;
     return 0;

@@ -64,6 +64,28 @@ struct Orbit {
     }
 };
 
+// A lower bound on the smallest eigenvalue of a symmetric positive semi-definite 3x3 matrix (xx xy xz yy yz zz),
+// FP64, by the trigonometric solution of the characteristic cubic (Smith, Comm. ACM 4, 168, 1961).  The margin covers
+// the rounding of q + 2p cos(phi + 2 pi/3) (a few ulps of the trace) and the sensitivity of acos near r = 1 (the
+// eigenvalue moves by <= 1.8 p dphi, dphi <= sqrt(2 dr) / 3 with dr ~ 1e-15).
+// The bound is not clamped at zero: a matrix rounded to slightly indefinite keeps a valid (negative) bound.
+__device__ __forceinline__ double sym3_min_eig_lb(double a, double b, double c, double d, double e, double f) {
+    const double p1 = b * b + c * c + e * e;
+    const double tiny = 4.0 * 1.1102230246251565e-16 * (fabs(a) + fabs(d) + fabs(f));
+    if (p1 == 0.0) return fmin(a, fmin(d, f)) - tiny;
+    const double q = (a + d + f) * (1.0 / 3.0);
+    const double A = a - q, D = d - q, F = f - q;
+    const double p = sqrt((A * A + D * D + F * F + 2.0 * p1) * (1.0 / 6.0));
+    if (!(p > 0.0)) return q - tiny;
+    const double ip = 1.0 / p;
+    const double detB = (A * (D * F - e * e) - b * (b * F - e * c) + c * (b * e - D * c)) * (ip * ip * ip);
+    const double r = fmin(fmax(0.5 * detB, -1.0), 1.0);
+    const double phi = acos(r) * (1.0 / 3.0);
+    const double lmin = q + 2.0 * p * cos(phi + 2.0943951023931957);
+    const double margin = 4e-8 * p + 32.0 * 1.1102230246251565e-16 * (fabs(q) + 2.0 * p);
+    return lmin - margin;
+}
+
 // splitmix64 output for call n (n >= 1) of a generator seeded with `seed`: its state is a Weyl sequence,
 // state_n = seed + n * golden, so any draw of a pair's stream is reachable without the ones before it.
 __device__ __forceinline__ uint64_t splitmix_at(uint64_t seed, uint64_t n) {

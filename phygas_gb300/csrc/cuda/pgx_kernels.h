@@ -36,9 +36,11 @@ struct ScreenTables {
     int nc, ncp;                     // clusters, points of the longest cluster track
     const double *t64;
     const float4 *t32;
+    const float *lm_t;               // [k][nt]: lower bound on lambda_min(S) of the star track (FP32, rounded down)
     const uint64_t *seed_prefix;     // per star: FNV-1a state after "id|"
     const double *c64;
     const float4 *c32;
+    const float *lm_c;               // [k][nc]: the same for the cluster table
     const int *cn;
     const double *R2, *r50, *rtot;
     const char *cname;               // nc * 40 bytes
@@ -63,7 +65,7 @@ struct ScreenRowDev {                // layout-identical to PgxScreenRow (includ
 // ---- kernels ------------------------------------------------------------------------------------------------------
 __global__ void k_stm_orbits(int N, const double *ps0, const int *npts, int nmax, double *opos, double *ovel);
 __global__ void k_stm_cov(int N, int nmax, const int *npts, const double *opos, const double *ovel,
-                          const double *sig21, double *t64, float4 *t32);
+                          const double *sig21, double *t64, float4 *t32, float *lm);
 __global__ void k_pair_mc(McPairs P);
 __global__ void k_pair_reduce_big(McPairs P);
 __global__ void k_pair_reduce_only(McPairs P);

@@ -58,26 +58,29 @@ void mixed_free(MixedBufs &m) {
 
 // ---- cluster table: slot order (longest track first) -> cluster order ------------------------------------------
 __global__ void k_gather_cols(int nc, int nmax, const int *__restrict__ order, const double *__restrict__ s64,
-                              const float4 *__restrict__ s32, double *__restrict__ d64, float4 *__restrict__ d32) {
+                              const float4 *__restrict__ s32, const float *__restrict__ slm, double *__restrict__ d64,
+                              float4 *__restrict__ d32, float *__restrict__ dlm) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (size_t)nc * nmax) return;
     const int slot = (int)(idx % nc), k = (int)(idx / nc), col = order[slot];
     const size_t NC = nc;
     for (int f = 0; f < 12; f++) d64[((size_t)k * 12 + f) * NC + col] = s64[((size_t)k * 12 + f) * NC + slot];
     for (int q = 0; q < 3; q++) d32[((size_t)k * NC + col) * 3 + q] = s32[((size_t)k * NC + slot) * 3 + q];
+    dlm[(size_t)k * NC + col] = slm[(size_t)k * NC + slot];
 }
 
 int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, const double *t64_slot,
-                   const float4 *t32_slot, double *c64, float4 *c32, MixedBufs &m) {
+                   const float4 *t32_slot, const float *lm_slot, double *c64, float4 *c32, float *clm, MixedBufs &m) {
     int rc = grow(m.order, (size_t)nc * 4, m.err);
     if (rc) return rc;
     if ((rc = check(cudaMemcpyAsync(m.order.p, order_host, (size_t)nc * 4, cudaMemcpyHostToDevice, st), m.err, "order")))
         return rc;
     if ((rc = check(cudaMemsetAsync(c64, 0, (size_t)nmax * 12 * nc * 8, st), m.err, "memset"))) return rc;
     if ((rc = check(cudaMemsetAsync(c32, 0, (size_t)nmax * 3 * nc * 16, st), m.err, "memset"))) return rc;
+    if ((rc = check(cudaMemsetAsync(clm, 0, (size_t)nmax * nc * 4, st), m.err, "memset"))) return rc;
     const size_t work = (size_t)nc * nmax;
     k_gather_cols<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(nc, nmax, Pb<int>(m.order), t64_slot, t32_slot,
-                                                                   c64, c32);
+                                                                   lm_slot, c64, c32, clm);
     if ((rc = check(cudaGetLastError(), m.err, "k_gather_cols"))) return rc;
     return check(cudaStreamSynchronize(st), m.err, "gather sync");
 }
@@ -103,99 +106,127 @@ __device__ __forceinline__ float ldl_form(float l10, float l20, float l21, float
     return fmaf(y2 * y2, i3, fmaf(y1 * y1, i2, x * x * i1));
 }
 
-// Bounds on the FP64 path's point chi2 (the smaller of the forms at m0 and at the segment's nearest point to the
-// origin, pgx_screen_math.cuh point_chi2_64) from FP32 data.  Returns false when the point is rejected by the
-// reference's trace bound with a margin, i.e. when the FP64 path rejects it as well and never uses its value.
+// Bounds on the FP64 path's point chi2 v = min(q(m0), q(ms)) -- the forms at the step's start and at the segment's
+// nearest point to the origin, pgx_screen_math.cuh point_chi2_64 -- from FP32 data.  Returns false when the point is
+// rejected by the reference's trace bound with margins (see below): then v, if the FP64 path evaluates it at all,
+// is above the cut, and the point can neither be the minimum of a kept pair nor bring a pair under the cut.
 //
-// Lower bound, robust to any conditioning: for every x on the segment and u = its nearest point to the origin,
-// u.x >= |u|^2, and by Cauchy-Schwarz x^T M^-1 x >= (u.x)^2 / u^T M u, so the whole segment's forms are
-// >= |u|^4 / u^T M u (u^T M u needs no inversion and no cancellation bound beyond 10 eps (sum sqrt(M_ii)|u_i|)^2;
-// u's own FP32 error is taken off |u|).
-// Upper and lower bound from an FP32 LDL^T solve, when it is well conditioned: the computed form is exact for a
-// matrix within C1 eps tr(M) of M (storage, the two additions, the backward error of the factorization), and since
-// lambda_min(M) >= R^2 (both covariances are positive semi-definite), rho = C1 eps tr(M) / R^2 bounds the relative
-// change; plus C2 eps for the separations and the sums.  Used when rho <= 1/4.
-// Both are bounds on the exact form; the FP64 path's adjugate evaluation adds its own relative error
-// <= kAdj64 T^3 / det(M), with det(M) >= R^4 tr(M) / 3 (eigenvalues >= R^2, the largest >= tr/3), or from the FP32
-// pivots when rho <= 1/4.
-__device__ __forceinline__ bool point_bound32(const float (&St)[6], const float (&Sc)[6], float R2, const float (&m0)[3],
-                                              const float (&m1)[3], bool more, float cut, Bound &b) {
+// lam = R^2 + lmin(S_t) + lmin(S_c) <= lambda_min(M) (Weyl; the lmin are FP64 lower bounds from the covariance
+// kernel).  Bounds on the exact forms, then the FP64 path's own rounding on top:
+//  * Rayleigh, robust to any conditioning: for any vector w, x^T M^-1 x >= (w.x)^2 / w^T M w (Cauchy-Schwarz), and
+//    on the segment w.x >= min(w.m0, w.m1); with w = m0, m1 and the FP32 nearest point u this bounds the whole
+//    segment from below (w^T M w needs no inversion: error <= 10 eps (sum sqrt(M_ii) |w_i|)^2).
+//  * LDL^T in FP32 where it is well conditioned: the computed form is exact for a matrix within C1 eps tr(M) of M
+//    (storage, two additions, the factorization's backward error), so it moves by at most rho/(1-rho) relative,
+//    rho = C1 eps tr(M) / lam; C2 eps more for squares and sums.  A point that differs from the FP64 path's by
+//    <= d moves a form by <= 2 sqrt(q / lam) d + d^2 / lam in any direction: d0 = 3 eps |m0| for the start (hi/lo
+//    rounding), du for the nearest point.  Locating that point is ill-conditioned for a short step nearly
+//    tangent to the sphere through m0 (s = -m0.dr / |dr|^2), so du comes from the errors of m0.dr and |dr|^2, and is
+//    never more than the segment's own length (both points lie on it).
+//  * The FP64 adjugate evaluation adds relative error <= kAdj64 T^3 / det(M), det(M) >= lam^2 tr(M) / 3.
+// lb <= v <= ub: lb = max(Rayleigh, min(lb(q0), lb(qs))), ub = min(ub(q0), ub(qs)) (+inf without LDL^T).
+__device__ __forceinline__ bool point_bound32(const float (&St)[6], const float (&Sc)[6], float R2, float lmt, float lmc,
+                                              const float (&m0)[3], const float (&m1)[3], bool more, float cut,
+                                              Bound &b) {
     const float inf = __int_as_float(0x7f800000);
     const float M0 = St[0] + Sc[0] + R2, M1 = St[1] + Sc[1], M2 = St[2] + Sc[2];
     const float M3 = St[3] + Sc[3] + R2, M4 = St[4] + Sc[4], M5 = St[5] + Sc[5] + R2;
     const float tr = M0 + M3 + M5;
+    const float lam = (R2 + lmt + lmc) * (1.f - 16.f * kEps32);
     const float thr = 2.f * cut * tr;
     const float dx = m1[0] - m0[0], dy = m1[1] - m0[1], dz = m1[2] - m0[2];
     const float a = fmaf(m0[0], dx, fmaf(m0[1], dy, m0[2] * dz));
     const float dd = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float m00 = fmaf(m0[0], m0[0], fmaf(m0[1], m0[1], m0[2] * m0[2]));
     const float m11 = fmaf(m1[0], m1[0], fmaf(m1[1], m1[1], m1[2] * m1[2]));
-    // Rejected points: the exact distance satisfies dist^2 > 1.5 cut tr(M) (the FP32 test has a factor 2 and its
-    // cancellation is limited by the m00 guard), so the exact chi2 > 1.5 cut, and the FP64 path's value -- rejected
-    // by its own test, or evaluated with relative error < 1/3 (the tr / R^2 guard, see kAdj64) -- is above the cut:
-    // the point can be neither the minimum of a kept pair nor bring a pair under the cut.
+    // Rejection: the exact dist^2 > 1.5 cut tr (factor 2, cancellation limited by the m00 guard), so the exact chi2
+    // > 1.5 cut, and the FP64 path's value -- rejected by its own test, or evaluated with relative error < 1/3 (the
+    // tr / lam guard, see kAdj64) -- is above the cut.
     const float thr_m = thr * (1.f + 1e-5f);
     bool far;
     if (a >= 0.f) far = m00 > thr_m;
     else if (-a >= dd) far = m11 > thr_m;
     else far = (fmaf(m00, dd, -a * a) > thr_m * dd) && (m00 * (8.f * kEps32) < cut * tr);
-    if (far && tr < 1.8e6f * R2) return false;
-    // nearest point of the segment (FP32) and its error bound
+    if (far && tr < 1.8e6f * lam) return false;
+    if (!(lam > 0.f)) {
+        b.lb = 0.f;
+        b.ub = inf;
+        return true;
+    }
+    const float big = sqrtf(fmaxf(m00, m11));
+    const float n0 = sqrtf(m00);
+    const float dr_err = 8.f * kEps32 * big + 1e-12f;   // |FP32 dr - FP64 dr|: the rounding of m0 and m1
     float s = 0.f;
     if (more && dd > 0.f) s = fminf(fmaxf(-a / dd, 0.f), 1.f);
     const float ux = fmaf(dx, s, m0[0]), uy = fmaf(dy, s, m0[1]), uz = fmaf(dz, s, m0[2]);
-    const float big = sqrtf(fmaxf(m00, m11));
-    const float du = 8.f * kEps32 * big + 1e-12f;
-    const float uu = fmaf(ux, ux, fmaf(uy, uy, uz * uz));
-    // Rayleigh lower bound
-    const float uMu = fmaf(M0, ux * ux, fmaf(M3, uy * uy, fmaf(M5, uz * uz,
-                      2.f * fmaf(M1, ux * uy, fmaf(M2, ux * uz, M4 * uy * uz)))));
-    const float sw = sqrtf(M0) * fabsf(ux) + sqrtf(M3) * fabsf(uy) + sqrtf(M5) * fabsf(uz);
-    const float uMu_ub = fmaxf(uMu, 0.f) + 10.f * kEps32 * sw * sw;
-    const float un = fmaxf(sqrtf(uu) - du, 0.f);
-    const float g = fmaxf(fmaf(un, un, -du * big), 0.f);
-    float lb = uMu_ub > 0.f ? g * g / uMu_ub * (1.f - 8.f * kEps32) : 0.f;
+    float du = 3.f * kEps32 * n0 + 1e-12f;
+    if (more) {
+        const float dn = sqrtf(dd);
+        float dv = 2.f * dn + dr_err + 3.f * kEps32 * big;      // both points lie on the segment
+        if (dn > 2.f * dr_err) {
+            const float dd_lo = (dn - dr_err) * (dn - dr_err), dr_hi = dn + dr_err;
+            const float a_err = big * dr_err * (1.f + 4.f * kEps32) + 6.f * kEps32 * big * dn;
+            const float dd_err = 2.f * dn * dr_err + dr_err * dr_err + 4.f * kEps32 * dd;
+            const float ds = a_err / dd_lo + fabsf(a) * dd_err / (dd * dd_lo);
+            dv = fminf(dv, 3.f * kEps32 * big + dr_err + ds * dr_hi);
+        }
+        du = dv * (1.f + 8.f * kEps32);
+    }
+    // Rayleigh lower bound over the segment, w = m0, m1, u
+    float lb = 0.f;
+    {
+        const float sq0 = sqrtf(M0), sq3 = sqrtf(M3), sq5 = sqrtf(M5);
+        const float W[3][3] = {{m0[0], m0[1], m0[2]}, {m1[0], m1[1], m1[2]}, {ux, uy, uz}};
+#pragma unroll
+        for (int w = 0; w < 3; w++) {
+            if (w > 0 && !more) break;
+            const float wx = W[w][0], wy = W[w][1], wz = W[w][2];
+            const float wn = sqrtf(fmaf(wx, wx, fmaf(wy, wy, wz * wz)));
+            const float e0 = fmaf(wx, m0[0], fmaf(wy, m0[1], wz * m0[2]));
+            const float e1 = more ? fmaf(wx, m1[0], fmaf(wy, m1[1], wz * m1[2])) : e0;
+            const float t = fminf(e0, e1) - 9.f * kEps32 * wn * big;
+            const float wMw = fmaf(M0, wx * wx, fmaf(M3, wy * wy, fmaf(M5, wz * wz,
+                              2.f * fmaf(M1, wx * wy, fmaf(M2, wx * wz, M4 * wy * wz)))));
+            const float sw = fmaf(sq0, fabsf(wx), fmaf(sq3, fabsf(wy), sq5 * fabsf(wz)));
+            const float wMw_ub = fmaxf(wMw, 0.f) + 10.f * kEps32 * sw * sw;
+            if (t > 0.f && wMw_ub > 0.f) lb = fmaxf(lb, t * t / wMw_ub * (1.f - 8.f * kEps32));
+        }
+    }
     float ub = inf;
     // LDL^T
-    const float lam = R2 * (1.f - 4.f * kEps32);
     const float rho = kC1 * kEps32 * tr / lam;
     const float D1 = M0;
     const float i1 = 1.f / D1;
     const float l10 = M1 * i1, l20 = M2 * i1;
     const float D2 = fmaf(-l10, M1, M3);
     const float i2 = 1.f / D2;
-    const float u = fmaf(-l20, M1, M4);
-    const float l21 = u * i2;
-    const float D3 = fmaf(-l21, u, fmaf(-l20, M2, M5));
+    const float uu = fmaf(-l20, M1, M4);
+    const float l21 = uu * i2;
+    const float D3 = fmaf(-l21, uu, fmaf(-l20, M2, M5));
     const float i3 = 1.f / D3;
-    const bool ldl = D1 > 0.f && D2 > 0.f && D3 > 0.f && rho <= 0.25f && lam > 0.f;
-    // det(M) lower bound -> the FP64 path's own error
+    const bool ldl = D1 > 0.f && D2 > 0.f && D3 > 0.f && rho <= 0.25f;
     const float T = tr * (1.f + 4.f * kEps32);
     float det_lb = lam * lam * tr * (1.f / 3.f) * (1.f - 8.f * kEps32);
     if (ldl) {
+        const float rel = 2.f * rho + kC2 * kEps32;
+        const float il = 1.f / lam;
+        const float q0 = ldl_form(l10, l20, l21, i1, i2, i3, m0[0], m0[1], m0[2]);
+        const float d0 = 3.f * kEps32 * n0 + 1e-12f;
+        const float e0 = 2.f * sqrtf(q0 * (1.f + rel) * il) * d0 + d0 * d0 * il;
+        float lo = fmaf(q0, -rel, q0) - e0;
+        ub = fmaf(q0, rel, q0) + e0;
+        if (more) {
+            const float qs = ldl_form(l10, l20, l21, i1, i2, i3, ux, uy, uz);
+            const float es = 2.f * sqrtf(qs * (1.f + rel) * il) * du + du * du * il;
+            lo = fminf(lo, fmaf(qs, -rel, qs) - es);
+            ub = fminf(ub, fmaf(qs, rel, qs) + es);
+        }
+        lb = fmaxf(lb, lo);
         const float r1 = rho / (1.f - rho);
         const float f = 1.f - r1;
         det_lb = fmaxf(det_lb, D1 * D2 * D3 * (f * f * f) * (1.f - 8.f * kEps32));
     }
     const float r64 = det_lb > 0.f ? kAdj64 * (T * T) * (T / det_lb) : inf;
-    if (ldl) {
-        // a point that differs from the FP64 path's by <= d moves the form by <= 2 sqrt(q / lam) d + d^2 / lam,
-        // whatever the direction: the FP32 separation m0 (hi/lo rounding, <= 3 eps |m0|) and the segment point (du)
-        const float rel = 2.f * rho + kC2 * kEps32;
-        const float il = 1.f / lam;
-        const float q0 = ldl_form(l10, l20, l21, i1, i2, i3, m0[0], m0[1], m0[2]);
-        const float d0 = 3.f * kEps32 * sqrtf(m00) + 1e-12f;
-        const float e0 = 2.f * sqrtf(q0 * (1.f + rel) * il) * d0 + d0 * d0 * il;
-        float lo = fmaf(q0, -rel, q0) - e0, hi = fmaf(q0, rel, q0) + e0;
-        if (more) {
-            const float qs = ldl_form(l10, l20, l21, i1, i2, i3, ux, uy, uz);
-            const float ea = 2.f * sqrtf(qs * (1.f + rel) * il) * du + du * du * il;
-            lo = fminf(lo, fmaf(qs, -rel, qs) - ea);
-            hi = fminf(hi, fmaf(qs, rel, qs) + ea);
-        }
-        lb = fmaxf(lb, lo);
-        ub = hi;
-    }
     if (!(r64 < 0.5f)) {
         b.lb = 0.f;
         b.ub = inf;
@@ -229,6 +260,7 @@ __device__ __forceinline__ void walk32(const ScreenTables &T, int s, int c, floa
     for (int k = 0; k < n; k++) {
         const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
         const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
+        const float lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
         const bool more = k + 1 < n;
         float mnext[3] = {mcur[0], mcur[1], mcur[2]};
         if (more) {
@@ -238,7 +270,7 @@ __device__ __forceinline__ void walk32(const ScreenTables &T, int s, int c, floa
             sep32(t0, t1, c0, c1, mnext);
         }
         Bound b;
-        if (point_bound32(St, Sc, R2, mcur, mnext, more, cut, b)) f(k, b);
+        if (point_bound32(St, Sc, R2, lmt, lmc, mcur, mnext, more, cut, b)) f(k, b);
         mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
     }
 }
@@ -652,8 +684,11 @@ __global__ void k_mx_check_bounds(int n, const double *__restrict__ pos, const d
     sep32(q[0][0], q[0][1], q[1][0], q[1][1], m0);
     sep32(q[2][0], q[2][1], q[3][0], q[3][1], m1);
     for (int j = 0; j < 6; j++) { St[j] = (float)s[j]; Sc[j] = (float)s[6 + j]; }
+    const double lt = sym3_min_eig_lb(s[0], s[1], s[2], s[3], s[4], s[5]);
+    const double lc = sym3_min_eig_lb(s[6], s[7], s[8], s[9], s[10], s[11]);
     Bound b;
-    const bool dec = point_bound32(St, Sc, (float)R2[i], m0, m1, true, (float)cut, b);
+    const bool dec = point_bound32(St, Sc, (float)R2[i], __double2float_rd(lt - 1e-12 * fabs(lt)),
+                                   __double2float_rd(lc - 1e-12 * fabs(lc)), m0, m1, true, (float)cut, b);
     double M[6], d0[3], d1[3], sv;
     for (int j = 0; j < 6; j++) M[j] = s[j] + s[6 + j];
     for (int j = 0; j < 3; j++) { d0[j] = p[j] - p[3 + j]; d1[j] = p[6 + j] - p[9 + j]; }

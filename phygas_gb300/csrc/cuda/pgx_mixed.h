@@ -20,7 +20,7 @@ struct MixedBufs {
 void mixed_free(MixedBufs &m);
 // slot-ordered tracks (longest first) -> cluster-ordered table columns
 int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, const double *t64_slot,
-                   const float4 *t32_slot, double *c64, float4 *c32, MixedBufs &m);
+                   const float4 *t32_slot, const float *lm_slot, double *c64, float4 *c32, float *clm, MixedBufs &m);
 // per-cluster quantities the FP32 filter reads (kept resident with the table)
 int mixed_cluster_aux(cudaStream_t st, int nc, int nmax, const float4 *c32, const int *cn, const double *R2,
                       MixedBufs &m);

@@ -4,8 +4,9 @@
 //   k_stm_orbits   one thread per orbit: an object's nominal orbit and its 6 neighbours (+1e-5 on one phase-space
 //                  axis) are 7 independent threads, so a warp is 32 orbits with identical work and no barrier
 //                  (reference lin_integrate, src/phygas.c:286-323)
-//   k_stm_cov      one thread per (object, point): A = (neighbour - nominal) / eps, S = A Sigma0 A^T, and the two
-//                  track layouts the screen reads (FP64 for the exact stages, split FP32 for the filter)
+//   k_stm_cov      one thread per (object, point): A = (neighbour - nominal) / eps, S = A Sigma0 A^T, and the
+//                  track layouts the screen reads (FP64 for the exact stages, split FP32 for the filter, and a
+//                  lower bound on the smallest eigenvalue of S for the filter's error bounds)
 //   k_pair_mc      persistent: warps take items of <= 32 clones of one pair from a device queue (longest first),
 //                  trace them back with KDK leapfrog and the segment closest approach (reference ph_pair_clone,
 //                  src/phygas.c:200-216); the warp that finishes a pair's last item reduces it in registers
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(128) k_stm_orbits(int N, const double *__restr
 __global__ void __launch_bounds__(256) k_stm_cov(int N, int nmax, const int *__restrict__ npts,
                                                  const double *__restrict__ opos, const double *__restrict__ ovel,
                                                  const double *__restrict__ sig21, double *__restrict__ t64,
-                                                 float4 *__restrict__ t32) {
+                                                 float4 *__restrict__ t32, float *__restrict__ lm) {
     const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t NN = N;
     if (idx >= NN * nmax) return;
@@ -109,6 +110,9 @@ __global__ void __launch_bounds__(256) k_stm_cov(int N, int nmax, const int *__r
     o[0] = make_float4(hx, hy, hz, (float)(x0 - (double)hx));
     o[1] = make_float4((float)(y0 - (double)hy), (float)(z0 - (double)hz), (float)S[0], (float)S[1]);
     o[2] = make_float4((float)S[2], (float)S[3], (float)S[4], (float)S[5]);
+    // lower bound on lambda_min(S), rounded down to FP32, for the mixed-precision filter's error bounds
+    const double l = sym3_min_eig_lb(S[0], S[1], S[2], S[3], S[4], S[5]);
+    lm[(size_t)k * NN + i] = __double2float_rd(l - 1e-12 * fabs(l));
 }
 
 // ---------------------------------------------------------------------------------------------------------------

@@ -92,6 +92,19 @@ uint64_t pgx_seed_prefix(const char *target_id);
 int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,
              const double *dt, const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out);
 
+/* pgx_pair for callers that cannot allocate GPU memory (no counterpart in the reference): code running inside
+ * another framework's device memory pool, loops that must not stall on the allocator, hosts that can only hand
+ * over buffers they already own.  Every pointer is DEVICE memory the caller provides (clone_off[n_pairs + 1],
+ * ps[12 * n_clones], steps/dt/r50_pc/rtot_pc[n_pairs], res[n_pairs]); n_clones = clone_off[n_pairs].  The call only
+ * enqueues work on `stream` (a cudaStream_t, NULL = the legacy default stream) of the current device and returns;
+ * res is complete when the stream reaches that point.  No cudaMalloc, cudaFree or allocating library call: the
+ * per-clone scratch is a fixed 24 MiB array inside the library.  The first call on a device looks up that array's
+ * address (set-up); make it before any stream capture.  At most 2^20 clones per call (PGX_E_LIMIT beyond);
+ * pairs of more than 1024 clones get n = -1.  The scratch is shared by all calls and keeps the last call's
+ * contents: calls that overlap on the GPU race, so serialise them. */
+int pgx_pair_noalloc(void *stream, int n_pairs, int n_clones, const int *clone_off, const double *ps,
+                     const int *steps, const double *dt, const double *r50_pc, const double *rtot_pc, PhResult *res);
+
 /* ---- measurement ------------------------------------------------------------------------------------------------ */
 /* Device times (CUDA events on the context's stream) and counts of the last pgx_screen_exec / pgx_pair call. */
 typedef struct {

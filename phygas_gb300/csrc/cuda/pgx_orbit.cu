@@ -12,6 +12,11 @@
 //                  src/phygas.c:200-216); the warp that finishes a pair's last item reduces it in registers
 //                  with warp shuffles (reference ph_pair_reduce, src/phygas.c:218-238)
 //   k_pair_reduce_big  the same reduction for pairs of more than 1024 clones, one CTA per pair in shared memory
+#include <algorithm>
+#include <cstdio>
+#include <mutex>
+
+#include "phygas_gb300.h"
 #include "pgx_internal.cuh"
 #include "pgx_kernels.h"
 
@@ -429,3 +434,161 @@ __global__ void k_peak_ffma(float *out, int iters, float a, float b) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 }  // namespace pgx
+
+// ---------------------------------------------------------------------------------------------------------------
+// pgx_pair_noalloc: the pair Monte Carlo for callers that cannot allocate GPU memory.
+//
+// Some callers may not call cudaMalloc at all: code that runs inside another framework's memory pool (the pool
+// owns the device memory and a stray allocation fragments it or fails), real-time loops that must not stall on the
+// allocator, and host code that hands this library only the device buffers it already has.  This entry point takes
+// the caller's device buffers for inputs and outputs and keeps its own scratch -- the per-clone closest approaches
+// and the work-queue head -- in a fixed array compiled into the library (static __device__ storage, held by every
+// GPU that loads the library until the process exits).  It calls no allocating routine.
+//
+// Limits: at most kNoAllocMaxClones clones per call (24 MiB of scratch); pairs of more than 1024 clones get a result
+// with n = -1 (pgx_pair handles them).  Every call shares the one scratch array and leaves its contents behind; two
+// calls whose work overlaps on the GPU (different streams, or different host threads) race on it and must be
+// serialised by the caller.
+namespace pgx {
+
+constexpr int kNoAllocMaxClones = 1 << 20;
+
+// per-clone results: best (kpc), tbest (Myr), vbest (kpc/Myr), each kNoAllocMaxClones long
+static __device__ __align__(256) double g_noalloc_cres[3 * kNoAllocMaxClones];
+// work-queue head (cleared at the start of every call)
+static __device__ __align__(256) int g_noalloc_qhead[64];
+
+// persistent: warps take chunks of 32 consecutive clones; a lane finds its clone's pair by binary search
+__global__ void __launch_bounds__(kMcThreads) k_pair_mc_noalloc(int n_pairs, int n_clones,
+                                                                const int *__restrict__ clone_off,
+                                                                const double *__restrict__ ps,
+                                                                const int *__restrict__ steps,
+                                                                const double *__restrict__ dt, double *cres, int *qhead) {
+    const int lane = threadIdx.x & 31;
+    const int n_chunks = (n_clones + 31) / 32;
+    for (;;) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(qhead, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= n_chunks) break;
+        const int c = q * 32 + lane;
+        if (c < n_clones) {
+            int lo = 0, hi = n_pairs;          // clone_off[lo] <= c < clone_off[hi]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (clone_off[mid] <= c) lo = mid; else hi = mid;
+            }
+            double b, t, v;
+            trace_clone(ps + (size_t)c * 12, steps[lo], dt[lo], b, t, v);
+            cres[c] = b;
+            cres[kNoAllocMaxClones + c] = t;
+            cres[2 * (size_t)kNoAllocMaxClones + c] = v;
+        }
+    }
+}
+
+// one warp per pair, after all clones are traced (stream order)
+__global__ void __launch_bounds__(kMcThreads) k_pair_reduce_noalloc(int n_pairs, const int *__restrict__ clone_off,
+                                                                    const double *__restrict__ r50,
+                                                                    const double *__restrict__ rt,
+                                                                    const double *cres, PhResultDev *res) {
+    __shared__ double smem[kMcThreads / 32][1024];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int p = blockIdx.x * (kMcThreads / 32) + w;
+    if (p >= n_pairs) return;
+    const int o = clone_off[p], m = clone_off[p + 1] - o;
+    if (m <= 0 || m > 1024) {
+        if (lane == 0) {
+            PhResultDev z;
+            z.n = m <= 0 ? 0 : -1;
+            z.d05 = z.d50 = z.d95 = z.t05 = z.t50 = z.t95 = z.v05 = z.v50 = z.v95 = z.f_r50 = z.f_rtot = 0.0;
+            res[p] = z;
+        }
+        return;
+    }
+    const double *b = cres + o, *t = cres + kNoAllocMaxClones + o, *v = cres + 2 * (size_t)kNoAllocMaxClones + o;
+    if (m <= 32) warp_reduce_pair<1>(b, t, v, m, r50[p], rt[p], smem[w], res + p, lane);
+    else if (m <= 64) warp_reduce_pair<2>(b, t, v, m, r50[p], rt[p], smem[w], res + p, lane);
+    else if (m <= 128) warp_reduce_pair<4>(b, t, v, m, r50[p], rt[p], smem[w], res + p, lane);
+    else if (m <= 256) warp_reduce_pair<8>(b, t, v, m, r50[p], rt[p], smem[w], res + p, lane);
+    else if (m <= 512) warp_reduce_pair<16>(b, t, v, m, r50[p], rt[p], smem[w], res + p, lane);
+    else warp_reduce_pair<32>(b, t, v, m, r50[p], rt[p], smem[w], res + p, lane);
+}
+
+namespace {
+// set-up, once per device: the device addresses of the scratch arrays (in host code their names are host-side
+// stand-ins, not device addresses) and the persistent grid size
+struct NoAllocDevice {
+    double *cres = nullptr;
+    int *qhead = nullptr;
+    int grid = 0;
+    bool ready = false;
+};
+NoAllocDevice g_noalloc_dev[64];
+std::mutex g_noalloc_mu;
+
+int noalloc_setup(int dev, NoAllocDevice *&out) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoAllocDevice &d = g_noalloc_dev[dev];
+    if (!d.ready) {
+        cudaError_t e = cudaGetSymbolAddress((void **)&d.cres, g_noalloc_cres);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&d.qhead, g_noalloc_qhead);
+        int sms = 0, per_sm = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_mc_noalloc, kMcThreads, 0);
+        if (e != cudaSuccess) {
+            fprintf(stderr, "pgx_pair_noalloc: set-up on device %d failed: %s\n", dev, cudaGetErrorString(e));
+            return PGX_E_CUDA;
+        }
+        d.grid = sms * (per_sm > 0 ? per_sm : 1);
+        d.ready = true;
+    }
+    out = &d;
+    return 0;
+}
+}  // namespace
+}  // namespace pgx
+
+extern "C" int pgx_pair_noalloc(void *stream, int n_pairs, int n_clones, const int *clone_off, const double *ps,
+                                const int *steps, const double *dt, const double *r50_pc, const double *rtot_pc,
+                                PhResult *res) {
+    if (n_pairs < 0 || n_clones < 0 || (n_pairs > 0 && (!clone_off || !steps || !dt || !r50_pc || !rtot_pc || !res)) ||
+        (n_clones > 0 && !ps)) {
+        fprintf(stderr, "pgx_pair_noalloc: invalid arguments\n");
+        return PGX_E_ARG;
+    }
+    if (n_clones > pgx::kNoAllocMaxClones) {
+        fprintf(stderr, "pgx_pair_noalloc: %d clones in one call; its fixed scratch holds %d (use pgx_pair)\n",
+                n_clones, pgx::kNoAllocMaxClones);
+        return PGX_E_LIMIT;
+    }
+    if (n_pairs == 0) return 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 64) {
+        fprintf(stderr, "pgx_pair_noalloc: no current device (%s)\n", cudaGetErrorString(e));
+        return PGX_E_NODEV;
+    }
+    pgx::NoAllocDevice *d = nullptr;
+    int rc = pgx::noalloc_setup(dev, d);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    e = cudaMemsetAsync(d->qhead, 0, sizeof(int), st);
+    if (e == cudaSuccess && n_clones > 0) {
+        const int grid = std::max(1, std::min(d->grid, (n_clones + 127) / 128));
+        pgx::k_pair_mc_noalloc<<<grid, pgx::kMcThreads, 0, st>>>(n_pairs, n_clones, clone_off, ps, steps, dt,
+                                                                  d->cres, d->qhead);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        const int wpb = pgx::kMcThreads / 32;
+        pgx::k_pair_reduce_noalloc<<<(n_pairs + wpb - 1) / wpb, pgx::kMcThreads, 0, st>>>(
+            n_pairs, clone_off, r50_pc, rtot_pc, d->cres, reinterpret_cast<pgx::PhResultDev *>(res));
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        fprintf(stderr, "pgx_pair_noalloc: launch failed: %s\n", cudaGetErrorString(e));
+        return PGX_E_CUDA;
+    }
+    return 0;
+}

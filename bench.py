@@ -274,6 +274,8 @@ def main():
             "plain_fp64": {"value": ws * pairs / (ms64 * 1e-3), "unit": "pairs/s", "ms_per_step": ms64,
                            "speedup_of_value": ms64 / ms},
             "rows_per_step": n_rows, "rows_fp64": n_rows64,
+            "work_per_step": {k: int(s[k]) for k in ("candidates", "ambiguous", "rechecked_points",
+                                                     "rechecked_draws", "kept")},
             "stages_ms": {k: statistics.mean(x[k] for x in stats) for k in
                           ("ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish")},
             "stages_ms_fp64": {k: statistics.mean(x[k] for x in stats64) for k in

@@ -110,6 +110,8 @@ int pgx_pair_noalloc(void *stream, int n_pairs, int n_clones, const int *clone_o
 typedef struct {
     double ms_total, ms_orbit, ms_cov, ms_scan, ms_select, ms_finish, ms_pair;
     long pairs, kept, candidates, rechecked_points, rechecked_draws, clones, clone_steps, body_steps;
+    long ambiguous;                  /* mixed screen: pairs that may be kept (candidates) whose candidate points
+                                        were found by a second walk; rechecked_points = points evaluated in FP64 */
     int kernels;                     /* kernel launches of the call */
 } PgxStats;
 int pgx_stats(const PgxContext *ctx, PgxStats *out);
@@ -122,7 +124,8 @@ int pgx_peaks(PgxContext *ctx, double *fp64_flops, double *fp32_flops);
  * FP64 -- pos[12n] = star and cluster positions at the point and at the next (t0 c0 t1 c1), S[12n] = the star's and
  * the cluster's covariance (xx xy xz yy yz zz), R2[n] -- returns the FP64 point chi2 (v64; -1 singular, +inf
  * rejected by the trace bound) and the FP32 filter's bounds lb <= v64 <= ub, or rej = 1 where the filter rejects
- * the point (then v64 >= chi2_max). */
+ * the point (then v64 >= chi2_max); rej = 2 where its cheap pre-test skips the point (then v64 >= chi2_max too; the
+ * bounds are returned). */
 int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S, const double *R2, double chi2_max,
                      double *v64, float *lb, float *ub, int *rej);
 

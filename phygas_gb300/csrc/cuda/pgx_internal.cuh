@@ -88,11 +88,12 @@ __device__ __forceinline__ double sym3_min_eig_lb(double a, double b, double c, 
 
 // splitmix64 output for call n (n >= 1) of a generator seeded with `seed`: its state is a Weyl sequence,
 // state_n = seed + n * golden, so any draw of a pair's stream is reachable without the ones before it.
-__device__ __forceinline__ uint64_t splitmix_at(uint64_t seed, uint64_t n) {
-    uint64_t z = seed + n * 0x9E3779B97F4A7C15ULL;
+constexpr uint64_t kGolden = 0x9E3779B97F4A7C15ULL;
+__device__ __forceinline__ uint64_t splitmix_mix(uint64_t z) {      // output for state z
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
     return z ^ (z >> 31);
 }
+__device__ __forceinline__ uint64_t splitmix_at(uint64_t seed, uint64_t n) { return splitmix_mix(seed + n * kGolden); }
 
 }  // namespace pgx

@@ -43,6 +43,7 @@ struct ScreenTables {
     const float *lm_c;               // [k][nc]: the same for the cluster table
     const int *cn;
     const double *R2, *r50, *rtot;
+    const float *R2f;                // R2 rounded to FP32 (the mixed-precision filter)
     const char *cname;               // nc * 40 bytes
 };
 

@@ -9,17 +9,20 @@
 //   k_mx_scan32      FP32 filter, one thread per pair (warp = 32 stars x one cluster).  Per point: the reference's
 //                    trace bound (chi2 >= dist^2 / trace M), then bounds LB <= chi2_64 <= UB on the FP64 path's
 //                    value (a Rayleigh lower bound that needs no inversion, and an LDL^T solve where it is well
-//                    conditioned).  Per pair: may it be kept (some LB < cut), and its smallest UB.
+//                    conditioned).
+//                    Per pair: its candidate points -- those that can be the FP64 minimum of a kept pair
+//                    (LB_k < cut, LB_k <= min UB) -- in four slots, or "more than four".
 //   k_mx_count / k_mx_emit   stable compaction, per star, of the pairs that may be kept
-//   k_mx_cand        those pairs again: the points that can be the FP64 minimum (LB_k <= min UB, LB_k < cut),
-//                    counted, then written in point order after a scan
+//   k_mx_list_*      the listed candidates written out; k_mx_cand walks the overflowed pairs again for theirs
 //   k_mx_eval64      one thread per candidate point: the FP64 point chi2 (full warps on the scarce FP64 pipe)
-//   k_mx_best        per possible pair: FP64 argmin over its candidates, strict < in point order
+//   k_mx_best        per possible pair: FP64 argmin over its candidates (smallest value, first point of equals)
 //   k_mx_kept_*      stable compaction of the pairs under the cut
 //   k_mx_finish32    one warp per kept pair: the 512 draws in FP32 with a per-draw error bound; a draw whose
 //                    distance is within the bound of r50 or rtot is redone in FP64
 #include <algorithm>
 #include <vector>
+#include "pgx_bits.cuh"
+#include "pgx_bounds32.cuh"
 #include "pgx_internal.cuh"
 #include "pgx_mixed.h"
 #include "pgx_screen_math.cuh"
@@ -50,7 +53,7 @@ template <class T> T *Pb(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
 }  // namespace
 
 void mixed_free(MixedBufs &m) {
-    DevBuf *all[] = {&m.order, &m.ub, &m.flag, &m.cnt, &m.off, &m.total, &m.kept, &m.cand, &m.cand_off,
+    DevBuf *all[] = {&m.order, &m.ub, &m.kmin, &m.flag, &m.cnt, &m.off, &m.total, &m.kept, &m.cand, &m.cand_off,
                      &m.ent, &m.entq, &m.aux};
     for (DevBuf *b : all)
         if (b->p) { cudaFree(b->p); b->p = nullptr; b->cap = 0; }
@@ -87,156 +90,6 @@ int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, con
 
 int mixed_cluster_aux(cudaStream_t, int, int, const float4 *, const int *, const double *, MixedBufs &) { return 0; }
 
-// ---- the FP32 point evaluation with its error bounds ------------------------------------------------------------
-constexpr float kEps32 = 5.9604645e-8f;      // 2^-24
-constexpr float kC1 = 48.f, kC2 = 32.f;
-// relative error of the FP64 path's adjugate form m^T adj(M) m / det(M) (pgx_screen_math.cuh): cofactors, det
-// and numerator each lose at most a few hundred ulps of T^3 / det, T = trace(M) (all |M_ij| <= T); 256 eps_64
-constexpr float kAdj64 = 2.85e-14f;
-
-struct Bound {
-    float lb, ub;          // lb <= the FP64 path's point chi2 <= ub (ub = +inf: no upper bound)
-};
-
-// m^T (L D L^T)^-1 m with the factors of one point
-__device__ __forceinline__ float ldl_form(float l10, float l20, float l21, float i1, float i2, float i3, float x,
-                                          float y, float z) {
-    const float y1 = fmaf(-l10, x, y);
-    const float y2 = fmaf(-l21, y1, fmaf(-l20, x, z));
-    return fmaf(y2 * y2, i3, fmaf(y1 * y1, i2, x * x * i1));
-}
-
-// Bounds on the FP64 path's point chi2 v = min(q(m0), q(ms)) -- the forms at the step's start and at the segment's
-// nearest point to the origin, pgx_screen_math.cuh point_chi2_64 -- from FP32 data.  Returns false when the point is
-// rejected by the reference's trace bound with margins (see below): then v, if the FP64 path evaluates it at all,
-// is above the cut, and the point can neither be the minimum of a kept pair nor bring a pair under the cut.
-//
-// lam = R^2 + lmin(S_t) + lmin(S_c) <= lambda_min(M) (Weyl; the lmin are FP64 lower bounds from the covariance
-// kernel).  Bounds on the exact forms, then the FP64 path's own rounding on top:
-//  * Rayleigh, robust to any conditioning: for any vector w, x^T M^-1 x >= (w.x)^2 / w^T M w (Cauchy-Schwarz), and
-//    on the segment w.x >= min(w.m0, w.m1); with w = m0, m1 and the FP32 nearest point u this bounds the whole
-//    segment from below (w^T M w needs no inversion: error <= 10 eps (sum sqrt(M_ii) |w_i|)^2).
-//  * LDL^T in FP32 where it is well conditioned: the computed form is exact for a matrix within C1 eps tr(M) of M
-//    (storage, two additions, the factorization's backward error), so it moves by at most rho/(1-rho) relative,
-//    rho = C1 eps tr(M) / lam; C2 eps more for squares and sums.  A point that differs from the FP64 path's by
-//    <= d moves a form by <= 2 sqrt(q / lam) d + d^2 / lam in any direction: d0 = 3 eps |m0| for the start (hi/lo
-//    rounding), du for the nearest point.  Locating that point is ill-conditioned for a short step nearly
-//    tangent to the sphere through m0 (s = -m0.dr / |dr|^2), so du comes from the errors of m0.dr and |dr|^2, and is
-//    never more than the segment's own length (both points lie on it).
-//  * The FP64 adjugate evaluation adds relative error <= kAdj64 T^3 / det(M), det(M) >= lam^2 tr(M) / 3.
-// lb <= v <= ub: lb = max(Rayleigh, min(lb(q0), lb(qs))), ub = min(ub(q0), ub(qs)) (+inf without LDL^T).
-__device__ __forceinline__ bool point_bound32(const float (&St)[6], const float (&Sc)[6], float R2, float lmt, float lmc,
-                                              const float (&m0)[3], const float (&m1)[3], bool more, float cut,
-                                              Bound &b) {
-    const float inf = __int_as_float(0x7f800000);
-    const float M0 = St[0] + Sc[0] + R2, M1 = St[1] + Sc[1], M2 = St[2] + Sc[2];
-    const float M3 = St[3] + Sc[3] + R2, M4 = St[4] + Sc[4], M5 = St[5] + Sc[5] + R2;
-    const float tr = M0 + M3 + M5;
-    const float lam = (R2 + lmt + lmc) * (1.f - 16.f * kEps32);
-    const float thr = 2.f * cut * tr;
-    const float dx = m1[0] - m0[0], dy = m1[1] - m0[1], dz = m1[2] - m0[2];
-    const float a = fmaf(m0[0], dx, fmaf(m0[1], dy, m0[2] * dz));
-    const float dd = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float m00 = fmaf(m0[0], m0[0], fmaf(m0[1], m0[1], m0[2] * m0[2]));
-    const float m11 = fmaf(m1[0], m1[0], fmaf(m1[1], m1[1], m1[2] * m1[2]));
-    // Rejection: the exact dist^2 > 1.5 cut tr (factor 2, cancellation limited by the m00 guard), so the exact chi2
-    // > 1.5 cut, and the FP64 path's value -- rejected by its own test, or evaluated with relative error < 1/3 (the
-    // tr / lam guard, see kAdj64) -- is above the cut.
-    const float thr_m = thr * (1.f + 1e-5f);
-    bool far;
-    if (a >= 0.f) far = m00 > thr_m;
-    else if (-a >= dd) far = m11 > thr_m;
-    else far = (fmaf(m00, dd, -a * a) > thr_m * dd) && (m00 * (8.f * kEps32) < cut * tr);
-    if (far && tr < 1.8e6f * lam) return false;
-    if (!(lam > 0.f)) {
-        b.lb = 0.f;
-        b.ub = inf;
-        return true;
-    }
-    const float big = sqrtf(fmaxf(m00, m11));
-    const float n0 = sqrtf(m00);
-    const float dr_err = 8.f * kEps32 * big + 1e-12f;   // |FP32 dr - FP64 dr|: the rounding of m0 and m1
-    float s = 0.f;
-    if (more && dd > 0.f) s = fminf(fmaxf(-a / dd, 0.f), 1.f);
-    const float ux = fmaf(dx, s, m0[0]), uy = fmaf(dy, s, m0[1]), uz = fmaf(dz, s, m0[2]);
-    float du = 3.f * kEps32 * n0 + 1e-12f;
-    if (more) {
-        const float dn = sqrtf(dd);
-        float dv = 2.f * dn + dr_err + 3.f * kEps32 * big;      // both points lie on the segment
-        if (dn > 2.f * dr_err) {
-            const float dd_lo = (dn - dr_err) * (dn - dr_err), dr_hi = dn + dr_err;
-            const float a_err = big * dr_err * (1.f + 4.f * kEps32) + 6.f * kEps32 * big * dn;
-            const float dd_err = 2.f * dn * dr_err + dr_err * dr_err + 4.f * kEps32 * dd;
-            const float ds = a_err / dd_lo + fabsf(a) * dd_err / (dd * dd_lo);
-            dv = fminf(dv, 3.f * kEps32 * big + dr_err + ds * dr_hi);
-        }
-        du = dv * (1.f + 8.f * kEps32);
-    }
-    // Rayleigh lower bound over the segment, w = m0, m1, u
-    float lb = 0.f;
-    {
-        const float sq0 = sqrtf(M0), sq3 = sqrtf(M3), sq5 = sqrtf(M5);
-        const float W[3][3] = {{m0[0], m0[1], m0[2]}, {m1[0], m1[1], m1[2]}, {ux, uy, uz}};
-#pragma unroll
-        for (int w = 0; w < 3; w++) {
-            if (w > 0 && !more) break;
-            const float wx = W[w][0], wy = W[w][1], wz = W[w][2];
-            const float wn = sqrtf(fmaf(wx, wx, fmaf(wy, wy, wz * wz)));
-            const float e0 = fmaf(wx, m0[0], fmaf(wy, m0[1], wz * m0[2]));
-            const float e1 = more ? fmaf(wx, m1[0], fmaf(wy, m1[1], wz * m1[2])) : e0;
-            const float t = fminf(e0, e1) - 9.f * kEps32 * wn * big;
-            const float wMw = fmaf(M0, wx * wx, fmaf(M3, wy * wy, fmaf(M5, wz * wz,
-                              2.f * fmaf(M1, wx * wy, fmaf(M2, wx * wz, M4 * wy * wz)))));
-            const float sw = fmaf(sq0, fabsf(wx), fmaf(sq3, fabsf(wy), sq5 * fabsf(wz)));
-            const float wMw_ub = fmaxf(wMw, 0.f) + 10.f * kEps32 * sw * sw;
-            if (t > 0.f && wMw_ub > 0.f) lb = fmaxf(lb, t * t / wMw_ub * (1.f - 8.f * kEps32));
-        }
-    }
-    float ub = inf;
-    // LDL^T
-    const float rho = kC1 * kEps32 * tr / lam;
-    const float D1 = M0;
-    const float i1 = 1.f / D1;
-    const float l10 = M1 * i1, l20 = M2 * i1;
-    const float D2 = fmaf(-l10, M1, M3);
-    const float i2 = 1.f / D2;
-    const float uu = fmaf(-l20, M1, M4);
-    const float l21 = uu * i2;
-    const float D3 = fmaf(-l21, uu, fmaf(-l20, M2, M5));
-    const float i3 = 1.f / D3;
-    const bool ldl = D1 > 0.f && D2 > 0.f && D3 > 0.f && rho <= 0.25f;
-    const float T = tr * (1.f + 4.f * kEps32);
-    float det_lb = lam * lam * tr * (1.f / 3.f) * (1.f - 8.f * kEps32);
-    if (ldl) {
-        const float rel = 2.f * rho + kC2 * kEps32;
-        const float il = 1.f / lam;
-        const float q0 = ldl_form(l10, l20, l21, i1, i2, i3, m0[0], m0[1], m0[2]);
-        const float d0 = 3.f * kEps32 * n0 + 1e-12f;
-        const float e0 = 2.f * sqrtf(q0 * (1.f + rel) * il) * d0 + d0 * d0 * il;
-        float lo = fmaf(q0, -rel, q0) - e0;
-        ub = fmaf(q0, rel, q0) + e0;
-        if (more) {
-            const float qs = ldl_form(l10, l20, l21, i1, i2, i3, ux, uy, uz);
-            const float es = 2.f * sqrtf(qs * (1.f + rel) * il) * du + du * du * il;
-            lo = fminf(lo, fmaf(qs, -rel, qs) - es);
-            ub = fminf(ub, fmaf(qs, rel, qs) + es);
-        }
-        lb = fmaxf(lb, lo);
-        const float r1 = rho / (1.f - rho);
-        const float f = 1.f - r1;
-        det_lb = fmaxf(det_lb, D1 * D2 * D3 * (f * f * f) * (1.f - 8.f * kEps32));
-    }
-    const float r64 = det_lb > 0.f ? kAdj64 * (T * T) * (T / det_lb) : inf;
-    if (!(r64 < 0.5f)) {
-        b.lb = 0.f;
-        b.ub = inf;
-        return true;
-    }
-    b.lb = fmaxf(lb * (1.f - r64), 0.f);
-    b.ub = ub < inf ? ub * (1.f + r64) * (1.f + 4.f * kEps32) : inf;
-    return true;
-}
-
 // separation of star and cluster at one point from the split FP32 positions
 __device__ __forceinline__ void sep32(const float4 &t0, const float4 &t1, const float4 &c0, const float4 &c1,
                                       float (&m)[3]) {
@@ -245,12 +98,13 @@ __device__ __forceinline__ void sep32(const float4 &t0, const float4 &t1, const 
     m[2] = (t0.z - c0.z) + (t1.y - c1.y);
 }
 
-// Walks the points of one (star, cluster) pair in order, calling f(k, bound) for every point the trace bound keeps.
+// Walks the points of one (star, cluster) pair in order, calling f(k, bound) for every point the cheap test
+// (point_skip32) keeps.
 template <class F>
 __device__ __forceinline__ void walk32(const ScreenTables &T, int s, int c, float cut, F &&f) {
     const size_t NT = T.nt, NC = T.nc;
     const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
-    const float R2 = (float)T.R2[c];
+    const float R2 = T.R2f[c];
     const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
     const size_t tstride = NT * 3, cstride = NC * 3;
     float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
@@ -270,27 +124,147 @@ __device__ __forceinline__ void walk32(const ScreenTables &T, int s, int c, floa
             sep32(t0, t1, c0, c1, mnext);
         }
         Bound b;
-        if (point_bound32(St, Sc, R2, lmt, lmc, mcur, mnext, more, cut, b)) f(k, b);
+        if (!point_skip32(St, Sc, R2, lmt, lmc, mcur, mnext, cut) &&
+            point_bound32(St, Sc, R2, lmt, lmc, mcur, mnext, more, cut, b))
+            f(k, b);
         mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
     }
 }
 
 // ---- K1: FP32 filter over every pair -------------------------------------------------------------------------
-// ubmin[c][s] = the smallest upper bound over the pair's points (+inf if none); flag[c][s] = 1 when some point's
-// lower bound is under the cut (the pair may be kept), else 0.
-__global__ void __launch_bounds__(128) k_mx_scan32(ScreenTables T, float cut, unsigned char *__restrict__ flag,
-                                                   float *__restrict__ ubmin) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= T.nt) return;
-    for (int c = blockIdx.y; c < T.nc; c += gridDim.y) {
-        float ub = __int_as_float(0x7f800000), lb = ub;
-        walk32(T, s, c, cut, [&](int, const Bound &b) {
-            ub = fminf(ub, b.ub);
-            lb = fminf(lb, b.lb);
-        });
-        const size_t o = (size_t)c * T.nt + s;
-        flag[o] = lb < cut;
-        ubmin[o] = ub;
+// A point k can be the FP64 minimum of a kept pair only if lb_k < cut and lb_k <= min_j ub_j (otherwise some point
+// is certainly lower, or none is under the cut): the pair's candidates.  The walk keeps them in kCandSlots slots:
+// the running min ub only decreases, so a point that qualifies at the end qualified when it was walked, and a slot
+// whose lb has risen above the running min ub is free again.  Per pair: flag[c][s] = 0 (no candidate: the pair
+// cannot be kept), 1 (its candidates are in klist[c][s], kCandSlots 16-bit point numbers, 0xffff = empty) or 2 (more
+// candidates than slots, or a point number that does not fit 16 bits: the candidates are found again by a second
+// walk, which needs ubmin[c][s]).  A slot is taken while its lb is under the cut (empty slots hold +inf) and not
+// above the running min ub.  ubmin and klist are written for flagged pairs only.
+constexpr int kCandSlots = 4;
+constexpr unsigned kNoPoint = 0xffffu;
+constexpr int kScanStars = 128;         // stars per block (one per thread)
+constexpr int kQueue = 64;              // per warp: points waiting for their full bounds
+
+// The bounds of point k of pair (s, c), as walk32 computes them: false when the point is skipped or rejected.
+__device__ __forceinline__ bool point_at32(const ScreenTables &T, int s, int c, int k, float cut, Bound &b) {
+    const size_t NT = T.nt, NC = T.nc;
+    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
+    const bool more = k + 1 < n;
+    const float4 *tp = T.t32 + ((size_t)k * NT + s) * 3, *cp = T.c32 + ((size_t)k * NC + c) * 3;
+    const float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
+    const float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2);
+    float m0[3], m1[3];
+    sep32(t0, t1, c0, c1, m0);
+    if (more) {
+        const float4 *tn = tp + NT * 3, *cn = cp + NC * 3;
+        sep32(tn[0], tn[1], __ldg(cn), __ldg(cn + 1), m1);
+    } else {
+        m1[0] = m0[0]; m1[1] = m0[1]; m1[2] = m0[2];
+    }
+    const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+    const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
+    return point_bound32(St, Sc, T.R2f[c], T.lm_t[(size_t)k * NT + s], __ldg(T.lm_c + (size_t)k * NC + c), m0, m1,
+                         more, cut, b);
+}
+
+// One block: kScanStars stars x one cluster; a warp walks its 32 pairs' points in step.  Clusters are the grid's fast
+// axis, so the blocks resident at one time share one block of stars, whose track data stays in L2.
+// Each lane runs the cheap test (point_skip32) on its point; the few points it cannot settle are queued per warp in
+// shared memory and given their full bounds 32 at a time, one per lane, so the long evaluation runs on full warps
+// instead of diverging on most steps; the owner lane then folds the results into its pair's state.  The state (min
+// ub and the candidate slots) does not depend on the order the points are folded in.
+__global__ void __launch_bounds__(kScanStars) k_mx_scan32(ScreenTables T, float cut, unsigned char *__restrict__ flag,
+                                                          float *__restrict__ ubmin,
+                                                          unsigned long long *__restrict__ klist) {
+    __shared__ int s_q[kScanStars / 32][kQueue];
+    __shared__ float s_lb[kScanStars / 32][32], s_ub[kScanStars / 32][32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, c = blockIdx.x;
+    const int s0 = blockIdx.y * kScanStars + w * 32;
+    if (s0 >= T.nt) return;                                       // the whole warp: uniform
+    const bool active = s0 + lane < T.nt;
+    const int s = active ? s0 + lane : T.nt - 1;                  // lanes past the end shadow a valid star
+    const float inf = __int_as_float(0x7f800000);
+    float um = inf, ls[kCandSlots];
+    unsigned kq[kCandSlots];
+#pragma unroll
+    for (int i = 0; i < kCandSlots; i++) { ls[i] = inf; kq[i] = kNoPoint; }
+    bool over = false;
+    auto fold = [&](int k, float lb, float ub) {
+        um = fminf(um, ub);
+        if (lb < cut && lb <= um) {
+            bool placed = false;
+#pragma unroll
+            for (int i = 0; i < kCandSlots; i++)
+                if (!placed && !(ls[i] < cut && ls[i] <= um)) { ls[i] = lb; kq[i] = (unsigned)k; placed = true; }
+            over |= !placed || k >= (int)kNoPoint;
+        }
+    };
+    // full bounds for queue entries [0, cnt): entry = owner lane | k << 5
+    auto drain = [&](int cnt) {
+        __syncwarp();
+        if (lane < cnt) {
+            const int e = s_q[w][lane];
+            Bound b;
+            const bool keep = point_at32(T, s0 + (e & 31), c, e >> 5, cut, b);
+            s_lb[w][lane] = keep ? b.lb : inf;
+            s_ub[w][lane] = keep ? b.ub : inf;
+        }
+        __syncwarp();
+        for (int j = 0; j < cnt; j++) {
+            const int e = s_q[w][j];
+            if ((e & 31) == lane) fold(e >> 5, s_lb[w][j], s_ub[w][j]);
+        }
+        __syncwarp();
+    };
+    const size_t NT = T.nt, NC = T.nc;
+    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
+    const float R2 = T.R2f[c];
+    const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
+    float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
+    float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2);
+    float mcur[3];
+    sep32(t0, t1, c0, c1, mcur);
+    int qn = 0;
+    for (int k = 0; k < n; k++) {
+        const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+        const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
+        const float lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
+        float mnext[3] = {mcur[0], mcur[1], mcur[2]};
+        if (k + 1 < n) {
+            const float4 *tn = tp + (size_t)(k + 1) * NT * 3, *cn = cp + (size_t)(k + 1) * NC * 3;
+            t0 = tn[0]; t1 = tn[1]; t2 = tn[2];
+            c0 = __ldg(cn); c1 = __ldg(cn + 1); c2 = __ldg(cn + 2);
+            sep32(t0, t1, c0, c1, mnext);
+        }
+        const bool need = active && !point_skip32(St, Sc, R2, lmt, lmc, mcur, mnext, cut);
+        const unsigned mask = __ballot_sync(0xffffffffu, need);
+        if (need) s_q[w][qn + __popc(mask & ((1u << lane) - 1u))] = lane | (k << 5);
+        qn += __popc(mask);
+        if (qn >= 32) {
+            drain(32);
+            const int rest = qn - 32;
+            const int v = lane < rest ? s_q[w][32 + lane] : 0;
+            __syncwarp();
+            if (lane < rest) s_q[w][lane] = v;
+            qn = rest;
+        }
+        mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
+    }
+    if (qn > 0) drain(qn);
+    if (!active) return;
+    unsigned long long kl = 0;
+    bool any = false;
+#pragma unroll
+    for (int i = 0; i < kCandSlots; i++) {
+        const bool live = ls[i] < cut && ls[i] <= um;
+        any |= live;
+        kl |= (unsigned long long)(live ? kq[i] : kNoPoint) << (16 * i);
+    }
+    const size_t o = (size_t)c * NT + s;
+    flag[o] = over ? 2 : (any ? 1 : 0);
+    if (over || any) {
+        ubmin[o] = um;
+        klist[o] = kl;
     }
 }
 
@@ -369,37 +343,73 @@ int exclusive_scan(cudaStream_t st, int n, const int *in, int *out, int *part, i
 struct PossPair {
     int s, c;
     float ubmin;
-    int pad;
+    int over;                     // 1: more candidates than slots (found again by a walk)
+    unsigned long long klist;     // the candidate slots, as k_mx_scan32 left them
 };
 
 __global__ void k_mx_count(int nt, int nc, const unsigned char *__restrict__ flag, int *__restrict__ npair) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nt) return;
     int a = 0;
-    for (int c = 0; c < nc; c++) a += flag[(size_t)c * nt + s];
+    for (int c = 0; c < nc; c++) a += flag[(size_t)c * nt + s] != 0;
     npair[s] = a;
 }
 
 __global__ void k_mx_emit(int nt, int nc, const unsigned char *__restrict__ flag, const float *__restrict__ ubmin,
-                          const int *__restrict__ opair, PossPair *__restrict__ P) {
+                          const unsigned long long *__restrict__ klist, const int *__restrict__ opair,
+                          PossPair *__restrict__ P) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nt) return;
     int p = opair[s];
     for (int c = 0; c < nc; c++) {
         const size_t o = (size_t)c * nt + s;
-        if (!flag[o]) continue;
+        const int f = flag[o];
+        if (!f) continue;
         PossPair r;
-        r.s = s; r.c = c; r.ubmin = ubmin[o]; r.pad = 0;
+        r.s = s; r.c = c; r.ubmin = ubmin[o]; r.over = f == 2; r.klist = klist[o];
         P[p++] = r;
     }
 }
 
-// ---- K3: candidate points of the possible pairs (counted, then written in point order) ------------------------
-// a point can be its pair's FP64 minimum only if lb_k <= (the pair's smallest ub) and lb_k < cut
-__global__ void k_mx_cand(ScreenTables T, float cut, int np, const PossPair *__restrict__ P, int *__restrict__ cnt,
-                          const int *__restrict__ off, int2 *__restrict__ E) {
+// per possible pair: its number of listed candidates (0 for an overflowed pair, counted by its walk) and whether it
+// overflowed
+__global__ void k_mx_list_count(int np, const PossPair *__restrict__ P, int *__restrict__ cnt, int *__restrict__ ovf) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
+    const PossPair r = P[p];
+    int n = 0;
+#pragma unroll
+    for (int i = 0; i < kCandSlots; i++) n += ((r.klist >> (16 * i)) & 0xffffu) != kNoPoint;
+    cnt[p] = r.over ? 0 : n;
+    ovf[p] = r.over;
+}
+
+__global__ void k_mx_list_emit(int np, const PossPair *__restrict__ P, const int *__restrict__ off,
+                               int2 *__restrict__ E) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const PossPair r = P[p];
+    if (r.over) return;
+    int e = off[p];
+#pragma unroll
+    for (int i = 0; i < kCandSlots; i++) {
+        const unsigned k = (unsigned)(r.klist >> (16 * i)) & 0xffffu;
+        if (k != kNoPoint) E[e++] = make_int2(p, (int)k);
+    }
+}
+
+__global__ void k_mx_ovf_emit(int np, const int *__restrict__ ovf, const int *__restrict__ off, int *__restrict__ A) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < np && ovf[p]) A[off[p]] = p;
+}
+
+// ---- K3: the overflowed pairs walked again: their candidate points, counted, then written --------------------------
+__global__ void k_mx_cand(ScreenTables T, float cut, int na, const int *__restrict__ A,
+                          const PossPair *__restrict__ P, int *__restrict__ cnt, const int *__restrict__ off,
+                          int2 *__restrict__ E) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= na) return;
+    const int p = A[i];
     const PossPair r = P[p];
     if (!E) {
         int n = 0;
@@ -449,21 +459,23 @@ struct PairBest {
     int kb, pad;
 };
 
-// FP64 argmin over a pair's candidates (in point order: strict <, the first of equal minima wins)
+// FP64 argmin over a pair's candidates: the smallest value, the first point of equal ones (as the strict < of a
+// walk in point order) -- the candidates need not be in point order
 __global__ void k_mx_best(int np, const int *__restrict__ off, const int *__restrict__ cnt,
                           const int2 *__restrict__ E, const double *__restrict__ ev, const double *__restrict__ es,
                           PairBest *__restrict__ B) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     double best = kInf, sb = 0.0;
-    int kb = 0;
+    int kb = 0x7fffffff;
     const int e0 = off[p], n = cnt[p];
     for (int q = 0; q < n; q++) {
         const double v = ev[e0 + q];
-        if (v >= 0 && v < best) { best = v; kb = E[e0 + q].y; sb = es[e0 + q]; }
+        const int k = E[e0 + q].y;
+        if (v >= 0 && (v < best || (v == best && k < kb))) { best = v; kb = k; sb = es[e0 + q]; }
     }
     PairBest o;
-    o.chi2 = best; o.sb = sb; o.kb = kb; o.pad = 0;
+    o.chi2 = best; o.sb = best < kInf ? sb : 0.0; o.kb = best < kInf ? kb : 0; o.pad = 0;
     B[p] = o;
 }
 
@@ -493,14 +505,19 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
     const size_t pairs = (size_t)nt * nc;
     int rc, launches = 0;
     const int nbs = nt / kScanBlock + 2;
-    if ((rc = grow(m.flag, pairs, err)) || (rc = grow(m.ub, pairs * 4, err)) ||
+    if ((rc = grow(m.flag, pairs, err)) || (rc = grow(m.ub, pairs * 4, err)) || (rc = grow(m.kmin, pairs * 8, err)) ||
         (rc = grow(m.cnt, (size_t)nt * 4, err)) || (rc = grow(m.off, (size_t)nt * 4, err)) ||
         (rc = grow(m.total, 64, err)) || (rc = grow(m.aux, (size_t)nbs * 4 + 64, err)))
         return rc;
     int *cnt = Pb<int>(m.cnt), *off = Pb<int>(m.off), *tot = Pb<int>(m.total), *part = Pb<int>(m.aux);
-    dim3 g((nt + 127) / 128, std::min(nc, 65535));
+    if ((size_t)(nt + kScanStars - 1) / kScanStars > 65535) {
+        err = "mixed precision: too many stars in one call";
+        return PGX_E_LIMIT;
+    }
+    dim3 g(nc, (nt + kScanStars - 1) / kScanStars);
     const float cutf = (float)cut;
-    k_mx_scan32<<<g, 128, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub));
+    k_mx_scan32<<<g, kScanStars, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
+                                   Pb<unsigned long long>(m.kmin));
     if ((rc = check(cudaGetLastError(), err, "k_mx_scan32"))) return rc;
     if ((rc = check(cudaEventRecord(ev_scan, st), err, "event"))) return rc;
     k_mx_count<<<(nt + 127) / 128, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), cnt);
@@ -510,39 +527,55 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
     if ((rc = check(cudaMemcpyAsync(&np, tot, 4, cudaMemcpyDeviceToHost, st), err, "counts")) ||
         (rc = check(cudaStreamSynchronize(st), err, "counts sync")))
         return rc;
+    // per possible pair p: PossPair P[p], PairBest B[p]; int arrays A (overflowed pairs), pc / po (candidate
+    // counts and offsets), flags / offsets (overflowed, then kept), and the scan's block partials
     const int nbp = np / kScanBlock + 2;
     if ((rc = grow(m.cand, (size_t)np * sizeof(PossPair) + 64, err)) ||
-        (rc = grow(m.cand_off, ((size_t)np * 2 + nbp) * 4 + 64, err)) ||
+        (rc = grow(m.cand_off, ((size_t)np * 3 + nbp) * 4 + 64, err)) ||
         (rc = grow(m.entq, (size_t)np * (sizeof(PairBest) + 8) + 64, err)))
         return rc;
     PossPair *P = Pb<PossPair>(m.cand);
-    int *pc = Pb<int>(m.cand_off), *po = pc + np, *ppart = po + np;
+    int *A = Pb<int>(m.cand_off), *pc = A + np, *po = pc + np, *ppart = po + np;
     PairBest *B = Pb<PairBest>(m.entq);
     int *kf = reinterpret_cast<int *>(B + np), *ko = kf + np;
-    k_mx_emit<<<(nt + 127) / 128, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), Pb<float>(m.ub), off, P);
+    k_mx_emit<<<(nt + 127) / 128, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
+                                                Pb<unsigned long long>(m.kmin), off, P);
     launches += 1;
-    int ne = 0;
+    int na = 0, ne = 0, nk = 0;
     if (np > 0) {
-        k_mx_cand<<<(np + 127) / 128, 128, 0, st>>>(T, cutf, np, P, pc, nullptr, nullptr);
+        // candidate counts: from the slots, or by walking the overflowed pairs again
+        k_mx_list_count<<<(np + 255) / 256, 256, 0, st>>>(np, P, pc, kf);
+        if ((rc = exclusive_scan(st, np, kf, ko, ppart, tot + 2, err))) return rc;
+        k_mx_ovf_emit<<<(np + 255) / 256, 256, 0, st>>>(np, kf, ko, A);
+        if ((rc = check(cudaMemcpyAsync(&na, tot + 2, 4, cudaMemcpyDeviceToHost, st), err, "overflowed")) ||
+            (rc = check(cudaStreamSynchronize(st), err, "overflowed sync")))
+            return rc;
+        launches += 2 + 3;
+        if (na > 0) {
+            k_mx_cand<<<(na + 127) / 128, 128, 0, st>>>(T, cutf, na, A, P, pc, nullptr, nullptr);
+            launches += 1;
+        }
         if ((rc = exclusive_scan(st, np, pc, po, ppart, tot + 1, err))) return rc;
         if ((rc = check(cudaMemcpyAsync(&ne, tot + 1, 4, cudaMemcpyDeviceToHost, st), err, "entries")) ||
             (rc = check(cudaStreamSynchronize(st), err, "entries sync")))
             return rc;
-        launches += 4;
-    }
-    if ((long long)ne > kMaxEntries) {
-        err = "mixed precision: too many candidate points for the work buffers";
-        return PGX_E_LIMIT;
-    }
-    if ((rc = grow(m.ent, (size_t)ne * (sizeof(int2) + 16) + 64, err))) return rc;
-    int2 *E = Pb<int2>(m.ent);
-    double *ev = reinterpret_cast<double *>(E + ne), *es = ev + ne;
-    int nk = 0;
-    if (np > 0) {
+        launches += 3;
+        if ((long long)ne > kMaxEntries) {
+            err = "mixed precision: too many candidate points for the work buffers";
+            return PGX_E_LIMIT;
+        }
+        if ((rc = grow(m.ent, (size_t)ne * (sizeof(int2) + 16) + 64, err))) return rc;
+        int2 *E = Pb<int2>(m.ent);
+        double *ev = reinterpret_cast<double *>(E + ne), *es = ev + ne;
+        k_mx_list_emit<<<(np + 255) / 256, 256, 0, st>>>(np, P, po, E);
+        launches += 1;
+        if (na > 0) {
+            k_mx_cand<<<(na + 127) / 128, 128, 0, st>>>(T, cutf, na, A, P, pc, po, E);
+            launches += 1;
+        }
         if (ne > 0) {
-            k_mx_cand<<<(np + 127) / 128, 128, 0, st>>>(T, cutf, np, P, pc, po, E);
             k_mx_eval64<<<(ne + 127) / 128, 128, 0, st>>>(T, cut, ne, P, E, ev, es);
-            launches += 2;
+            launches += 1;
         }
         k_mx_best<<<(np + 127) / 128, 128, 0, st>>>(np, po, pc, E, ev, es, B);
         k_mx_kept_flags<<<(np + 255) / 256, 256, 0, st>>>(np, B, cut, kf);
@@ -560,6 +593,7 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
     *total = nk;
     if (stats) {
         stats->candidates = np;
+        stats->ambiguous = na;
         stats->rechecked_points = ne;
         stats->kernels += launches;
     }
@@ -580,13 +614,12 @@ __device__ __forceinline__ void gauss32(uint64_t a, uint64_t b, float &z, float 
     if (k1 == 0) {
         r2 = 88.7228391f;                               // -2 ln 2^-64, the reference's floor for u1 = 0
     } else if (k1 >= (1ull << 52)) {
-        const float v = (float)(int64_t)((1ull << 53) - k1) * 1.1102230246251565e-16f;
-        r2 = -2.f * log1pf(-v);
+        r2 = -2.f * log1pf(-u64_to_f32_scaled((1ull << 53) - k1, 53));
     } else {
-        r2 = -2.f * logf((float)(int64_t)k1 * 1.1102230246251565e-16f);
+        r2 = -2.f * logf(u64_to_f32_scaled(k1, 53));
     }
     rad = sqrtf(r2);
-    z = rad * cospif(2.f * ((float)(int64_t)k2 * 1.1102230246251565e-16f));
+    z = rad * cospif(u64_to_f32_scaled(k2, 52));      // 2 u2
 }
 
 struct Fin32 {
@@ -597,25 +630,33 @@ __global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__re
                                                      ScreenRowDev *__restrict__ rows, int *__restrict__ nrecheck) {
     const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (h >= n) return;
-    const FinishIn f = fin[h];
+    // the FP32 copies of the pair's constants: lane j converts field j, the warp shares them (one conversion per
+    // warp instead of one per field)
+    const double *fd = reinterpret_cast<const double *>(fin + h);
+    double v = fd[lane < 11 ? lane : (lane < 13 ? lane - 2 : 0)];
+    if (lane == 11 || lane == 12) v = v * v;                 // r50^2, rtot^2
+    const float fv = (float)v;
     Fin32 g;
-    g.mx = (float)f.mx; g.my = (float)f.my; g.mz = (float)f.mz;
-    g.l00 = (float)f.l00; g.l10 = (float)f.l10; g.l20 = (float)f.l20;
-    g.l11 = (float)f.l11; g.l21 = (float)f.l21; g.l22 = (float)f.l22;
-    g.r50s = (float)(f.r50 * f.r50); g.rts = (float)(f.rt * f.rt);
+    g.mx = __shfl_sync(0xffffffffu, fv, 0); g.my = __shfl_sync(0xffffffffu, fv, 1);
+    g.mz = __shfl_sync(0xffffffffu, fv, 2);
+    g.l00 = __shfl_sync(0xffffffffu, fv, 3); g.l10 = __shfl_sync(0xffffffffu, fv, 4);
+    g.l20 = __shfl_sync(0xffffffffu, fv, 5); g.l11 = __shfl_sync(0xffffffffu, fv, 6);
+    g.l21 = __shfl_sync(0xffffffffu, fv, 7); g.l22 = __shfl_sync(0xffffffffu, fv, 8);
+    g.r50s = __shfl_sync(0xffffffffu, fv, 11); g.rts = __shfl_sync(0xffffffffu, fv, 12);
     g.mabs = fabsf(g.mx) + fabsf(g.my) + fabsf(g.mz);
     g.lsum = fabsf(g.l00) + fabsf(g.l10) + fabsf(g.l20) + fabsf(g.l11) + fabsf(g.l21) + fabsf(g.l22);
     g.e50 = 8.f * kEps32 * g.r50s;                 // rounding of r50^2 and of the comparison
     g.etot = 8.f * kEps32 * g.rts;
     int in50 = 0, intot = 0, rechecks = 0;
+    // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden
+    uint64_t w = fin[h].seed + (uint64_t)(6 * lane) * kGolden;
 #pragma unroll 1
-    for (int q = 0; q < 16; q++) {
+    for (int q = 0; q < 16; q++, w += 192 * kGolden) {
         const int i = lane + 32 * q;
-        const uint64_t nn = 6ull * (uint64_t)i;
         float z0, z1, z2, a0, a1, a2;
-        gauss32(splitmix_at(f.seed, nn + 1), splitmix_at(f.seed, nn + 2), z0, a0);
-        gauss32(splitmix_at(f.seed, nn + 3), splitmix_at(f.seed, nn + 4), z1, a1);
-        gauss32(splitmix_at(f.seed, nn + 5), splitmix_at(f.seed, nn + 6), z2, a2);
+        gauss32(splitmix_mix(w + kGolden), splitmix_mix(w + 2 * kGolden), z0, a0);
+        gauss32(splitmix_mix(w + 3 * kGolden), splitmix_mix(w + 4 * kGolden), z1, a1);
+        gauss32(splitmix_mix(w + 5 * kGolden), splitmix_mix(w + 6 * kGolden), z2, a2);
         const float x = fmaf(g.l00, z0, g.mx);
         const float y = fmaf(g.l11, z1, fmaf(g.l10, z0, g.my));
         const float z = fmaf(g.l22, z2, fmaf(g.l21, z1, fmaf(g.l20, z0, g.mz)));
@@ -630,7 +671,7 @@ __global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__re
             in50 += d50 < 0.f;
             intot += dt < 0.f;
         } else {
-            const int v = draw_inside64(f, i);             // the FP64 path's own draw
+            const int v = draw_inside64(fin[h], i);        // the FP64 path's own draw
             in50 += v & 1;
             intot += v >> 1;
             rechecks++;
@@ -666,7 +707,8 @@ int mixed_finish(cudaStream_t st, int n, const FinishIn *fin, ScreenRowDev *rows
 namespace pgx {
 // Self-check of point_bound32: n independent points given in FP64 (star and cluster positions at the point and at
 // the next one, the two covariances, R^2), evaluated as the screen evaluates them -- the FP32 bounds from split
-// positions and FP32 covariances, and the FP64 point chi2.  rej[i] = 1 when FP32 rejects the point by the bound.
+// positions and FP32 covariances, and the FP64 point chi2.  rej[i] = 1 when FP32 rejects the point by the trace
+// bound, 2 when the cheap test (point_skip32) skips it (its bounds are returned all the same), else 0.
 __global__ void k_mx_check_bounds(int n, const double *__restrict__ pos, const double *__restrict__ S,
                                   const double *__restrict__ R2, double cut, double *__restrict__ v64,
                                   float *__restrict__ lb, float *__restrict__ ub, int *__restrict__ rej) {
@@ -695,7 +737,8 @@ __global__ void k_mx_check_bounds(int n, const double *__restrict__ pos, const d
     v64[i] = point_chi2_64(M, R2[i], d0, d1, true, cut, sv);
     lb[i] = dec ? b.lb : 0.f;
     ub[i] = dec ? b.ub : 0.f;
-    rej[i] = dec ? 0 : 1;
+    rej[i] = !dec ? 1 : (point_skip32(St, Sc, (float)R2[i], __double2float_rd(lt - 1e-12 * fabs(lt)),
+                                      __double2float_rd(lc - 1e-12 * fabs(lc)), m0, m1, (float)cut) ? 2 : 0);
 }
 
 int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *S, const double *R2, double cut,

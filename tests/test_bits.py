@@ -1,0 +1,63 @@
+"""The integer-only FP32 conversion the FP32 draws use (phygas_gb300/csrc/cuda/pgx_bits.cuh) gives the bits of the
+compiler's own int64 -> float conversion, checked on the CPU: the header also compiles as host C++."""
+import os
+import subprocess
+import tempfile
+
+from tests import oracle_tools as ot
+
+PROBE = r"""
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+#include <initializer_list>
+#include "pgx_bits.cuh"
+static uint64_t sm = 12345;
+static uint64_t next() {                       // splitmix64
+    uint64_t z = (sm += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+static long bad = 0, tested = 0;
+static void check(uint64_t k, int sh) {
+    const float want = (float)(int64_t)k * (sh == 53 ? 1.1102230246251565e-16f : 2.220446049250313e-16f);
+    const float got = pgx::u64_to_f32_scaled(k, sh);
+    uint32_t a, b;
+    std::memcpy(&a, &want, 4);
+    std::memcpy(&b, &got, 4);
+    tested++;
+    if (a != b && bad++ < 5) std::printf("k=%llu sh=%d want %a got %a\n", (unsigned long long)k, sh, want, got);
+}
+int main() {
+    for (int sh : {52, 53}) {
+        check(0, sh);
+        for (int e = 0; e < 54; e++) {                 // around every power of two up to 2^53
+            const uint64_t p = 1ull << e;
+            for (int d = -40; d <= 40; d++)
+                if ((int64_t)p + d >= 0 && p + d <= (1ull << 53)) check(p + d, sh);
+        }
+        for (int s = 1; s < 30; s++)                   // exact ties and their neighbours, even and odd significands
+            for (uint64_t q : {0x800000ull, 0x800001ull, 0xABCDEFull, 0xFFFFFEull, 0xFFFFFFull})
+                for (int d = -1; d <= 1; d++) check(((q << s) | (1ull << (s - 1))) + d, sh);
+        for (long i = 0; i < 4000000; i++) {
+            const uint64_t r = next();
+            check(r >> 11, sh);                        // uniform 53-bit, as the draws use
+            check((r >> 11) >> (r & 63) % 53, sh);      // every magnitude
+        }
+    }
+    std::printf("tested %ld bad %ld\n", tested, bad);
+    return bad != 0;
+}
+"""
+
+
+def test_u64_to_f32_scaled_matches_the_cast():
+    inc = os.path.join(ot.REPO, "phygas_gb300", "csrc", "cuda")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "probe.cpp"), os.path.join(d, "probe")
+        open(src, "w").write(PROBE)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", inc, src, "-o", exe], check=True)
+        r = subprocess.run([exe], stdout=subprocess.PIPE, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "bad 0" in r.stdout

@@ -47,12 +47,16 @@ def random_points(n, seed):
 @pytest.mark.parametrize("cut", [25.0, 1e6])
 def test_fp32_bounds_hold(ctx, cut):
     """2 million random points, 15 % with rank-1 (needle) star covariances: where the FP32 filter rejects a point
-    by the trace bound, the FP64 path rejects it too or finds it above the cut; elsewhere lb <= chi2_64 <= ub (the
-    FP64 path's computed value, adjugate rounding included)."""
+    by the trace bound, the FP64 path rejects it too or finds it above the cut; where its cheap pre-test skips a
+    point, the FP64 value is at or above the cut; elsewhere lb <= chi2_64 <= ub (the FP64 path's computed value,
+    adjugate rounding included)."""
     pos, S, R2 = random_points(2_000_000, 11 if cut == 25.0 else 12)
     v, lb, ub, rej = ctx.check_bounds(pos, S, R2, cut)
     r = rej == 1
     assert np.all(np.isinf(v[r]) | (v[r] > cut)), np.sort(v[r])[:5]
+    sk = rej == 2
+    assert np.all(np.isinf(v[sk]) | (v[sk] >= cut)), np.sort(v[sk])[:5]
+    print("skipped by the cheap test %.3f" % sk.mean())
     ok = ~r & (v >= 0) & np.isfinite(v)
     lbv, ubv, vv = lb[ok].astype(np.float64), ub[ok].astype(np.float64), v[ok]
     bad = (lbv > vv) | (ubv < vv)

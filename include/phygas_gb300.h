@@ -129,6 +129,12 @@ int pgx_peaks(PgxContext *ctx, double *fp64_flops, double *fp32_flops);
 int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S, const double *R2, double chi2_max,
                      double *v64, float *lb, float *ub, int *rej);
 
+/* Self-check of the mixed-precision finish's FP32 draws (no counterpart in the reference): for n pairs given by
+ * fin11[11n] = (mx my mz, the covariance's Cholesky factor l00 l10 l20 l11 l21 l22, r50, rtot; kpc) and their draw
+ * seeds, ratio[i] = the largest |x_j - x_j,64| / bound over the pair's 512 draws and three components, where x is
+ * the FP32 draw, x_64 the FP64 path's and bound the FP32 draw's own error bound: <= 1 when the bound holds. */
+int pgx_check_draws(PgxContext *ctx, int n, const double *fin11, const uint64_t *seed, double *ratio);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,7 @@ SIGNATURES = [
     ("pgx_peaks", C.c_int, [C.c_void_p, _D, _D]),
     ("pgx_check_bounds", C.c_int, [C.c_void_p, C.c_int, _D, _D, _D, C.c_double, _D, _P(C.c_float),
                                    _P(C.c_float), _I]),
+    ("pgx_check_draws", C.c_int, [C.c_void_p, C.c_int, _D, _P(C.c_uint64), _D]),
     ("ph_init", None, []),
     ("ph_seed", C.c_uint64, [C.c_char_p, C.c_char_p]),
     ("ph_read_clusters", C.c_int, [C.c_char_p, _P(_P(PhCluster))]),
@@ -210,6 +211,15 @@ class Context:
                                            _ptr(lb, C.c_float), _ptr(ub, C.c_float), _ptr(rej, C.c_int)),
                     "pgx_check_bounds")
         return v, lb, ub, rej
+
+    def check_draws(self, fin11, seeds):
+        """Per pair, the FP32 draws' largest error relative to their own bound (see pgx_check_draws)."""
+        fin11 = np.ascontiguousarray(fin11, np.float64)
+        seeds = np.ascontiguousarray(seeds, np.uint64)
+        ratio = np.zeros(len(seeds))
+        self._check(lib().pgx_check_draws(self.h, len(seeds), _ptr(fin11), _ptr(seeds, C.c_uint64), _ptr(ratio)),
+                    "pgx_check_draws")
+        return ratio
 
     def lin(self, ps0, sig, npts):
         ps0 = np.ascontiguousarray(ps0, np.float64)

@@ -275,6 +275,27 @@ int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S,
     return 0;
 }
 
+int pgx_check_draws(PgxContext *ctx, int n, const double *fin11, const uint64_t *seed, double *ratio) {
+    if (!ctx) return PGX_E_ARG;
+    if (n <= 0 || !fin11 || !seed || !ratio) return fail(ctx, PGX_E_ARG, "pgx_check_draws");
+    CK(cudaSetDevice(ctx->device));
+    std::vector<pgx::FinishIn> h(n);
+    for (int i = 0; i < n; i++) {
+        const double *v = fin11 + (size_t)11 * i;
+        pgx::FinishIn &f = h[i];
+        f.mx = v[0]; f.my = v[1]; f.mz = v[2]; f.l00 = v[3]; f.l10 = v[4]; f.l20 = v[5];
+        f.l11 = v[6]; f.l21 = v[7]; f.l22 = v[8]; f.r50 = v[9]; f.rt = v[10]; f.seed = seed[i];
+    }
+    RET(ensure(ctx, ctx->x_opos, (size_t)n * (sizeof(pgx::FinishIn) + 8) + 64));
+    pgx::FinishIn *df = P<pgx::FinishIn>(ctx->x_opos);
+    double *dr = reinterpret_cast<double *>(df + n);
+    CK(cudaMemcpyAsync(df, h.data(), (size_t)n * sizeof(pgx::FinishIn), cudaMemcpyHostToDevice, ctx->st));
+    MRET(pgx::mixed_check_draws(ctx->st, n, df, dr, ctx->mixed.err));
+    CK(cudaMemcpyAsync(ratio, dr, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
 int pgx_lin(PgxContext *ctx, int n, const double *ps0, const double *sig, const int *npts, double *pos, double *vel,
             double *S) {
     if (!ctx) return PGX_E_ARG;

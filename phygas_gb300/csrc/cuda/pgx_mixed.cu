@@ -603,36 +603,41 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
 const KeptPair *mixed_kept(MixedBufs &m) { return (const KeptPair *)m.kept.p; }
 
 // ---- the 512 draws in FP32 --------------------------------------------------------------------------------------
-// Box-Muller radius^2 = -2 ln u1 and cos(2 pi u2) in FP32 from the 53-bit integers: ln u1 by log1pf(-v) with
-// v = 1 - u1 exact in integers when u1 >= 1/2 (no cancellation near u1 = 1), by logf otherwise (1 ulp each, plus
-// the rounding of u1 or v to FP32): relative error of the radius <= 1.6e-7; the cosine by cospif(2 u2) with absolute
-// error <= 3.1e-7 (pi x the rounding of 2 u2 to FP32, plus 1 ulp).  So |z - z_64| <= 5.3e-7 * radius, and with the
-// roundings of L, m and the three fused multiply-adds of x = m + L z, |x_i - x_i,64| <= 4 eps |m| + 16 eps |L| radius.
-__device__ __forceinline__ void gauss32(uint64_t a, uint64_t b, float &z, float &rad) {
-    const uint64_t k1 = a >> 11, k2 = b >> 11;
-    float r2;
-    if (k1 == 0) {
-        r2 = 88.7228391f;                               // -2 ln 2^-64, the reference's floor for u1 = 0
-    } else if (k1 >= (1ull << 52)) {
-        r2 = -2.f * log1pf(-u64_to_f32_scaled((1ull << 53) - k1, 53));
-    } else {
-        r2 = -2.f * logf(u64_to_f32_scaled(k1, 53));
-    }
-    rad = sqrtf(r2);
-    z = rad * cospif(u64_to_f32_scaled(k2, 52));      // 2 u2
+// Box-Muller with the GPU's fast transcendental units, each with its documented worst-case error, and a bound per
+// draw on the distance to the FP64 path's draw (gauss64, draw_xyz64):
+//  * u = k 2^-53 from the 53-bit integer k in FP32 within 2^-23 relative (two 32-bit conversions and a fused
+//    multiply-add), so |ln U - ln u| <= 1.2e-7;
+//  * __logf: absolute error <= 2^-21.41 on [0.5, 2], else 3 ulp, so r^2 = -2 ln u1 is within
+//    D = 9.6e-7 + 3.6e-7 r^2;  radius = r^2 rsqrtf(r^2) (rsqrtf: 2 ulp) within 3e-7 relative of sqrt(r^2), and
+//    |sqrt(r^2) - sqrt(r^2_64)| <= min(D / sqrt(r^2), sqrt(D)) <= min(D rsqrtf 1.000001, 1e-3 + 6e-4 radius);
+//  * cos(2 pi u2) = -cos(theta), theta = (U2 - 1/2) 6.283185f in [-pi, pi] (6.283185f < 2 pi): the angle is within
+//    1.19e-6 of 2 pi (u2 - 1/2) (conversion, subtraction, the constant, the product) and __cosf adds <= 2^-21.19
+//    absolute, so the cosine is within 1.61e-6;
+//  * z = -radius cos: |z - z_64| <= 1.000003 e_radius + 1.68e-6 radius.
+// x = m + L z by three fused multiply-adds from FP32 m and L: every component within
+// 4 eps (|m| + |L| max|z|) + |L| max|z - z_64| of the FP64 path's.
+__device__ __forceinline__ float u53_unit(uint64_t k) {
+    return fmaf((float)(uint32_t)(k >> 21), 0x1p-32f, (float)(uint32_t)(k & 0x1fffffu) * 0x1p-53f);
+}
+
+__device__ __forceinline__ void gauss32(uint64_t a, uint64_t b, float &z, float &rad, float &err) {
+    const float u1 = fmaxf(u53_unit(a >> 11), 0x1p-64f);       // the reference's floor for u1 = 0
+    const float r2 = fmaxf(-2.f * __logf(u1), 0.f);
+    const float rs = rsqrtf(fmaxf(r2, 1e-30f));
+    rad = r2 * rs;
+    z = -rad * __cosf((u53_unit(b >> 11) - 0.5f) * 6.283185f);
+    const float D = fmaf(3.6e-7f, r2, 9.6e-7f);
+    const float erad = fmaf(3e-7f, rad, fminf(D * rs * 1.000001f, fmaf(6e-4f, rad, 1e-3f)));
+    err = fmaf(erad, 1.000003f, 1.68e-6f * rad);
 }
 
 struct Fin32 {
     float mx, my, mz, l00, l10, l20, l11, l21, l22, r50s, rts, mabs, lsum, e50, etot;
 };
 
-__global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__restrict__ fin,
-                                                     ScreenRowDev *__restrict__ rows, int *__restrict__ nrecheck) {
-    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (h >= n) return;
-    // the FP32 copies of the pair's constants: lane j converts field j, the warp shares them (one conversion per
-    // warp instead of one per field)
-    const double *fd = reinterpret_cast<const double *>(fin + h);
+// the pair's FP32 constants: lane j converts field j of fin, the warp shares them (one conversion per warp)
+__device__ __forceinline__ Fin32 fin32(const FinishIn &fin, int lane) {
+    const double *fd = reinterpret_cast<const double *>(&fin);
     double v = fd[lane < 11 ? lane : (lane < 13 ? lane - 2 : 0)];
     if (lane == 11 || lane == 12) v = v * v;                 // r50^2, rtot^2
     const float fv = (float)v;
@@ -647,23 +652,36 @@ __global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__re
     g.lsum = fabsf(g.l00) + fabsf(g.l10) + fabsf(g.l20) + fabsf(g.l11) + fabsf(g.l21) + fabsf(g.l22);
     g.e50 = 8.f * kEps32 * g.r50s;                 // rounding of r50^2 and of the comparison
     g.etot = 8.f * kEps32 * g.rts;
+    return g;
+}
+
+// FP32 draw whose splitmix64 state before its first call is w: position and ex >= |x_j - x_j,64| for each j
+__device__ __forceinline__ void draw32(const Fin32 &g, uint64_t w, float &x, float &y, float &z, float &ex) {
+    float z0, z1, z2, a0, a1, a2, e0, e1, e2;
+    gauss32(splitmix_mix(w + kGolden), splitmix_mix(w + 2 * kGolden), z0, a0, e0);
+    gauss32(splitmix_mix(w + 3 * kGolden), splitmix_mix(w + 4 * kGolden), z1, a1, e1);
+    gauss32(splitmix_mix(w + 5 * kGolden), splitmix_mix(w + 6 * kGolden), z2, a2, e2);
+    x = fmaf(g.l00, z0, g.mx);
+    y = fmaf(g.l11, z1, fmaf(g.l10, z0, g.my));
+    z = fmaf(g.l22, z2, fmaf(g.l21, z1, fmaf(g.l20, z0, g.mz)));
+    const float emax = fmaxf(e0, fmaxf(e1, e2));
+    const float amax = fmaf(fmaxf(a0, fmaxf(a1, a2)), 1.000001f, emax);
+    ex = fmaf(4.f * kEps32, g.mabs, g.lsum * fmaf(4.f * kEps32, amax, emax * (1.f + 2.f * kEps32)));
+}
+
+__global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__restrict__ fin,
+                                                     ScreenRowDev *__restrict__ rows, int *__restrict__ nrecheck) {
+    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (h >= n) return;
+    const Fin32 g = fin32(fin[h], lane);
     int in50 = 0, intot = 0, rechecks = 0;
     // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden
     uint64_t w = fin[h].seed + (uint64_t)(6 * lane) * kGolden;
 #pragma unroll 1
     for (int q = 0; q < 16; q++, w += 192 * kGolden) {
-        const int i = lane + 32 * q;
-        float z0, z1, z2, a0, a1, a2;
-        gauss32(splitmix_mix(w + kGolden), splitmix_mix(w + 2 * kGolden), z0, a0);
-        gauss32(splitmix_mix(w + 3 * kGolden), splitmix_mix(w + 4 * kGolden), z1, a1);
-        gauss32(splitmix_mix(w + 5 * kGolden), splitmix_mix(w + 6 * kGolden), z2, a2);
-        const float x = fmaf(g.l00, z0, g.mx);
-        const float y = fmaf(g.l11, z1, fmaf(g.l10, z0, g.my));
-        const float z = fmaf(g.l22, z2, fmaf(g.l21, z1, fmaf(g.l20, z0, g.mz)));
+        float x, y, z, ex;
+        draw32(g, w, x, y, z, ex);
         const float r2 = fmaf(x, x, fmaf(y, y, z * z));
-        // |x_i - x_i,64| <= ex for every component: 4 eps (|m| + |L||z|) plus |L| times the Gaussians' error
-        const float amax = fmaxf(a0, fmaxf(a1, a2));
-        const float ex = 4.f * kEps32 * g.mabs + (16.f * kEps32) * g.lsum * amax;
         const float x1 = fabsf(x) + fabsf(y) + fabsf(z);
         const float er = 3.f * kEps32 * r2 + 2.f * x1 * ex + 3.f * ex * ex;
         const float d50 = r2 - g.r50s, dt = r2 - g.rts;
@@ -671,7 +689,7 @@ __global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__re
             in50 += d50 < 0.f;
             intot += dt < 0.f;
         } else {
-            const int v = draw_inside64(fin[h], i);        // the FP64 path's own draw
+            const int v = draw_inside64(fin[h], lane + 32 * q);      // the FP64 path's own draw
             in50 += v & 1;
             intot += v >> 1;
             rechecks++;
@@ -685,6 +703,33 @@ __global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__re
         rows[h].p_rtot = (double)intot / 512.0;
         if (rechecks) atomicAdd(nrecheck, rechecks);
     }
+}
+
+// Self-check of the FP32 draws: per pair (one warp), the largest |x_j - x_j,64| / ex over its 512 draws and three
+// components -- at most 1 when the per-draw bound holds.
+__global__ void __launch_bounds__(256) k_mx_check_draws(int n, const FinishIn *__restrict__ fin,
+                                                        double *__restrict__ ratio) {
+    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (h >= n) return;
+    const FinishIn f = fin[h];
+    const Fin32 g = fin32(f, lane);
+    double worst = 0.0;
+    uint64_t w = f.seed + (uint64_t)(6 * lane) * kGolden;
+    for (int q = 0; q < 16; q++, w += 192 * kGolden) {
+        float x, y, z, ex;
+        draw32(g, w, x, y, z, ex);
+        double x64, y64, z64;
+        draw_xyz64(f, lane + 32 * q, x64, y64, z64);
+        const double d = fmax(fabs((double)x - x64), fmax(fabs((double)y - y64), fabs((double)z - z64)));
+        worst = fmax(worst, d / (double)ex);
+    }
+    for (int o = 16; o > 0; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+    if (lane == 0) ratio[h] = worst;
+}
+
+int mixed_check_draws(cudaStream_t st, int n, const FinishIn *fin, double *ratio, std::string &err) {
+    k_mx_check_draws<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(n, fin, ratio);
+    return check(cudaGetLastError(), err, "k_mx_check_draws");
 }
 
 int mixed_finish(cudaStream_t st, int n, const FinishIn *fin, ScreenRowDev *rows, MixedBufs &m, PgxStats *stats) {

@@ -32,6 +32,8 @@ const KeptPair *mixed_kept(MixedBufs &m);
 int mixed_finish(cudaStream_t st, int n, const FinishIn *fin, ScreenRowDev *rows, MixedBufs &m, PgxStats *stats);
 
 // self-check of the FP32 point bounds (pgx_check_bounds)
+// self-check of the FP32 draws' error bound (pgx_check_draws)
+int mixed_check_draws(cudaStream_t st, int n, const FinishIn *fin, double *ratio, std::string &err);
 int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *S, const double *R2, double cut,
                        double *v64, float *lb, float *ub, int *rej, std::string &err);
 

@@ -112,15 +112,21 @@ __device__ __forceinline__ double gauss64(uint64_t a, uint64_t b) {
     return sqrt(-2.0 * log(u1)) * cos(2.0 * 3.14159265358979323846 * u2);
 }
 
-// draw i of a kept pair (its Gaussians are calls 6i+1 .. 6i+6 of the pair's stream): bit 0 = inside r50,
-// bit 1 = inside rtot
-__device__ __forceinline__ int draw_inside64(const FinishIn &f, int i) {
+// position of draw i of a kept pair (its Gaussians are calls 6i+1 .. 6i+6 of the pair's stream)
+__device__ __forceinline__ void draw_xyz64(const FinishIn &f, int i, double &x, double &y, double &z) {
     const uint64_t n = 6ull * (uint64_t)i;
     const double z0 = gauss64(splitmix_at(f.seed, n + 1), splitmix_at(f.seed, n + 2));
     const double z1 = gauss64(splitmix_at(f.seed, n + 3), splitmix_at(f.seed, n + 4));
     const double z2 = gauss64(splitmix_at(f.seed, n + 5), splitmix_at(f.seed, n + 6));
-    const double x = f.mx + f.l00 * z0, y = f.my + f.l10 * z0 + f.l11 * z1,
-                 z = f.mz + f.l20 * z0 + f.l21 * z1 + f.l22 * z2;
+    x = f.mx + f.l00 * z0;
+    y = f.my + f.l10 * z0 + f.l11 * z1;
+    z = f.mz + f.l20 * z0 + f.l21 * z1 + f.l22 * z2;
+}
+
+// draw i of a kept pair: bit 0 = inside r50, bit 1 = inside rtot
+__device__ __forceinline__ int draw_inside64(const FinishIn &f, int i) {
+    double x, y, z;
+    draw_xyz64(f, i, x, y, z);
     const double r = sqrt(x * x + y * y + z * z);
     return (r < f.r50 ? 1 : 0) | (r < f.rt ? 2 : 0);
 }

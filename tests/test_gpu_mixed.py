@@ -44,6 +44,26 @@ def random_points(n, seed):
     return pos, S, R2
 
 
+def test_fp32_draw_error_within_bound(ctx):
+    """The FP32 draws of the mixed finish (fast log / cosine / reciprocal square root units with their documented
+    worst-case errors) stay within their per-draw bound of the FP64 path's draws: 100,000 random pairs x 512 draws
+    x 3 components, separations from 0.1 pc to 3 kpc, covariances from isotropic to needles, sigma 0.1 pc to 1 kpc."""
+    rng = np.random.default_rng(5)
+    n = 100_000
+    m = rng.normal(size=(n, 3)) * (10.0 ** rng.uniform(-4, 0.5, n))[:, None]
+    S = _psd(rng, n, -8, 0, 0.3)
+    A = S[:, [0, 1, 2, 1, 3, 4, 2, 4, 5]].reshape(n, 3, 3)
+    A += np.eye(3) * (1e-9 * (S[:, 0] + S[:, 3] + S[:, 5]))[:, None, None]
+    C = np.linalg.cholesky(A)
+    L = np.column_stack([C[:, 0, 0], C[:, 1, 0], C[:, 2, 0], C[:, 1, 1], C[:, 2, 1], C[:, 2, 2]])
+    r50 = 10.0 ** rng.uniform(-3.5, -2, n)
+    fin = np.column_stack([m, L, r50, r50 * 10.0 ** rng.uniform(0.3, 1, n)])
+    seeds = rng.integers(0, 2**63, n, dtype=np.uint64) * np.uint64(2) + rng.integers(0, 2, n, dtype=np.uint64)
+    ratio = ctx.check_draws(fin, seeds)
+    print("draw error / bound: median %.3g, max %.3g" % (np.median(ratio), ratio.max()))
+    assert np.all(np.isfinite(ratio)) and ratio.max() <= 1.0, np.sort(ratio)[-5:]
+
+
 @pytest.mark.parametrize("cut", [25.0, 1e6])
 def test_fp32_bounds_hold(ctx, cut):
     """2 million random points, 15 % with rank-1 (needle) star covariances: where the FP32 filter rejects a point

@@ -36,10 +36,11 @@ N_STARS, N_CLUSTERS, SEED = 20000, 4087, 1001
 CHI2_MAX, N_SAMP, R_KERNEL = 25.0, 64, 2.0
 # FP64 flops of one body step (one kick-drift-kick step of one orbit, its force evaluation included), from the
 # executed FP64 instructions of k_stm_orbits per body step: 40.4 DFMA + 7.5 DADD + 19.9 DMUL (ncu sass op counters,
-# FMA = 2 flops; profiles/k_stm_orbits.md)
+# FMA = 2 flops)
 FLOPS_PER_BODY_STEP = 108.0
-# DRAM traffic of one orbit-kernel launch on this chunk, from one ncu capture (same profile summary), bytes
-ORBIT_TRAFFIC_BYTES = None
+# DRAM traffic of one k_stm_orbits launch on this chunk (dram__bytes_read.sum + dram__bytes_write.sum from one ncu
+# capture of `python -m phygas_gb300.run_screen --stars 20000`): 4.9 MB read + 711.8 MB of orbit output written
+ORBIT_TRAFFIC_BYTES = 716.7e6
 
 
 def log(*a):

@@ -137,6 +137,97 @@ def cpu_baseline(cp, tp, stars_per_proc=192, procs=None):
                           stars_per_proc * procs, N_CLUSTERS, procs, stars_per_proc, max(runs), max(preps), wall)}
 
 
+# Batched uneven Monte Carlo (the benchmark spec's C3 shape, scaled to a benchmark step): C3_SCREEN_PAIRS pairs from the
+# mixed screen's rows with p_r50 >= 0.001, plus C3_PULSARS synthetic pulsars x their prefiltered clusters; clone
+# counts uniform in {200, 500, 1000}; steps = ceil(tmax / 0.05 Myr).  A synthetic pulsar (pm error 1 mas/yr, no
+# parallax) reaches ~96 % of the 4,087 clusters, so the 702 pulsars of the full configuration are ~1e12 clone-steps;
+# two stand in for them here.
+C3_SCREEN_PAIRS, C3_PULSARS, C3_SEED = 10000, 2, 1003
+
+
+def pair_cpu_baseline(cp, pp, n_clones=200, clusters_per_proc=24, procs=None):
+    """Oracle pair Monte Carlo on all host cores: process p traces pulsar 0 against clusters
+    [p * k, (p + 1) * k) (prefiltered, n_clones clones each); clone-steps/s from the slowest process's loop time."""
+    import math
+    from tests import oracle_tools as ot
+    import phygas_gb300 as pg
+    procs = procs or os.cpu_count() or 1
+    tmp = tempfile.mkdtemp(prefix="phygas_cpu_pair_")
+    inp = os.path.join(tmp, "in")
+    with open(pp) as f, open(inp, "w") as g:
+        g.write("PHYGAS 1 pair %d 0.05\n" % n_clones)
+        g.write(f.readline())
+    k = clusters_per_proc
+    ps = [subprocess.Popen([ot.ORACLE_WU, cp, inp, "0", "1", str(p * k), str((p + 1) * k)], stdout=subprocess.PIPE,
+                           stderr=subprocess.PIPE, text=True) for p in range(procs)]
+    tmax = {c.name.decode(): c.tmax_myr for c in pg.read_clusters(cp)}
+    runs, clone_steps = [], 0
+    for p in ps:
+        out, err = p.communicate()
+        if p.returncode:
+            raise RuntimeError("oracle_wu pair failed: " + err[-500:])
+        runs.append(float(err.split("wu_time")[-1].split()[3]))
+        for ln in out.splitlines():
+            f = ln.split()
+            clone_steps += int(f[3]) * int(math.ceil(tmax[f[1]] / 0.05 - 1e-9))
+    return {"value": clone_steps / max(runs), "unit": "clone-steps/s", "cores": procs, "kind": "port",
+            "sample": "1 synthetic pulsar x %d prefiltered clusters (%d per process) x %d clones, %.3g clone-steps; "
+                      "slowest process %.1f s" % (procs * k, k, n_clones, clone_steps, max(runs))}
+
+
+def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu):
+    """C3-style batch: draws on the host, the autotuner on a sample of it, then the batch timed on the GPU."""
+    import numpy as np
+    import phygas_gb300 as pg
+    from phygas_gb300 import synth
+    sel = np.flatnonzero(rows["p_r50"] >= 0.001)
+    take = sel[np.unique(np.linspace(0, len(sel) - 1, min(C3_SCREEN_PAIRS, len(sel))).astype(np.int64))]
+    tmp = tempfile.mkdtemp(prefix="phygas_c3_")
+    pp = os.path.join(tmp, "pulsars.txt")
+    with open(pp, "w") as f:
+        f.write("\n".join(synth.pulsars(C3_PULSARS, C3_SEED)) + "\n")
+    pulsars = pg.read_targets(pp)
+    t0 = time.perf_counter()
+    pti, pci = pg.prefilter_pairs(pulsars, clusters)
+    t_pref = time.perf_counter() - t0
+    targets = list(stars) + list(pulsars)
+    ti = np.concatenate([rows["star"][take], pti + len(stars)]).astype(np.int32)
+    ci = np.concatenate([rows["cluster"][take], pci]).astype(np.int32)
+    ncl = np.random.default_rng(C3_SEED).choice([200, 500, 1000], len(ti)).astype(np.int32)
+    t0 = time.perf_counter()
+    batch = pg.draw_pair_batch(targets, ti, clusters, ci, ncl, 0.05)
+    t_draw = time.perf_counter() - t0
+    best, table = ctx.tune_pair(*pg.draw_pair_batch(targets, ti[::25], clusters, ci[::25], ncl[::25], 0.05))
+    ctx.pair(*batch)                                         # warm-up
+    ms, walls = [], []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        ctx.pair(*batch)
+        walls.append(time.perf_counter() - t0)
+        st = ctx.stats()
+        ms.append(st["ms_pair"])
+    cs = st["clone_steps"]
+    out = {"metric": "clone-steps/s", "value": cs / (statistics.mean(ms) * 1e-3), "unit": "clone-steps/s",
+           "ms_per_batch": statistics.mean(ms),
+           "workload": "%d screen pairs (p_r50 >= 0.001) + %d pulsars x %d prefiltered clusters; clones U{200,500,1000}, "
+                       "dt 0.05 Myr" % (len(take), C3_PULSARS, len(pti)),
+           "pairs": int(len(ti)), "clones": int(st["clones"]), "clone_steps": int(cs),
+           "launch": "one captured CUDA graph (prep, persistent trace, reduce) per shape, replayed per batch",
+           "autotune": {"chosen": {"warps_per_block": table[best][0], "clones_per_lane": table[best][1]},
+                        "ms_on_sample": [{"warps_per_block": w, "clones_per_lane": c, "ms": t} for w, c, t in table]},
+           "e2e": {"value": cs / (t_draw + statistics.mean(walls)), "unit": "clone-steps/s",
+                   "host_draw_s": t_draw, "prefilter_s": t_pref, "gpu_call_s": statistics.mean(walls),
+                   "h2d_bytes_per_step": int(12 * 8 * st["clones"] + 28 * len(ti)),
+                   "d2h_bytes_per_step": int(96 * len(ti))},
+           "cpu_baseline": None}
+    if want_cpu:
+        try:
+            out["cpu_baseline"] = pair_cpu_baseline(cp, pp)
+        except Exception as e:
+            log("pair cpu baseline failed: %s" % e)
+    return out
+
+
 def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -176,6 +267,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-pair", action="store_true", help="skip the batched Monte Carlo measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -256,6 +348,13 @@ def main():
     h2d = N_STARS * (6 + 21 + 1) * 8
     d2h = len(r) * pg.ROW_DTYPE.itemsize + 8
 
+    pair_mc = None
+    if not args.no_pair:
+        try:
+            pair_mc = pair_mc_measure(ctx, stars, clusters, cp, r, rank == 0 and not args.no_cpu)
+        except Exception as e:          # reported beside the headline, not part of it
+            log("pair Monte Carlo measurement failed: %s" % e)
+
     s = stats[-1]
     orbit_ms = statistics.mean(x["ms_orbit"] for x in stats)
     achieved = FLOPS_PER_BODY_STEP * s["body_steps"] / (orbit_ms * 1e-3)
@@ -293,6 +392,7 @@ def main():
             "gpu_launches": int(sum(x["kernels"] for x in stats)),
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
+            "pair_mc": pair_mc,
         }
         print(json.dumps(out))
     ctx.close()

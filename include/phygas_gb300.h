@@ -82,6 +82,20 @@ int pgx_draw_targets(const PhTarget *t, int n, int n_samp, int threads, double *
 int pgx_draw_clusters(const PhCluster *c, int n, int n_samp, int threads, double *ps0, double *sig);
 uint64_t pgx_seed_prefix(const char *target_id);
 
+/* Pair jobs on the host (the reference's pair mode: phygas_cli's target loop, src/phygas_cli.c:37-51, and
+ * ph_pair_draw, src/phygas.c:182-198):
+ * pgx_prefilter_pairs -- the (target, cluster) pairs that pass ph_prefilter, tracks built as the reference's CLI
+ *   builds them (32 spread clones, seeds ph_seed("track", id/name), traced back over the longest cluster tmax); pair
+ *   k = (ti[k], ci[k]) in (target, cluster) order; at most cap pairs written, *n = how many pass.
+ * pgx_draw_pair_batch -- ph_pair_draw for pair q = (t[ti[q]], c[ci[q]]) with its own clone count n_clones[q] and the
+ *   pair's seed ph_seed(id, name): the clones of all pairs back to back in ps (room for 12 * sum(n_clones) doubles),
+ *   clone_off[n_pairs + 1], and per pair steps, dt, r50_pc, rtot_pc -- the arguments of pgx_pair. */
+int pgx_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti, int *ci,
+                        long cap, long *n);
+int pgx_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
+                        const int *n_clones, double dt_myr, int threads, int *clone_off, double *ps, int *steps,
+                        double *dt, double *r50_pc, double *rtot_pc);
+
 /* ---- pair Monte Carlo ------------------------------------------------------------------------------------------ */
 /* Trace every clone of n_pairs pairs back and reduce each pair (reference ph_pair_clone + ph_pair_reduce,
  * src/phygas.c:200-238; GPU pg_pair + the host reduction of src/main_phygas_boinc.cpp:236-246).
@@ -91,6 +105,17 @@ uint64_t pgx_seed_prefix(const char *target_id);
  * vbest kpc/Myr, clone-major blocks) the per-clone closest approaches. */
 int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,
              const double *dt, const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out);
+
+/* Launch-shape autotuner of the clone kernel (no counterpart in the reference): runs the batch (the arguments of
+ * pgx_pair) with every shape this build has -- warps per block x clones traced per lane -- and keeps the fastest for
+ * this context's later pgx_pair calls.  ms[pgx_pair_shapes()] (or NULL) gets each shape's device time; *best (or NULL)
+ * its index.  Every shape must give the same bits: a shape whose results differ fails the call (PGX_E_CUDA).
+ * Batches whose pairs all have at most 1024 clones run as one captured CUDA graph (prep, persistent trace, reduce)
+ * replayed with the batch's parameters; the tuner's runs also capture each shape's graph. */
+int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,
+                  const double *dt, const double *r50_pc, const double *rtot_pc, double *ms, int *best);
+/* number of launch shapes; the first n as (warps per block, clones per lane) */
+int pgx_pair_shapes(int n, int *warps, int *clones_per_lane);
 
 /* pgx_pair for callers that cannot allocate GPU memory (no counterpart in the reference): code running inside
  * another framework's device memory pool, loops that must not stall on the allocator, hosts that can only hand

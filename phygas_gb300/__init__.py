@@ -81,7 +81,13 @@ SIGNATURES = [
     ("pgx_draw_targets", C.c_int, [_P(PhTarget), C.c_int, C.c_int, C.c_int, _D, _D, _U64]),
     ("pgx_draw_clusters", C.c_int, [_P(PhCluster), C.c_int, C.c_int, C.c_int, _D, _D]),
     ("pgx_seed_prefix", C.c_uint64, [C.c_char_p]),
+    ("pgx_prefilter_pairs", C.c_int, [_P(PhTarget), C.c_int, _P(PhCluster), C.c_int, C.c_int, _I, _I, C.c_long,
+                                      _P(C.c_long)]),
+    ("pgx_draw_pair_batch", C.c_int, [C.c_int, _P(PhTarget), _I, _P(PhCluster), _I, _I, C.c_double, C.c_int, _I, _D,
+                                      _I, _D, _D, _D]),
     ("pgx_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, C.c_void_p, _D]),
+    ("pgx_tune_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, _D, _I]),
+    ("pgx_pair_shapes", C.c_int, [C.c_int, _I, _I]),
     ("pgx_stats", C.c_int, [C.c_void_p, _P(PgxStats)]),
     ("pgx_peaks", C.c_int, [C.c_void_p, _D, _D]),
     ("pgx_check_bounds", C.c_int, [C.c_void_p, C.c_int, _D, _D, _D, C.c_double, _D, _P(C.c_float),
@@ -287,6 +293,60 @@ class Context:
                                    _ptr(dt), _ptr(r50), _ptr(rt), res.ctypes.data,
                                    _ptr(clones) if want_clones else None), "pgx_pair")
         return (res, clones) if want_clones else res
+
+    def tune_pair(self, clone_off, ps, steps, dt, r50_pc, rtot_pc):
+        """Time every launch shape of the clone kernel on this batch and keep the fastest (pgx_tune_pair):
+        -> (index of the chosen shape, [(warps per block, clones per lane, ms), ...])."""
+        args = [np.ascontiguousarray(clone_off, np.int32), np.ascontiguousarray(ps, np.float64),
+                np.ascontiguousarray(steps, np.int32), np.ascontiguousarray(dt, np.float64),
+                np.ascontiguousarray(r50_pc, np.float64), np.ascontiguousarray(rtot_pc, np.float64)]
+        shapes = pair_shapes()
+        ms, best = np.zeros(len(shapes)), C.c_int()
+        self._check(lib().pgx_tune_pair(self.h, len(args[2]), _ptr(args[0], C.c_int), _ptr(args[1]),
+                                        _ptr(args[2], C.c_int), _ptr(args[3]), _ptr(args[4]), _ptr(args[5]),
+                                        _ptr(ms), C.byref(best)), "pgx_tune_pair")
+        return best.value, [(w, c, t) for (w, c), t in zip(shapes, ms.tolist())]
+
+
+def pair_shapes():
+    """The clone kernel's launch shapes: [(warps per block, clones per lane), ...]."""
+    n = lib().pgx_pair_shapes(0, None, None)
+    w, c = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    lib().pgx_pair_shapes(n, _ptr(w, C.c_int), _ptr(c, C.c_int))
+    return list(zip(w.tolist(), c.tolist()))
+
+
+def prefilter_pairs(targets, clusters, threads=0):
+    """(target index, cluster index) arrays of the pairs that pass ph_prefilter (see pgx_prefilter_pairs)."""
+    targets, clusters = as_array(targets, PhTarget), as_array(clusters, PhCluster)
+    n = C.c_long()
+    cap = 0
+    for _ in range(2):
+        ti, ci = np.zeros(max(cap, 1), np.int32), np.zeros(max(cap, 1), np.int32)
+        rc = lib().pgx_prefilter_pairs(targets, len(targets), clusters, len(clusters), threads, _ptr(ti, C.c_int),
+                                       _ptr(ci, C.c_int), cap, C.byref(n))
+        if rc:
+            raise ValueError("pgx_prefilter_pairs: %d" % rc)
+        if n.value <= cap:
+            return ti[:n.value], ci[:n.value]
+        cap = n.value
+    raise RuntimeError("pgx_prefilter_pairs: pair count changed between calls")
+
+
+def draw_pair_batch(targets, ti, clusters, ci, n_clones, dt_myr=0.05, threads=0):
+    """pgx_draw_pair_batch: host clone draws with a clone count per pair -> clone_off, ps, steps, dt, r50, rtot."""
+    targets, clusters = as_array(targets, PhTarget), as_array(clusters, PhCluster)
+    ti, ci = np.ascontiguousarray(ti, np.int32), np.ascontiguousarray(ci, np.int32)
+    nc = np.ascontiguousarray(np.broadcast_to(n_clones, ti.shape), np.int32)
+    n = len(ti)
+    off, ps = np.zeros(n + 1, np.int32), np.zeros(12 * max(int(nc.sum()), 1))
+    steps, dt, r50, rt = np.zeros(n, np.int32), np.zeros(n), np.zeros(n), np.zeros(n)
+    rc = lib().pgx_draw_pair_batch(n, targets, _ptr(ti, C.c_int), clusters, _ptr(ci, C.c_int), _ptr(nc, C.c_int),
+                                   dt_myr, threads, _ptr(off, C.c_int), _ptr(ps), _ptr(steps, C.c_int), _ptr(dt),
+                                   _ptr(r50), _ptr(rt))
+    if rc:
+        raise ValueError("pgx_draw_pair_batch: %d" % rc)
+    return off, ps[:12 * int(off[-1])], steps, dt, r50, rt
 
 
 def pair_draws(targets, clusters, pairs, n_clones, dt_myr=0.05):

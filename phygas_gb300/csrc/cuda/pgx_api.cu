@@ -50,7 +50,9 @@ struct PgxContext {
     pgx::MixedBufs mixed;
     long n_rows = 0;
     // pair Monte Carlo
-    Buf p_off, p_ps, p_steps, p_dt, p_r50, p_rt, p_items, p_q, p_done, p_cres, p_res;
+    Buf p_off, p_ps, p_steps, p_dt, p_r50, p_rt, p_items, p_q, p_done, p_cres, p_res, p_params;
+    int mc_variant = 0;                        // launch shape of the clone kernel (pgx_tune_pair picks it)
+    cudaGraphExec_t mc_exec[16] = {};          // prep + trace + reduce, captured once per shape, replayed
     // one-object helpers of the drop-in API
     Buf x_ps0, x_sig21, x_npts, x_opos, x_ovel, x_t64, x_t32, x_lm;
     PgxStats stats = {};
@@ -196,11 +198,14 @@ void pgx_close(PgxContext *ctx) {
                    &ctx->s_sig21, &ctx->s_prefix, &ctx->opos, &ctx->ovel, &ctx->t64, &ctx->t32, &ctx->chi2T,
                    &ctx->kbT, &ctx->sbT, &ctx->cnt, &ctx->off, &ctx->total, &ctx->kept, &ctx->fin, &ctx->rows,
                    &ctx->p_off, &ctx->p_ps, &ctx->p_steps, &ctx->p_dt, &ctx->p_r50, &ctx->p_rt, &ctx->p_items,
-                   &ctx->p_q, &ctx->p_done, &ctx->p_cres, &ctx->p_res, &ctx->x_ps0, &ctx->x_sig21, &ctx->x_npts,
+                   &ctx->p_q, &ctx->p_done, &ctx->p_cres, &ctx->p_res, &ctx->p_params, &ctx->x_ps0, &ctx->x_sig21,
+                   &ctx->x_npts,
                    &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32};
     for (Buf *b : bufs)
         if (b->p) cudaFree(b->p);
     pgx::mixed_free(ctx->mixed);
+    for (auto &g : ctx->mc_exec)
+        if (g) cudaGraphExecDestroy(g);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -222,6 +227,30 @@ int pgx_draw_clusters(const PhCluster *c, int n, int n_samp, int threads, double
     if (n < 0 || (n > 0 && (!c || !ps0 || !sig)) || n_samp < 0) return PGX_E_ARG;
     pgh_draw_clusters(c, n, n_samp, threads > 0 ? threads : pgh_default_threads(), ps0, sig);
     return 0;
+}
+
+int pgx_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti, int *ci,
+                        long cap, long *n) {
+    if (nt < 0 || nc < 0 || cap < 0 || !n || (nt > 0 && !t) || (nc > 0 && !c) || (cap > 0 && (!ti || !ci)))
+        return PGX_E_ARG;
+    const long r = pgh_prefilter_pairs(t, nt, c, nc, threads > 0 ? threads : pgh_default_threads(), ti, ci, cap);
+    if (r < 0) return PGX_E_NOMEM;
+    *n = r;
+    return 0;
+}
+
+int pgx_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
+                        const int *n_clones, double dt_myr, int threads, int *clone_off, double *ps, int *steps,
+                        double *dt, double *r50_pc, double *rtot_pc) {
+    if (n_pairs < 0 || !clone_off) return PGX_E_ARG;
+    if (n_pairs > 0 && (!t || !ti || !c || !ci || !n_clones || !ps || !steps || !dt || !r50_pc || !rtot_pc))
+        return PGX_E_ARG;
+    for (int q = 0; q < n_pairs; q++)
+        if (n_clones[q] < 0 || n_clones[q] > 16384) return PGX_E_LIMIT;
+    const int r = pgh_draw_pair_batch(n_pairs, t, ti, c, ci, n_clones, dt_myr,
+                                      threads > 0 ? threads : pgh_default_threads(), clone_off, ps, steps, dt,
+                                      r50_pc, rtot_pc);
+    return r == 0 ? 0 : (r == -1 ? PGX_E_NOMEM : PGX_E_LIMIT);
 }
 
 int pgx_stats(const PgxContext *ctx, PgxStats *out) {
@@ -535,8 +564,34 @@ int pgx_screen(PgxContext *ctx, int nt, const double *ps0, const double *sig, co
     return 0;
 }
 
-int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps, const double *dt,
-             const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out) {
+namespace {
+// the captured prep + trace + reduce sequence of clone-kernel variant v (parameters read from ctx->p_params)
+int mc_graph(PgxContext *ctx, int v, cudaGraphExec_t &exec) {
+    if (ctx->mc_exec[v]) {
+        exec = ctx->mc_exec[v];
+        return 0;
+    }
+    RET(ensure(ctx, ctx->p_params, sizeof(pgx::McPairs)));
+    int grid = 0;
+    CK(pgx::mc_variant_grid(v, ctx->sms, grid));
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t le = pgx::launch_mc(v, grid, ctx->sms * 4, ctx->sms * 8, ctx->st,
+                                          P<pgx::McPairs>(ctx->p_params));
+    const cudaError_t ce = cudaStreamEndCapture(ctx->st, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(ctx, PGX_E_CUDA, "clone graph capture: %s", cudaGetErrorString(le != cudaSuccess ? le : ce));
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&ctx->mc_exec[v], g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return fail(ctx, PGX_E_CUDA, "clone graph instantiate: %s", cudaGetErrorString(ie));
+    exec = ctx->mc_exec[v];
+    return 0;
+}
+
+int pair_run(PgxContext *ctx, int variant, int n_pairs, const int *clone_off, const double *ps, const int *steps,
+             const double *dt, const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out) {
     if (!ctx) return PGX_E_ARG;
     if (n_pairs < 0 || (n_pairs > 0 && (!clone_off || !steps || !dt || !r50_pc || !rtot_pc || !res)))
         return fail(ctx, PGX_E_ARG, "pgx_pair: bad args");
@@ -544,20 +599,32 @@ int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *p
     CK(cudaSetDevice(ctx->device));
     const int M = clone_off[n_pairs];
     if (clone_off[0] != 0 || M < 0 || (M > 0 && !ps)) return fail(ctx, PGX_E_ARG, "pgx_pair: clone_off");
-    std::vector<int4> items;
-    int big_n2 = 0;
-    long long clone_steps = 0;
+    int warps = 4, cpl = 1;
+    pgx::mc_variant_shape(variant, warps, cpl);
+    int mmax = 0;
     for (int p = 0; p < n_pairs; p++) {
         const int m = clone_off[p + 1] - clone_off[p];
         if (m < 0) return fail(ctx, PGX_E_ARG, "pgx_pair: clone_off not ascending at %d", p);
         if (m > 16384) return fail(ctx, PGX_E_LIMIT, "pgx_pair: pair %d has %d clones (limit 16384)", p, m);
         if (steps[p] < 0) return fail(ctx, PGX_E_ARG, "pgx_pair: steps[%d] = %d", p, steps[p]);
+        mmax = std::max(mmax, m);
+    }
+    // pairs of at most 1024 clones (every batch of the benchmark and serving workloads) run the captured
+    // prep + trace + reduce graph; bigger pairs the fused kernel and the block-wide reduction
+    const bool graph = mmax <= 1024;
+    const int chunk = graph ? 32 * cpl : 32;
+    std::vector<int4> items;
+    int big_n2 = 0;
+    long long clone_steps = 0;
+    for (int p = 0; p < n_pairs; p++) {
+        const int m = clone_off[p + 1] - clone_off[p];
         if (m > 1024) {
             int n2 = 1;
             while (n2 < m) n2 <<= 1;
             big_n2 = std::max(big_n2, n2);
         }
-        for (int c0 = 0; c0 < m; c0 += 32) items.push_back(make_int4(p, clone_off[p] + c0, std::min(32, m - c0), 0));
+        for (int c0 = 0; c0 < m; c0 += chunk)
+            items.push_back(make_int4(p, clone_off[p] + c0, std::min(chunk, m - c0), 0));
         clone_steps += (long long)m * steps[p];
     }
     std::stable_sort(items.begin(), items.end(), [&](const int4 &a, const int4 &b) { return steps[a.x] > steps[b.x]; });
@@ -580,8 +647,6 @@ int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *p
     CK(cudaMemcpyAsync(ctx->p_rt.p, rtot_pc, (size_t)n_pairs * 8, cudaMemcpyHostToDevice, ctx->st));
     if (!items.empty())
         CK(cudaMemcpyAsync(ctx->p_items.p, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemsetAsync(ctx->p_q.p, 0, 16, ctx->st));
-    CK(cudaMemsetAsync(ctx->p_done.p, 0, (size_t)n_pairs * 4, ctx->st));
     pgx::McPairs Pp;
     Pp.n_pairs = n_pairs; Pp.n_clones = M; Pp.n_items = (int)items.size();
     Pp.clone_off = P<int>(ctx->p_off); Pp.ps = P<double>(ctx->p_ps); Pp.steps = P<int>(ctx->p_steps);
@@ -589,23 +654,35 @@ int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *p
     Pp.items = P<int4>(ctx->p_items); Pp.qhead = P<int>(ctx->p_q); Pp.done = P<int>(ctx->p_done);
     Pp.cres = P<double>(ctx->p_cres); Pp.res = P<pgx::PhResultDev>(ctx->p_res);
     ctx->stats = PgxStats();
-    CK(cudaEventRecord(ctx->ev[EV_PAIR0], ctx->st));
-    if (!items.empty()) {
-        int per_sm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pgx::k_pair_mc, pgx::kMcThreads, 0));
-        const int warps_needed = (int)items.size();
-        int grid = std::max(1, ctx->sms * std::max(1, per_sm));
-        grid = std::min(grid, (warps_needed + pgx::kMcThreads / 32 - 1) / (pgx::kMcThreads / 32));
-        pgx::k_pair_mc<<<grid, pgx::kMcThreads, 0, ctx->st>>>(Pp);
+    if (graph) {
+        cudaGraphExec_t exec;
+        RET(mc_graph(ctx, variant, exec));
+        // the parameters travel by copy: the graph's kernels read them from p_params
+        CK(cudaMemcpyAsync(ctx->p_params.p, &Pp, sizeof Pp, cudaMemcpyHostToDevice, ctx->st));
+        CK(cudaEventRecord(ctx->ev[EV_PAIR0], ctx->st));
+        CK(cudaGraphLaunch(exec, ctx->st));
+        ctx->stats.kernels += 3;
+    } else {
+        CK(cudaMemsetAsync(ctx->p_q.p, 0, 16, ctx->st));
+        CK(cudaMemsetAsync(ctx->p_done.p, 0, (size_t)n_pairs * 4, ctx->st));
+        CK(cudaEventRecord(ctx->ev[EV_PAIR0], ctx->st));
+        if (!items.empty()) {
+            int per_sm = 0;
+            CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pgx::k_pair_mc, pgx::kMcThreads, 0));
+            const int warps_needed = (int)items.size();
+            int grid = std::max(1, ctx->sms * std::max(1, per_sm));
+            grid = std::min(grid, (warps_needed + pgx::kMcThreads / 32 - 1) / (pgx::kMcThreads / 32));
+            pgx::k_pair_mc<<<grid, pgx::kMcThreads, 0, ctx->st>>>(Pp);
+            CKL();
+            ctx->stats.kernels++;
+        }
+        const size_t smem = (size_t)big_n2 * 8;
+        if (smem > 48 * 1024)
+            CK(cudaFuncSetAttribute(pgx::k_pair_reduce_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        pgx::k_pair_reduce_big<<<n_pairs, 256, smem, ctx->st>>>(Pp);
         CKL();
         ctx->stats.kernels++;
     }
-    const size_t smem = (size_t)big_n2 * 8;
-    if (smem > 48 * 1024)
-        CK(cudaFuncSetAttribute(pgx::k_pair_reduce_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    pgx::k_pair_reduce_big<<<n_pairs, 256, smem, ctx->st>>>(Pp);
-    CKL();
-    ctx->stats.kernels++;
     CK(cudaEventRecord(ctx->ev[EV_PAIR1], ctx->st));
     CK(cudaMemcpyAsync(res, ctx->p_res.p, (size_t)n_pairs * sizeof(PhResult), cudaMemcpyDeviceToHost, ctx->st));
     if (clone_out && M > 0)
@@ -618,6 +695,43 @@ int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *p
     ctx->stats.body_steps = 2 * clone_steps;
     ctx->stats.pairs = n_pairs;
     return 0;
+}
+}  // namespace
+
+int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps, const double *dt,
+             const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out) {
+    if (!ctx) return PGX_E_ARG;
+    return pair_run(ctx, ctx->mc_variant, n_pairs, clone_off, ps, steps, dt, r50_pc, rtot_pc, res, clone_out);
+}
+
+int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,
+                  const double *dt, const double *r50_pc, const double *rtot_pc, double *ms, int *best) {
+    if (!ctx) return PGX_E_ARG;
+    if (n_pairs <= 0) return fail(ctx, PGX_E_ARG, "pgx_tune_pair: empty batch");
+    const int nv = pgx::mc_variants();
+    std::vector<PhResult> ref(n_pairs), got(n_pairs);
+    int b = 0;
+    double bms = 0;
+    for (int v = 0; v < nv; v++) {
+        PhResult *out = v == 0 ? ref.data() : got.data();
+        // twice: the first run of a shape also captures and instantiates its graph
+        RET(pair_run(ctx, v, n_pairs, clone_off, ps, steps, dt, r50_pc, rtot_pc, out, nullptr));
+        RET(pair_run(ctx, v, n_pairs, clone_off, ps, steps, dt, r50_pc, rtot_pc, out, nullptr));
+        const double t = ctx->stats.ms_pair;
+        if (ms) ms[v] = t;
+        if (v > 0 && memcmp(ref.data(), got.data(), sizeof(PhResult) * (size_t)n_pairs) != 0)
+            return fail(ctx, PGX_E_CUDA, "pgx_tune_pair: launch shape %d changed the results", v);
+        if (v == 0 || t < bms) { b = v; bms = t; }
+    }
+    ctx->mc_variant = b;
+    if (best) *best = b;
+    return 0;
+}
+
+int pgx_pair_shapes(int n, int *warps, int *clones_per_lane) {
+    const int nv = pgx::mc_variants();
+    for (int v = 0; v < n && v < nv; v++) pgx::mc_variant_shape(v, warps[v], clones_per_lane[v]);
+    return nv;
 }
 
 }  // extern "C"

@@ -68,6 +68,13 @@ __global__ void k_stm_orbits(int N, const double *ps0, const int *npts, int nmax
 __global__ void k_stm_cov(int N, int nmax, const int *npts, const double *opos, const double *ovel,
                           const double *sig21, double *t64, float4 *t32, float *lm);
 __global__ void k_pair_mc(McPairs P);
+// launch-shape variants of the persistent clone kernel (parameters in device memory): count, shape (warps per block,
+// clones per lane), full persistent grid, and the prep + trace + reduce kernels as one sequence on a stream (pairs of
+// at most 1024 clones)
+int mc_variants();
+void mc_variant_shape(int v, int &warps, int &cpl);
+cudaError_t mc_variant_grid(int v, int sms, int &grid);
+cudaError_t launch_mc(int v, int grid, int prep_grid, int reduce_grid, cudaStream_t st, const McPairs *Pd);
 __global__ void k_pair_reduce_big(McPairs P);
 __global__ void k_pair_reduce_only(McPairs P);
 __global__ void k_peak_dfma(double *out, int iters, double a, double b);

@@ -12,6 +12,12 @@
 //                  src/phygas.c:200-216); the warp that finishes a pair's last item reduces it in registers
 //                  with warp shuffles (reference ph_pair_reduce, src/phygas.c:218-238)
 //   k_pair_reduce_big  the same reduction for pairs of more than 1024 clones, one CTA per pair in shared memory
+//   k_mc_prep, k_pair_mc_t, k_pair_reduce_dev  the same work as one captured CUDA graph for batches of pairs of at
+//                  most 1024 clones: parameters read from device memory, tracing separate from the reduction, and
+//                  the tracing kernel's launch shape (warps per block, clones per lane) a template the autotuner picks
+//
+// Built with --fmad=false: every fused multiply-add is an explicit fma(), so the rounding does not depend on how the
+// compiler arranges a kernel, and every launch shape gives the same bits.
 #include <algorithm>
 #include <cstdio>
 #include <mutex>
@@ -123,57 +129,68 @@ __global__ void __launch_bounds__(256) k_stm_cov(int N, int nmax, const int *__r
 // ---------------------------------------------------------------------------------------------------------------
 // clone Monte Carlo
 
-// closest approach of one clone (ps: target pos/vel, cluster pos/vel); results in kpc, Myr, kpc/Myr
-__device__ __forceinline__ void trace_clone(const double *__restrict__ ps, int steps, double dt, double &best_o,
-                                            double &tbest_o, double &vbest_o) {
+// One clone traced back: the target's and the cluster's orbit, the closest approach so far (reference
+// ph_pair_clone and seg_min, src/phygas.c:147-156, 200-216).  Results in kpc, Myr, kpc/Myr.
+struct Clone {
     Orbit a, b;
-    a.x = ps[0]; a.y = ps[1]; a.z = ps[2]; a.vx = ps[3]; a.vy = ps[4]; a.vz = ps[5];
-    b.x = ps[6]; b.y = ps[7]; b.z = ps[8]; b.vx = ps[9]; b.vy = ps[10]; b.vz = ps[11];
-    a.init();
-    b.init();
-    double r0x = a.x - b.x, r0y = a.y - b.y, r0z = a.z - b.z;
-    double r0s = r0x * r0x + r0y * r0y + r0z * r0z;
-    double best = sqrt(r0s), best2 = r0s, tbest = 0.0;
-    double ux = a.vx - b.vx, uy = a.vy - b.vy, uz = a.vz - b.vz;
-    double vbest = sqrt(ux * ux + uy * uy + uz * uz);
-    const double h = 0.5 * dt;
-#pragma unroll 1
-    for (int i = 1; i <= steps; i++) {
+    double r0x, r0y, r0z, r0s, best, best2, tbest, vbest;
+    __device__ __forceinline__ void start(const double *__restrict__ ps) {
+        a.x = ps[0]; a.y = ps[1]; a.z = ps[2]; a.vx = ps[3]; a.vy = ps[4]; a.vz = ps[5];
+        b.x = ps[6]; b.y = ps[7]; b.z = ps[8]; b.vx = ps[9]; b.vy = ps[10]; b.vz = ps[11];
+        a.init();
+        b.init();
+        r0x = a.x - b.x; r0y = a.y - b.y; r0z = a.z - b.z;
+        r0s = fma(r0x, r0x, fma(r0y, r0y, r0z * r0z));
+        best = sqrt(r0s); best2 = r0s; tbest = 0.0;
+        const double ux = a.vx - b.vx, uy = a.vy - b.vy, uz = a.vz - b.vz;
+        vbest = sqrt(fma(ux, ux, fma(uy, uy, uz * uz)));
+    }
+    // step i (1-based) of length dt (negative), h = dt / 2
+    __device__ __forceinline__ void step(int i, double dt, double h) {
         a.kdk(dt, h);
         b.kdk(dt, h);
         const double r1x = a.x - b.x, r1y = a.y - b.y, r1z = a.z - b.z;
         const double dx = r1x - r0x, dy = r1y - r0y, dz = r1z - r0z;
-        const double dd = dx * dx + dy * dy + dz * dz;
-        const double an = r0x * dx + r0y * dy + r0z * dz;
-        const double r1s = r1x * r1x + r1y * r1y + r1z * r1z;
+        const double dd = fma(dx, dx, fma(dy, dy, dz * dz));
+        const double an = fma(r0x, dx, fma(r0y, dy, r0z * dz));
+        const double r1s = fma(r1x, r1x, fma(r1y, r1y, r1z * r1z));
         // squared distance of the segment r0 -> r1 from the origin, times dd (no division): the cheap pre-test
         double near2dd;
         if (!(dd > 0) || an >= 0) near2dd = r0s * dd;
         else if (-an >= dd) near2dd = r1s * dd;
-        else near2dd = r0s * dd - an * an;
+        else near2dd = fma(r0s, dd, -an * an);
         if (near2dd < best2 * dd * (1.0 + 1e-12) || (!(dd > 0) && r0s < best2 * (1.0 + 1e-12))) {
-            // the reference's segment minimum (seg_min, src/phygas.c:147-156) and its strict comparison
+            // the reference's segment minimum (seg_min) and its strict comparison
             double s = 0.0;
             if (dd > 0) {
                 s = -an / dd;
                 s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
             }
             const double mx = fma(dx, s, r0x), my = fma(dy, s, r0y), mz = fma(dz, s, r0z);
-            const double dm = sqrt(mx * mx + my * my + mz * mz);
+            const double dm = sqrt(fma(mx, mx, fma(my, my, mz * mz)));
             if (dm < best) {
                 best = dm;
                 best2 = dm * dm;
                 tbest = ((double)(i - 1) + s) * -dt;
                 const double wx = a.vx - b.vx, wy = a.vy - b.vy, wz = a.vz - b.vz;
-                vbest = sqrt(wx * wx + wy * wy + wz * wz);
+                vbest = sqrt(fma(wx, wx, fma(wy, wy, wz * wz)));
             }
         }
         r0x = r1x; r0y = r1y; r0z = r1z;
         r0s = r1s;
     }
-    best_o = best;
-    tbest_o = tbest;
-    vbest_o = vbest;
+};
+
+__device__ __forceinline__ void trace_clone(const double *__restrict__ ps, int steps, double dt, double &best_o,
+                                            double &tbest_o, double &vbest_o) {
+    Clone c;
+    c.start(ps);
+    const double h = 0.5 * dt;
+#pragma unroll 1
+    for (int i = 1; i <= steps; i++) c.step(i, dt, h);
+    best_o = c.best;
+    tbest_o = c.tbest;
+    vbest_o = c.vbest;
 }
 
 // ---- reduction of one pair (m clones) ---------------------------------------------------------------------------
@@ -322,6 +339,107 @@ __global__ void __launch_bounds__(kMcThreads) k_pair_mc(McPairs P) {
             if (m <= 1024) reduce_dispatch(P, p, smem[w], lane);
         }
     }
+}
+
+// Persistent clone tracing for batches replayed from a captured graph: parameters read from device memory, and the
+// launch shape a template: WARPS warps per block, CPL clones per lane traced in lockstep (items of up to 32 * CPL
+// clones; a lane past its item's end repeats its first clone and discards the copy).  Tracing only -- the pairs are
+// reduced by k_pair_reduce_dev afterwards, which keeps this kernel's registers to the orbits'.  The clones'
+// arithmetic is the same in every variant, so every variant gives the same bits.
+template <int WARPS, int CPL>
+__global__ void __launch_bounds__(WARPS * 32) k_pair_mc_t(const McPairs *__restrict__ Pd) {
+    const McPairs P = *Pd;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(P.qhead, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= P.n_items) break;
+        const int4 it = P.items[q];   // x = pair, y = first clone, z = count
+        if (lane >= it.z) continue;
+        const int p = it.x;
+        const int steps = P.steps[p];
+        const double dt = P.dt[p], h = 0.5 * dt;
+        Clone c[CPL];
+#pragma unroll
+        for (int j = 0; j < CPL; j++) {
+            const int e = lane + 32 * j < it.z ? lane + 32 * j : lane;
+            c[j].start(P.ps + (size_t)(it.y + e) * 12);
+        }
+#pragma unroll 1
+        for (int i = 1; i <= steps; i++) {
+#pragma unroll
+            for (int j = 0; j < CPL; j++) c[j].step(i, dt, h);
+        }
+#pragma unroll
+        for (int j = 0; j < CPL; j++) {
+            if (lane + 32 * j >= it.z) continue;
+            const int cc = it.y + lane + 32 * j;
+            P.cres[cc] = c[j].best;
+            P.cres[P.n_clones + cc] = c[j].tbest;
+            P.cres[2 * (size_t)P.n_clones + cc] = c[j].vbest;
+        }
+    }
+}
+
+// before k_pair_mc_t: queue head zeroed, empty results for pairs without clones
+__global__ void k_mc_prep(const McPairs *__restrict__ Pd) {
+    const McPairs P = *Pd;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) *P.qhead = 0;
+    for (int p = t; p < P.n_pairs; p += gridDim.x * blockDim.x) {
+        if (P.clone_off[p + 1] - P.clone_off[p] > 0) continue;
+        PhResultDev o;
+        o.n = 0;
+        o.d05 = o.d50 = o.d95 = o.t05 = o.t50 = o.t95 = o.v05 = o.v50 = o.v95 = o.f_r50 = o.f_rtot = 0.0;
+        P.res[p] = o;
+    }
+}
+
+// after k_pair_mc_t: one warp per pair of 1 .. 1024 clones, over a fixed grid
+__global__ void __launch_bounds__(kMcThreads) k_pair_reduce_dev(const McPairs *__restrict__ Pd) {
+    __shared__ double smem[kMcThreads / 32][1024];
+    const McPairs P = *Pd;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int p = blockIdx.x * (kMcThreads / 32) + w; p < P.n_pairs; p += gridDim.x * (kMcThreads / 32)) {
+        const int m = P.clone_off[p + 1] - P.clone_off[p];
+        if (m > 0 && m <= 1024) reduce_dispatch(P, p, smem[w], lane);
+    }
+}
+
+namespace {
+struct McVariant {
+    int warps, cpl;
+    void (*fn)(const McPairs *);
+};
+const McVariant kMcVariants[] = {
+    {4, 1, k_pair_mc_t<4, 1>}, {2, 1, k_pair_mc_t<2, 1>}, {8, 1, k_pair_mc_t<8, 1>},
+    {4, 2, k_pair_mc_t<4, 2>}, {2, 2, k_pair_mc_t<2, 2>}, {8, 2, k_pair_mc_t<8, 2>},
+};
+}  // namespace
+
+int mc_variants() { return (int)(sizeof kMcVariants / sizeof kMcVariants[0]); }
+
+void mc_variant_shape(int v, int &warps, int &cpl) {
+    warps = kMcVariants[v].warps;
+    cpl = kMcVariants[v].cpl;
+}
+
+// resident blocks of variant v for a full persistent grid (blocks per SM x SMs)
+cudaError_t mc_variant_grid(int v, int sms, int &grid) {
+    int per_sm = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, reinterpret_cast<const void *>(kMcVariants[v].fn), kMcVariants[v].warps * 32, 0);
+    grid = sms * (per_sm > 0 ? per_sm : 1);
+    return e;
+}
+
+// prep, trace (variant v on a persistent grid) and reduce on one stream; reduce_grid blocks of kMcThreads
+cudaError_t launch_mc(int v, int grid, int prep_grid, int reduce_grid, cudaStream_t st, const McPairs *Pd) {
+    k_mc_prep<<<prep_grid, 256, 0, st>>>(Pd);
+    kMcVariants[v].fn<<<grid, kMcVariants[v].warps * 32, 0, st>>>(Pd);
+    k_pair_reduce_dev<<<reduce_grid, kMcThreads, 0, st>>>(Pd);
+    return cudaGetLastError();
 }
 
 // reduction alone, one warp per pair, for results traced elsewhere (the drop-in ph_pair_reduce)

@@ -549,3 +549,108 @@ void pgh_draw_pairs(int n_pairs, const PhTarget *const *t, const PhCluster *cons
     PairDrawArg A = {t, c, n_clones, dt_myr, seed, ps, m, steps, dt};
     pgh_parallel_for(n_pairs, threads, 4, pair_draw_range, &A);
 }
+
+/* ---- batched pair jobs: tracks + prefilter, and clone draws with a clone count per pair ------------------------ */
+typedef struct {
+    const PhCluster *c;
+    PhTrack *tr;
+} ClusterTrackArg;
+
+static void cluster_track_range(void *p, int i0, int i1) {
+    ClusterTrackArg *A = p;
+    for (int i = i0; i < i1; i++) ph_track_cluster(&A->c[i], 32, ph_seed("track", A->c[i].name), &A->tr[i]);
+}
+
+typedef struct {
+    const PhTarget *t;
+    const PhCluster *c;
+    const PhTrack *ctr;
+    int nc;
+    double tmax;
+    unsigned char *keep;      /* [nt][nc] */
+} PrefilterArg;
+
+static void prefilter_range(void *p, int j0, int j1) {
+    PrefilterArg *A = p;
+    for (int j = j0; j < j1; j++) {
+        PhTrack tt;
+        ph_track_target(&A->t[j], A->tmax, 32, ph_seed("track", A->t[j].id), &tt);
+        unsigned char *k = A->keep + (size_t)j * A->nc;
+        for (int i = 0; i < A->nc; i++) k[i] = (unsigned char)ph_prefilter(&tt, &A->ctr[i], &A->c[i]);
+        ph_track_free(&tt);
+    }
+}
+
+long pgh_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti, int *ci,
+                         long cap) {
+    if (nt <= 0 || nc <= 0) return 0;
+    double tmax = 0;
+    for (int i = 0; i < nc; i++) if (c[i].tmax_myr > tmax) tmax = c[i].tmax_myr;
+    PhTrack *ctr = malloc(sizeof(PhTrack) * (size_t)nc);
+    unsigned char *keep = malloc((size_t)nt * nc);
+    if (!ctr || !keep) { free(ctr); free(keep); return -1; }
+    ClusterTrackArg ca = {c, ctr};
+    pgh_parallel_for(nc, threads, 16, cluster_track_range, &ca);
+    PrefilterArg pa = {t, c, ctr, nc, tmax, keep};
+    pgh_parallel_for(nt, threads, 1, prefilter_range, &pa);
+    long n = 0;
+    for (int j = 0; j < nt; j++)
+        for (int i = 0; i < nc; i++) {
+            if (!keep[(size_t)j * nc + i]) continue;
+            if (n < cap) { ti[n] = j; ci[n] = i; }
+            n++;
+        }
+    for (int i = 0; i < nc; i++) ph_track_free(&ctr[i]);
+    free(ctr);
+    free(keep);
+    return n;
+}
+
+typedef struct {
+    const PhTarget *t;
+    const int *ti;
+    const PhCluster *c;
+    const int *ci;
+    const int *n_clones;
+    const long *slot;         /* first clone slot of pair q, before compaction */
+    double dt_myr;
+    double *ps;
+    int *m, *steps;
+    double *dt;
+} BatchDrawArg;
+
+static void batch_draw_range(void *p, int q0, int q1) {
+    BatchDrawArg *A = p;
+    for (int q = q0; q < q1; q++) {
+        const PhTarget *t = &A->t[A->ti[q]];
+        const PhCluster *c = &A->c[A->ci[q]];
+        A->m[q] = ph_pair_draw(t, c, A->n_clones[q], A->dt_myr, ph_seed(t->id, c->name), A->ps + 12 * A->slot[q],
+                               &A->steps[q], &A->dt[q]);
+    }
+}
+
+int pgh_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
+                        const int *n_clones, double dt_myr, int threads, int *clone_off, double *ps, int *steps,
+                        double *dt, double *r50_pc, double *rtot_pc) {
+    long *slot = malloc(sizeof(long) * (size_t)(n_pairs + 1));
+    int *m = malloc(sizeof(int) * (size_t)(n_pairs > 0 ? n_pairs : 1));
+    if (!slot || !m) { free(slot); free(m); return -1; }
+    slot[0] = 0;
+    for (int q = 0; q < n_pairs; q++) slot[q + 1] = slot[q] + (n_clones[q] > 0 ? n_clones[q] : 0);
+    BatchDrawArg A = {t, ti, c, ci, n_clones, slot, dt_myr, ps, m, steps, dt};
+    pgh_parallel_for(n_pairs, threads, 4, batch_draw_range, &A);
+    /* compact: the clones of pair q follow those of pair q - 1 (a pair keeps only its successful draws) */
+    long off = 0;
+    clone_off[0] = 0;
+    for (int q = 0; q < n_pairs; q++) {
+        if (off != slot[q] && m[q] > 0) memmove(ps + 12 * off, ps + 12 * slot[q], sizeof(double) * 12 * (size_t)m[q]);
+        off += m[q];
+        if (off > 2147483647L) { free(slot); free(m); return -2; }
+        clone_off[q + 1] = (int)off;
+        r50_pc[q] = c[ci[q]].r50_pc;
+        rtot_pc[q] = c[ci[q]].rtot_pc;
+    }
+    free(slot);
+    free(m);
+    return 0;
+}

@@ -24,6 +24,16 @@ void pgh_parallel_for(int n, int threads, int chunk, void (*fn)(void *, int, int
 /* ph_pair_draw for n_pairs pairs (clones of pair i at ps + 12 * n_clones * i; m, steps, dt per pair) */
 void pgh_draw_pairs(int n_pairs, const PhTarget *const *t, const PhCluster *const *c, int n_clones, double dt_myr,
                     const uint64_t *seed, int threads, double *ps, int *m, int *steps, double *dt);
+/* pairs (ti[k], ci[k]) of targets x clusters that pass ph_prefilter (tracks as phygas_cli builds them), in (target,
+ * cluster) order; writes at most cap pairs and returns how many pass (-1: out of memory) */
+long pgh_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti, int *ci,
+                         long cap);
+/* ph_pair_draw for pair q = (t[ti[q]], c[ci[q]]) with n_clones[q] clones, seeds ph_seed(id, name); the clones of all
+ * pairs written back to back into ps (room for 12 * sum(n_clones) doubles) with clone_off[n_pairs + 1]; steps, dt,
+ * r50_pc, rtot_pc per pair.  Returns 0, or -1 (out of memory), -2 (more than 2^31 - 1 clones) */
+int pgh_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
+                        const int *n_clones, double dt_myr, int threads, int *clone_off, double *ps, int *steps,
+                        double *dt, double *r50_pc, double *rtot_pc);
 
 #ifdef __cplusplus
 }

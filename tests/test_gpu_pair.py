@@ -133,3 +133,32 @@ def test_pulsar_profile_published_hash_via_cli(built, golden):
     if (ot.rows_hash(rows), len(rows)) != ot.PUBLISHED["pulsar"]:
         diff = [(a, b) for a, b in zip(rows, gold) if a != b][:5]
         pytest.fail("rows %d vs %d; first differences %r" % (len(rows), len(gold), diff))
+
+
+def test_every_launch_shape_gives_the_same_bits(ctx):
+    """The autotuner's launch shapes (warps per block x clones per lane) of the graph-captured clone kernel give
+    identical results on an uneven batch (clone counts 1..1000), the tuner keeps one shape, pgx_pair then reproduces
+    its results, and the clones match the oracle's."""
+    rng = np.random.default_rng(4)
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "pair64", 2, 1000)
+        targets, clusters = pg.read_targets(tp), pg.read_clusters(cp)
+        ti = np.repeat(np.arange(2), 20).astype(np.int32)
+        ci = rng.integers(0, len(clusters), 40).astype(np.int32)
+        ncl = rng.choice([1, 31, 33, 200, 500, 1000], 40).astype(np.int32)
+        ncl[7] = 500
+        batch = pg.draw_pair_batch(targets, ti, clusters, ci, ncl, 0.05)
+        checks = {q: ot.parse_pair_dump(ot.run([ot.ORACLE_DUMP, "pair", cp, tp, str(ti[q]), str(ci[q]),
+                                                str(ci[q] + 1), str(ncl[q]), "0.05"]))[0] for q in (0, 7, 39)}
+    best, table = ctx.tune_pair(*batch)
+    assert 0 <= best < len(table) and all(t > 0 for _, _, t in table)
+    res, clones = ctx.pair(*batch, want_clones=True)
+    again = ctx.pair(*batch)
+    assert res.tobytes() == again.tobytes()
+    off = batch[0]
+    for q, p in checks.items():
+        assert off[q + 1] - off[q] == p["m"]
+        ref = np.array(p["clones"])
+        got = clones[:, off[q]:off[q + 1]].T
+        assert np.all(np.abs(got - ref) <= ot.REL_TOL * np.abs(ref) + 1e-12), q
+    print("launch shapes:", table, "chosen", table[best][:2])

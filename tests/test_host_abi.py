@@ -206,3 +206,60 @@ def test_tracks_and_prefilter_identical(both, golden):
             dec.append(L.ph_prefilter(C.byref(x), C.byref(t), C.byref(c)))
         assert C.string_at(ct[0].pos, 24 * ct[0].n) == C.string_at(ct[1].pos, 24 * ct[1].n), i
         assert dec[0] == dec[1], i
+
+
+def test_prefilter_pairs_matches_the_oracle(both, golden):
+    """pgx_prefilter_pairs (threaded tracks + ph_prefilter) keeps exactly the pairs the oracle's tracks and prefilter
+    keep, in (target, cluster) order, for the reference's pulsar against 600 of the golden clusters."""
+    P, O = both
+
+    class Track(C.Structure):
+        _fields_ = [("n", C.c_int), ("pos", C.POINTER(C.c_double)), ("sig_pos", C.c_double),
+                    ("sig_vel", C.c_double)]
+
+    clusters = pg.read_clusters(golden["clusters"])[:600]
+    targets = pg.read_targets(golden["pulsar"])[:2]
+    ti, ci = pg.prefilter_pairs(targets, clusters)
+    O.ph_track_target.argtypes = [C.POINTER(pg.PhTarget), C.c_double, C.c_int, C.c_uint64, C.POINTER(Track)]
+    O.ph_track_cluster.argtypes = [C.POINTER(pg.PhCluster), C.c_int, C.c_uint64, C.POINTER(Track)]
+    O.ph_prefilter.argtypes = [C.POINTER(Track), C.POINTER(Track), C.POINTER(pg.PhCluster)]
+    O.ph_seed.restype = C.c_uint64
+    O.ph_seed.argtypes = [C.c_char_p, C.c_char_p]
+    tmax = max(c.tmax_myr for c in clusters)
+    cts = []
+    for c in clusters:
+        t = Track()
+        O.ph_track_cluster(C.byref(c), 32, O.ph_seed(b"track", c.name), C.byref(t))
+        cts.append(t)
+    want = []
+    for j, tg in enumerate(targets):
+        tt = Track()
+        O.ph_track_target(C.byref(tg), tmax, 32, O.ph_seed(b"track", tg.id), C.byref(tt))
+        want += [(j, i) for i, c in enumerate(clusters) if O.ph_prefilter(C.byref(tt), C.byref(cts[i]), C.byref(c))]
+    assert list(zip(ti.tolist(), ci.tolist())) == want
+    assert 0 < len(want) < 1200
+
+
+def test_draw_pair_batch_matches_ph_pair_draw(both, golden):
+    """pgx_draw_pair_batch: every pair's clones, steps and dt bit-identical to the oracle's ph_pair_draw with the
+    pair's own clone count, packed back to back."""
+    P, O = both
+    clusters = pg.read_clusters(golden["clusters"])
+    targets = list(pg.read_targets(golden["pulsar"])[:1]) + list(pg.read_targets(golden["screen"])[:3])
+    rng = np.random.default_rng(2)
+    ti = rng.integers(0, len(targets), 40).astype(np.int32)
+    ci = rng.integers(0, len(clusters), 40).astype(np.int32)
+    ncl = rng.choice([0, 1, 7, 33, 200], 40).astype(np.int32)
+    off, ps, steps, dt, r50, rt = pg.draw_pair_batch(targets, ti, clusters, ci, ncl, 0.05)
+    O.ph_pair_draw.argtypes = [C.POINTER(pg.PhTarget), C.POINTER(pg.PhCluster), C.c_int, C.c_double, C.c_uint64,
+                               C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    O.ph_seed.restype = C.c_uint64
+    O.ph_seed.argtypes = [C.c_char_p, C.c_char_p]
+    for q in range(40):
+        t, c = targets[ti[q]], clusters[ci[q]]
+        buf, st, d = np.zeros(12 * max(int(ncl[q]), 1)), C.c_int(), C.c_double()
+        m = O.ph_pair_draw(C.byref(t), C.byref(c), int(ncl[q]), 0.05, O.ph_seed(t.id, c.name), pg._ptr(buf),
+                           C.byref(st), C.byref(d))
+        assert off[q + 1] - off[q] == m, q
+        assert ps[12 * off[q]:12 * off[q + 1]].tobytes() == buf[:12 * m].tobytes(), q
+        assert (steps[q], dt[q], r50[q], rt[q]) == (st.value, d.value, c.r50_pc, c.rtot_pc), q

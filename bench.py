@@ -228,6 +228,39 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu):
     return out
 
 
+# Serving (the benchmark spec's C4 shape): SERVE_JOBS jobs of a seeded Poisson stream at SERVE_RATE_HZ through the
+# request loop with SERVE_SLOTS slots -- screen and control chunks of 1,000-20,000 of the benchmark stars and
+# single-pulsar Monte Carlo jobs (4,087 clusters with the prefilter, 1000 clones) -- once with the mixed screen and
+# once with the plain FP64 screen, the same stream both times.
+SERVE_JOBS, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 20, 1.0, 3, 1004
+
+
+def serving_measure(cp, tp):
+    import phygas_gb300 as pg
+    from phygas_gb300 import synth
+    pp = os.path.join(tempfile.mkdtemp(prefix="phygas_serve_"), "pulsars.txt")
+    with open(pp, "w") as f:
+        f.write("\n".join(synth.pulsars(64, SERVE_SEED)) + "\n")
+    out = {"workload": "%d jobs, Poisson %.2f/s (seed %d): 40 %% screen, 20 %% control chunks of 1,000-20,000 stars, "
+                       "40 %% single-pulsar jobs (prefilter, 1000 clones); %d slots"
+                       % (SERVE_JOBS, SERVE_RATE_HZ, SERVE_SEED, SERVE_SLOTS)}
+    for prec in ("mixed", "fp64"):
+        r = subprocess.run([pg.SERVE_CLI, cp, tp, pp, str(SERVE_JOBS), str(SERVE_RATE_HZ), str(SERVE_SLOTS), prec,
+                            str(SERVE_SEED)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+        lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
+        summ = [x for x in lines if x.get("summary")]
+        jobs = [x for x in lines if not x.get("summary")]
+        if r.returncode or not summ:
+            raise RuntimeError("phygas_serve %s failed: %s" % (prec, r.stderr[-400:]))
+        s = dict(summ[0])
+        s.pop("summary")
+        s["latency_by_kind_p50_s"] = {k: statistics.median([x["latency_s"] for x in jobs if x["kind"] == k] or [0.0])
+                                      for k in ("screen", "control", "pulsar")}
+        s["jobs_by_kind"] = {k: sum(1 for x in jobs if x["kind"] == k) for k in ("screen", "control", "pulsar")}
+        out[prec] = s
+    return out
+
+
 def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -268,6 +301,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-pair", action="store_true", help="skip the batched Monte Carlo measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -355,6 +389,13 @@ def main():
         except Exception as e:          # reported beside the headline, not part of it
             log("pair Monte Carlo measurement failed: %s" % e)
 
+    serving = None
+    if rank == 0 and not args.no_serve:
+        try:
+            serving = serving_measure(cp, tp)
+        except Exception as e:          # reported beside the headline, not part of it
+            log("serving measurement failed: %s" % e)
+
     s = stats[-1]
     orbit_ms = statistics.mean(x["ms_orbit"] for x in stats)
     achieved = FLOPS_PER_BODY_STEP * s["body_steps"] / (orbit_ms * 1e-3)
@@ -393,6 +434,7 @@ def main():
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "pair_mc": pair_mc,
+            "serving": serving,
         }
         print(json.dumps(out))
     ctx.close()

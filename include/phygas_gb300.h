@@ -27,6 +27,7 @@ extern "C" {
 #define PGX_E_TIMEOUT 4    /* a bounded device-side wait ran out */
 #define PGX_E_LIMIT 5      /* beyond a documented size limit */
 #define PGX_E_NODEV 6      /* no usable GPU */
+#define PGX_E_PENDING 7    /* pgx_server_query: the job has not finished */
 
 #define PGX_FP64 0         /* the plain FP64 screen */
 #define PGX_MIXED 1        /* FP32 screen with FP64 rechecks (identical rows) */
@@ -90,6 +91,9 @@ uint64_t pgx_seed_prefix(const char *target_id);
  * pgx_draw_pair_batch -- ph_pair_draw for pair q = (t[ti[q]], c[ci[q]]) with its own clone count n_clones[q] and the
  *   pair's seed ph_seed(id, name): the clones of all pairs back to back in ps (room for 12 * sum(n_clones) doubles),
  *   clone_off[n_pairs + 1], and per pair steps, dt, r50_pc, rtot_pc -- the arguments of pgx_pair. */
+/* The screen's chance-alignment control (reference src/phygas_screen.c:35-47): out[j] = t[j] with the proper motions
+ * (rescaled by the parallax ratio) and the radial velocity of t[(j + n/2) % n]; out must not alias t. */
+int pgx_control_targets(const PhTarget *t, int n, PhTarget *out);
 int pgx_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti, int *ci,
                         long cap, long *n);
 int pgx_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
@@ -159,6 +163,59 @@ int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S,
  * seeds, ratio[i] = the largest |x_j - x_j,64| / bound over the pair's 512 draws and three components, where x is
  * the FP32 draw, x_64 the FP64 path's and bound the FP32 draw's own error bound: <= 1 when the bound holds. */
 int pgx_check_draws(PgxContext *ctx, int n, const double *fin11, const uint64_t *seed, double *ratio);
+
+/* ---- serving ---------------------------------------------------------------------------------------------------- */
+/* A request loop in front of the GPU (no counterpart in the reference, whose BOINC app runs one work unit at a time).
+ * pgx_server_open creates `slots` device contexts, each with its own stream and its own resident copy of the cluster
+ * table (clusters c, drawn once on the host with n_samp draws, kernel radius r_kernel as ph_screen_r).  Submitted
+ * jobs queue in arrival order; a job starts when a slot is idle and the estimated device memory of the running jobs
+ * plus its own stays within hbm_budget_gb (the first job of an idle GPU always starts).  Slots run their jobs' host
+ * parts (draws, prefilter) on host_threads / slots cores (host_threads <= 0: all cores) while other slots' kernels run,
+ * so jobs arriving while others are on the GPU are admitted as slots and memory free up and their work overlaps on the
+ * device.  A job's results depend only on its inputs: the same bits alone and in any mix.
+ * Kinds: PGX_JOB_SCREEN screens n_targets stars against the table (rows with p_r50 >= p_min kept, as the BOINC app's
+ * emit cut); PGX_JOB_CONTROL the same on the velocity-shuffled chunk (pgx_control_targets); PGX_JOB_PAIRS runs the
+ * pair Monte Carlo of n_targets targets against their prefiltered clusters (pgx_prefilter_pairs) with n_clones clones
+ * at dt_myr.  Times are seconds since pgx_server_open; digest = FNV-1a 64 of the job's result records. */
+#define PGX_JOB_SCREEN 0
+#define PGX_JOB_CONTROL 1
+#define PGX_JOB_PAIRS 2
+typedef struct PgxServer PgxServer;
+typedef struct {
+    int kind;                 /* PGX_JOB_* */
+    int precision;            /* screen and control: PGX_MIXED or PGX_FP64 */
+    const PhTarget *targets;  /* copied by pgx_server_submit */
+    int n_targets;
+    double chi2_max;          /* screen and control */
+    double p_min;             /* screen and control: keep rows with p_r50 >= p_min */
+    int n_clones;             /* pairs */
+    double dt_myr;            /* pairs */
+} PgxJob;
+typedef struct {
+    int status;               /* PGX_OK or the job's error code (-1 while it runs) */
+    int kind, slot;
+    double t_submit, t_start, t_end;
+    long n_out;               /* screen rows kept, or pairs traced */
+    double work;              /* star-cluster pairs screened, or clone-steps */
+    uint64_t digest;
+} PgxJobResult;
+typedef struct {
+    long submitted, finished, queued;
+    int running, max_running, slots;
+    double hbm_budget_gb, hbm_in_use_gb, hbm_peak_gb, now_s;
+} PgxServerStats;
+int pgx_server_open(int device, int slots, double hbm_budget_gb, const PhCluster *c, int nc, int n_samp,
+                    double r_kernel, int host_threads, PgxServer **out);
+int pgx_server_submit(PgxServer *s, const PgxJob *job, long *id);
+int pgx_server_wait(PgxServer *s, long id, PgxJobResult *out);     /* blocks until the job has finished */
+int pgx_server_query(PgxServer *s, long id, PgxJobResult *out);    /* PGX_E_PENDING until then */
+/* a finished job's results (cap records at most; returns the count, -1 if unknown or unfinished):
+ * screen and control rows, or the pair jobs' PhResult with each pair's cluster index */
+long pgx_server_rows(PgxServer *s, long id, PgxScreenRow *rows, long cap);
+long pgx_server_pairs(PgxServer *s, long id, PhResult *res, int *cluster, long cap);
+void pgx_server_release(PgxServer *s, long id);                    /* forget a finished job */
+int pgx_server_stats(PgxServer *s, PgxServerStats *out);
+void pgx_server_close(PgxServer *s);                               /* finishes the queued jobs first */
 
 #ifdef __cplusplus
 }

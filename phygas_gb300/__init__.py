@@ -14,10 +14,11 @@ LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libphygas_gb300.so")
 SCREEN_CLI = os.path.join(LIB_DIR, "phygas_screen")
 PAIR_CLI = os.path.join(LIB_DIR, "phygas_cli")
+SERVE_CLI = os.path.join(LIB_DIR, "phygas_serve")
 
 PGX_FP64, PGX_MIXED = 0, 1
 ERRORS = {1: "bad argument", 2: "CUDA error", 3: "out of device memory", 4: "device wait timed out",
-          5: "size limit", 6: "no usable GPU"}
+          5: "size limit", 6: "no usable GPU", 7: "job still running"}
 
 
 class PhCluster(C.Structure):
@@ -65,6 +66,25 @@ _D = _P(C.c_double)
 _I = _P(C.c_int)
 _U64 = _P(C.c_uint64)
 
+class PgxJob(C.Structure):
+    _fields_ = [("kind", C.c_int), ("precision", C.c_int), ("targets", C.c_void_p), ("n_targets", C.c_int),
+                ("chi2_max", C.c_double), ("p_min", C.c_double), ("n_clones", C.c_int), ("dt_myr", C.c_double)]
+
+
+class PgxJobResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("kind", C.c_int), ("slot", C.c_int), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_end", C.c_double), ("n_out", C.c_long), ("work", C.c_double),
+                ("digest", C.c_uint64)]
+
+
+class PgxServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_long), ("finished", C.c_long), ("queued", C.c_long), ("running", C.c_int),
+                ("max_running", C.c_int), ("slots", C.c_int), ("hbm_budget_gb", C.c_double),
+                ("hbm_in_use_gb", C.c_double), ("hbm_peak_gb", C.c_double), ("now_s", C.c_double)]
+
+
+PGX_JOB_SCREEN, PGX_JOB_CONTROL, PGX_JOB_PAIRS = 0, 1, 2
+
 # (name, restype, argtypes) of every C-ABI entry point bound here
 SIGNATURES = [
     ("pgx_open", C.c_int, [C.c_int, _P(C.c_void_p)]),
@@ -93,6 +113,17 @@ SIGNATURES = [
     ("pgx_check_bounds", C.c_int, [C.c_void_p, C.c_int, _D, _D, _D, C.c_double, _D, _P(C.c_float),
                                    _P(C.c_float), _I]),
     ("pgx_check_draws", C.c_int, [C.c_void_p, C.c_int, _D, _P(C.c_uint64), _D]),
+    ("pgx_control_targets", C.c_int, [_P(PhTarget), C.c_int, _P(PhTarget)]),
+    ("pgx_server_open", C.c_int, [C.c_int, C.c_int, C.c_double, _P(PhCluster), C.c_int, C.c_int, C.c_double, C.c_int,
+                                  _P(C.c_void_p)]),
+    ("pgx_server_submit", C.c_int, [C.c_void_p, _P(PgxJob), _P(C.c_long)]),
+    ("pgx_server_wait", C.c_int, [C.c_void_p, C.c_long, _P(PgxJobResult)]),
+    ("pgx_server_query", C.c_int, [C.c_void_p, C.c_long, _P(PgxJobResult)]),
+    ("pgx_server_rows", C.c_long, [C.c_void_p, C.c_long, C.c_void_p, C.c_long]),
+    ("pgx_server_pairs", C.c_long, [C.c_void_p, C.c_long, C.c_void_p, _I, C.c_long]),
+    ("pgx_server_release", None, [C.c_void_p, C.c_long]),
+    ("pgx_server_stats", C.c_int, [C.c_void_p, _P(PgxServerStats)]),
+    ("pgx_server_close", None, [C.c_void_p]),
     ("ph_init", None, []),
     ("ph_seed", C.c_uint64, [C.c_char_p, C.c_char_p]),
     ("ph_read_clusters", C.c_int, [C.c_char_p, _P(_P(PhCluster))]),
@@ -314,6 +345,68 @@ def pair_shapes():
     w, c = np.zeros(n, np.int32), np.zeros(n, np.int32)
     lib().pgx_pair_shapes(n, _ptr(w, C.c_int), _ptr(c, C.c_int))
     return list(zip(w.tolist(), c.tolist()))
+
+
+class Server:
+    """The request loop (pgx_server_*): slots device contexts with the cluster table resident, jobs admitted in
+    arrival order as slots and the device-memory budget allow."""
+
+    def __init__(self, clusters, slots=3, hbm_budget_gb=80.0, device=0, n_samp=64, r_kernel=2.0, host_threads=0):
+        self._clusters = as_array(clusters, PhCluster)
+        h = C.c_void_p()
+        rc = lib().pgx_server_open(device, slots, hbm_budget_gb, self._clusters, len(self._clusters), n_samp,
+                                   r_kernel, host_threads, C.byref(h))
+        if rc:
+            raise GpuError("pgx_server_open: %s" % ERRORS.get(rc, rc))
+        self.h = h
+        self._keep = {}
+
+    def submit(self, kind, targets, precision=PGX_MIXED, chi2_max=25.0, p_min=0.001, n_clones=1000, dt_myr=0.05):
+        t = as_array(targets, PhTarget)
+        j = PgxJob(kind, precision, C.cast(t, C.c_void_p), len(t), chi2_max, p_min, n_clones, dt_myr)
+        jid = C.c_long()
+        rc = lib().pgx_server_submit(self.h, C.byref(j), C.byref(jid))
+        if rc:
+            raise GpuError("pgx_server_submit: %s" % ERRORS.get(rc, rc))
+        return jid.value
+
+    def wait(self, jid):
+        r = PgxJobResult()
+        lib().pgx_server_wait(self.h, jid, C.byref(r))
+        return {k: getattr(r, k) for k, _ in PgxJobResult._fields_}
+
+    def rows(self, jid):
+        n = lib().pgx_server_rows(self.h, jid, None, 0)
+        out = np.zeros(max(n, 0), ROW_DTYPE)
+        if n > 0:
+            lib().pgx_server_rows(self.h, jid, out.ctypes.data, n)
+        return out
+
+    def pairs(self, jid):
+        n = lib().pgx_server_pairs(self.h, jid, None, None, 0)
+        res, cl = np.zeros(max(n, 0), RESULT_DTYPE), np.zeros(max(n, 0), np.int32)
+        if n > 0:
+            lib().pgx_server_pairs(self.h, jid, res.ctypes.data, _ptr(cl, C.c_int), n)
+        return res, cl
+
+    def release(self, jid):
+        lib().pgx_server_release(self.h, jid)
+
+    def stats(self):
+        s = PgxServerStats()
+        lib().pgx_server_stats(self.h, C.byref(s))
+        return {k: getattr(s, k) for k, _ in PgxServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            lib().pgx_server_close(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def prefilter_pairs(targets, clusters, threads=0):

@@ -1,7 +1,7 @@
 """In-tree build of libphygas_gb300 and its two CLIs (nvcc + gcc, sm_103a only, no cmake).
 
 Outputs go to phygas_gb300/_lib/: libphygas_gb300.so (CUDA kernels + C host code, static cudart), phygas_screen,
-phygas_cli.  Objects are rebuilt only when a source or header is newer; compiles run in parallel.
+phygas_cli, phygas_serve.  Objects are rebuilt only when a source or header is newer; compiles run in parallel.
 
     python -m phygas_gb300.build            (or __graft_entry__.build())
 """
@@ -81,7 +81,8 @@ def build(verbose=False, jobs=None):
     so = os.path.join(LIB, "libphygas_gb300.so")
     if _stale(so, objs):
         _run([nvcc()] + ARCH + ["-shared", "-o", so] + objs + ["-lpthread"])
-    for name, src in (("phygas_screen", "phygas_screen_main.c"), ("phygas_cli", "phygas_cli_main.c")):
+    for name, src in (("phygas_screen", "phygas_screen_main.c"), ("phygas_cli", "phygas_cli_main.c"),
+                      ("phygas_serve", "phygas_serve_main.c")):
         exe = os.path.join(LIB, name)
         s = os.path.join(CSRC, "host", src)
         if _stale(exe, [s, so] + hdrs):

@@ -229,6 +229,12 @@ int pgx_draw_clusters(const PhCluster *c, int n, int n_samp, int threads, double
     return 0;
 }
 
+int pgx_control_targets(const PhTarget *t, int n, PhTarget *out) {
+    if (n < 0 || (n > 0 && (!t || !out)) || (n > 0 && t == out)) return PGX_E_ARG;
+    pgh_control_targets(t, n, out);
+    return 0;
+}
+
 int pgx_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti, int *ci,
                         long cap, long *n) {
     if (nt < 0 || nc < 0 || cap < 0 || !n || (nt > 0 && !t) || (nc > 0 && !c) || (cap > 0 && (!ti || !ci)))

@@ -147,7 +147,9 @@ void ph_init(void) {
     g_ready = 1;
 }
 const Potential *ph_potential(void) { return &g_pot; }
-static void ensure_init(void) { if (!g_ready) ph_init(); }
+static pthread_once_t g_once = PTHREAD_ONCE_INIT;
+static void init_once(void) { ph_init(); }
+static void ensure_init(void) { if (!g_ready) pthread_once(&g_once, init_once); }
 
 static double rv_rotation(V3 q) {           /* RV of a circular orbit at q, seen from the Sun (reference :23-35) */
     double R = hypot(q.x, q.y);
@@ -653,4 +655,17 @@ int pgh_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhC
     free(slot);
     free(m);
     return 0;
+}
+
+/* the chance-alignment control of the screen (reference phygas_screen.c:35-47): star j takes the proper motions of
+ * the star n/2 further on (cyclically), rescaled by the parallax ratio, and its radial velocity */
+void pgh_control_targets(const PhTarget *t, int n, PhTarget *out) {
+    for (int j = 0; j < n; j++) {
+        out[j] = t[j];
+        const PhTarget *o = &t[(j + n / 2) % n];
+        double f = (t[j].plx > 0 && o->plx > 0) ? t[j].plx / o->plx : 1.0;
+        out[j].pmra = o->pmra * f; out[j].e_pmra = o->e_pmra * f;
+        out[j].pmdec = o->pmdec * f; out[j].e_pmdec = o->e_pmdec * f;
+        out[j].rv = o->rv; out[j].e_rv = o->e_rv; out[j].has_rv = o->has_rv;
+    }
 }

@@ -31,6 +31,9 @@ long pgh_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, 
 /* ph_pair_draw for pair q = (t[ti[q]], c[ci[q]]) with n_clones[q] clones, seeds ph_seed(id, name); the clones of all
  * pairs written back to back into ps (room for 12 * sum(n_clones) doubles) with clone_off[n_pairs + 1]; steps, dt,
  * r50_pc, rtot_pc per pair.  Returns 0, or -1 (out of memory), -2 (more than 2^31 - 1 clones) */
+/* the screen's chance-alignment control: velocities of the star n/2 further on, proper motions rescaled by the
+ * parallax ratio (out may not alias t) */
+void pgh_control_targets(const PhTarget *t, int n, PhTarget *out);
 int pgh_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
                         const int *n_clones, double dt_myr, int threads, int *clone_off, double *ps, int *steps,
                         double *dt, double *r50_pc, double *rtot_pc);

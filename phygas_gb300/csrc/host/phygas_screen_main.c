@@ -63,14 +63,7 @@ int main(int argc, char **argv) {
     fprintf(stderr, "%d clusters prepared in %.1f s; %d targets\n", nc, now_s() - t0, nt);
     if (control) {   /* velocities of the star nt/2 away, proper motions rescaled by the parallax ratio */
         PhTarget *v = malloc(sizeof(PhTarget) * nt);
-        for (int j = 0; j < nt; j++) {
-            v[j] = tg[j];
-            const PhTarget *o = &tg[(j + nt / 2) % nt];
-            double f = (tg[j].plx > 0 && o->plx > 0) ? tg[j].plx / o->plx : 1.0;
-            v[j].pmra = o->pmra * f; v[j].e_pmra = o->e_pmra * f;
-            v[j].pmdec = o->pmdec * f; v[j].e_pmdec = o->e_pmdec * f;
-            v[j].rv = o->rv; v[j].e_rv = o->e_rv; v[j].has_rv = o->has_rv;
-        }
+        pgx_control_targets(tg, nt, v);
         free(tg);
         tg = v;
         fprintf(stderr, "control run: velocities taken from the star %d lines away\n", nt / 2);

@@ -263,3 +263,27 @@ def test_draw_pair_batch_matches_ph_pair_draw(both, golden):
         assert off[q + 1] - off[q] == m, q
         assert ps[12 * off[q]:12 * off[q + 1]].tobytes() == buf[:12 * m].tobytes(), q
         assert (steps[q], dt[q], r50[q], rt[q]) == (st.value, d.value, c.r50_pc, c.rtot_pc), q
+
+
+def test_serving_stream_plan(built, golden):
+    """phygas_serve's seeded Poisson stream (its `plan` mode needs no GPU): the same seed gives the same stream,
+    inter-arrival times average 1/rate, chunk sizes stay in 1,000..20,000 stars (at most the file), and the job kinds
+    come in about 40 / 20 / 40 % (screen / control / pulsar)."""
+    import json
+    args = [pg.SERVE_CLI, golden["clusters"], golden["screen"], golden["pulsar"], "3000", "2.0", "3", "mixed", "77",
+            "plan"]
+    a = subprocess.run(args, stdout=subprocess.PIPE, check=True, text=True).stdout
+    b = subprocess.run(args, stdout=subprocess.PIPE, check=True, text=True).stdout
+    assert a == b
+    jobs = [json.loads(x) for x in a.splitlines()]
+    t = np.array([j["arrive_s"] for j in jobs])
+    assert np.all(np.diff(t) > 0) and abs(np.mean(np.diff(t)) - 0.5) < 0.05
+    kinds = [j["kind"] for j in jobs]
+    frac = {k: kinds.count(k) / len(kinds) for k in ("screen", "control", "pulsar")}
+    assert abs(frac["screen"] - 0.4) < 0.04 and abs(frac["control"] - 0.2) < 0.04 and abs(frac["pulsar"] - 0.4) < 0.04
+    n_stars = len(pg.read_targets(golden["screen"]))
+    for j in jobs:
+        if j["kind"] == "pulsar":
+            assert j["n"] == 1
+        else:
+            assert min(1000, n_stars) <= j["n"] <= min(20000, n_stars) and j["first"] + j["n"] <= n_stars

@@ -75,6 +75,13 @@ int pgx_screen(PgxContext *ctx, int nt, const double *ps0, const double *sig, co
 int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *seed_prefix);
 int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double chi2_max, int precision, long *n_rows);
 int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n);
+/* pgx_screen writing into the caller's rows[cap] (no allocation); *n_rows = the kept pairs, PGX_E_LIMIT (rows kept on
+ * the device for pgx_screen_fetch) when more than cap.  With rows from pgx_host_alloc the copy runs at the link's
+ * full rate: page-locked host memory, allocated once and freed with pgx_host_free. */
+int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *prefix,
+                    double tmax, double chi2_max, int precision, PgxScreenRow *rows, long cap, long *n_rows);
+void *pgx_host_alloc(size_t bytes);
+void pgx_host_free(void *p);
 
 /* Host draws for the records API (reference ph_lin_target_init / the draws of ph_lin_cluster, src/phygas.c:274-344,
  * seeds ph_seed("lin", id)), on `threads` host threads (<= 0: all cores). */

@@ -98,6 +98,10 @@ SIGNATURES = [
     ("pgx_screen_stage", C.c_int, [C.c_void_p, C.c_int, _D, _D, _U64]),
     ("pgx_screen_exec", C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int, _P(C.c_long)]),
     ("pgx_screen_fetch", C.c_int, [C.c_void_p, C.c_void_p, C.c_long]),
+    ("pgx_screen_into", C.c_int, [C.c_void_p, C.c_int, _D, _D, _U64, C.c_double, C.c_double, C.c_int, C.c_void_p,
+                                  C.c_long, _P(C.c_long)]),
+    ("pgx_host_alloc", C.c_void_p, [C.c_size_t]),
+    ("pgx_host_free", None, [C.c_void_p]),
     ("pgx_draw_targets", C.c_int, [_P(PhTarget), C.c_int, C.c_int, C.c_int, _D, _D, _U64]),
     ("pgx_draw_clusters", C.c_int, [_P(PhCluster), C.c_int, C.c_int, C.c_int, _D, _D]),
     ("pgx_seed_prefix", C.c_uint64, [C.c_char_p]),
@@ -294,6 +298,19 @@ class Context:
         lib().pgx_free(rows)
         return out
 
+    def screen_into(self, ps0, sig, prefix, tmax, out, chi2_max=25.0, precision=PGX_MIXED):
+        """pgx_screen_into: the rows written into `out` (a HostRows buffer, or any ROW_DTYPE array); returns the
+        filled part.  Grows nothing: raises if `out` is too small."""
+        n = C.c_long()
+        ps0 = np.ascontiguousarray(ps0, np.float64)
+        sig = np.ascontiguousarray(sig, np.float64)
+        prefix = np.ascontiguousarray(prefix, np.uint64)
+        arr = out.rows if isinstance(out, HostRows) else out
+        self._check(lib().pgx_screen_into(self.h, len(prefix), _ptr(ps0), _ptr(sig), _ptr(prefix, C.c_uint64), tmax,
+                                          chi2_max, precision, arr.ctypes.data, len(arr), C.byref(n)),
+                    "pgx_screen_into")
+        return arr[:n.value]
+
     def stage(self, ps0, sig, prefix):
         self._keep = (np.ascontiguousarray(ps0, np.float64), np.ascontiguousarray(sig, np.float64),
                       np.ascontiguousarray(prefix, np.uint64))
@@ -345,6 +362,31 @@ def pair_shapes():
     w, c = np.zeros(n, np.int32), np.zeros(n, np.int32)
     lib().pgx_pair_shapes(n, _ptr(w, C.c_int), _ptr(c, C.c_int))
     return list(zip(w.tolist(), c.tolist()))
+
+
+class HostRows:
+    """Page-locked host memory for n screen rows (pgx_host_alloc), reused across calls: the device-to-host copy of
+    a chunk's rows runs at the link's rate instead of through pageable staging."""
+
+    def __init__(self, n):
+        self.n = int(n)
+        self._p = lib().pgx_host_alloc(self.n * ROW_DTYPE.itemsize)
+        if not self._p:
+            raise MemoryError("pgx_host_alloc(%d rows)" % self.n)
+        buf = (C.c_char * (self.n * ROW_DTYPE.itemsize)).from_address(self._p)
+        self.rows = np.frombuffer(buf, ROW_DTYPE, self.n)
+
+    def close(self):
+        if self._p:
+            self.rows = None
+            lib().pgx_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Server:

@@ -570,6 +570,29 @@ int pgx_screen(PgxContext *ctx, int nt, const double *ps0, const double *sig, co
     return 0;
 }
 
+int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *prefix,
+                    double tmax, double cut, int precision, PgxScreenRow *rows, long cap, long *n_rows) {
+    if (!ctx) return PGX_E_ARG;
+    if (!n_rows || cap < 0 || (cap > 0 && !rows)) return fail(ctx, PGX_E_ARG, "pgx_screen_into: bad args");
+    *n_rows = 0;
+    RET(pgx_screen_stage(ctx, nt, ps0, sig, prefix));
+    long n = 0;
+    RET(pgx_screen_exec(ctx, tmax, cut, precision, &n));
+    *n_rows = n;
+    if (n > cap) return fail(ctx, PGX_E_LIMIT, "pgx_screen_into: %ld rows, room for %ld", n, cap);
+    return pgx_screen_fetch(ctx, rows, n);
+}
+
+void *pgx_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void pgx_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
 namespace {
 // the captured prep + trace + reduce sequence of clone-kernel variant v (parameters read from ctx->p_params)
 int mc_graph(PgxContext *ctx, int v, cudaGraphExec_t &exec) {

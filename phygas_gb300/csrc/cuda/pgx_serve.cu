@@ -32,6 +32,11 @@ uint64_t fnv(uint64_t h, const void *p, size_t n) {
     return h;
 }
 
+struct HostBuf {
+    void *p = nullptr;
+    long cap = 0;
+};
+
 struct Job {
     long id = 0;
     PgxJob spec = {};
@@ -52,6 +57,7 @@ struct PgxServer {
     double r_kernel = 2.0, tmax = 0.0;
     std::vector<PhCluster> clusters;
     std::vector<PgxContext *> ctx;
+    std::vector<HostBuf> rows_buf;             // per slot: page-locked row buffer
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<long> queue;
@@ -75,7 +81,7 @@ size_t footprint(const PgxServer &s, const PgxJob &j) {
     return (size_t)j.n_targets * (70000 + 40 * nc) + (64u << 20);
 }
 
-int run_screen(PgxServer &s, PgxContext *ctx, Job &job) {
+int run_screen(PgxServer &s, int slot, PgxContext *ctx, Job &job) {
     const PgxJob &j = job.spec;
     const int n = j.n_targets;
     std::vector<PhTarget> ctl;
@@ -88,13 +94,22 @@ int run_screen(PgxServer &s, PgxContext *ctx, Job &job) {
     std::vector<double> ps0((size_t)6 * n), sig((size_t)36 * n);
     std::vector<uint64_t> pre(n);
     pgh_draw_targets(t, n, s.n_samp, s.host_threads, ps0.data(), sig.data(), pre.data());
-    PgxScreenRow *rows = nullptr;
+    // rows into the slot's page-locked buffer (grown when a chunk keeps more pairs than it holds)
+    HostBuf &hb = s.rows_buf[slot];
     long nr = 0;
-    const int rc = pgx_screen(ctx, n, ps0.data(), sig.data(), pre.data(), s.tmax, j.chi2_max, j.precision, &rows, &nr);
+    int rc = pgx_screen_into(ctx, n, ps0.data(), sig.data(), pre.data(), s.tmax, j.chi2_max, j.precision,
+                             (PgxScreenRow *)hb.p, hb.cap, &nr);
+    if (rc == PGX_E_LIMIT) {
+        pgx_host_free(hb.p);
+        hb.cap = nr + nr / 4 + 4096;
+        hb.p = pgx_host_alloc(sizeof(PgxScreenRow) * (size_t)hb.cap);
+        if (!hb.p) { hb.cap = 0; return PGX_E_NOMEM; }
+        rc = pgx_screen_fetch(ctx, (PgxScreenRow *)hb.p, nr);
+    }
     if (rc) return rc;
+    const PgxScreenRow *rows = (const PgxScreenRow *)hb.p;
     for (long h = 0; h < nr; h++)
         if (rows[h].p_r50 >= j.p_min) job.rows.push_back(rows[h]);
-    pgx_free(rows);
     job.out.n_out = (long)job.rows.size();
     job.out.work = (double)n * (double)s.clusters.size();
     job.out.digest = fnv(1469598103934665603ULL, job.rows.data(), job.rows.size() * sizeof(PgxScreenRow));
@@ -152,7 +167,7 @@ void worker(PgxServer *s, int slot) {
             job->out.slot = slot;
         }
         const int rc = job->spec.kind == PGX_JOB_PAIRS ? run_pairs(*s, s->ctx[slot], *job)
-                                                       : run_screen(*s, s->ctx[slot], *job);
+                                                       : run_screen(*s, slot, s->ctx[slot], *job);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             job->out.status = rc;
@@ -208,6 +223,7 @@ int pgx_server_open(int device, int slots, double hbm_budget_gb, const PhCluster
         }
     }
     s->device = device;
+    s->rows_buf.resize(slots);
     s->t0 = std::chrono::steady_clock::now();
     for (int k = 0; k < slots; k++) s->workers.emplace_back(worker, s.get(), k);
     *out = s.release();
@@ -319,6 +335,7 @@ void pgx_server_close(PgxServer *s) {
     }
     s->cv_work.notify_all();
     for (auto &t : s->workers) t.join();
+    for (auto &b : s->rows_buf) pgx_host_free(b.p);
     for (PgxContext *c : s->ctx) pgx_close(c);
     delete s;
 }

@@ -121,3 +121,21 @@ def test_screen_profile_published_hash(ctx, data, precision):
     if (ot.rows_hash(lines), len(lines)) != ot.PUBLISHED["screen"]:
         diff = [(a, b) for a, b in zip(lines, gold) if a != b][:5]
         pytest.fail("rows %d vs %d; first differences %r" % (len(lines), len(gold), diff))
+
+
+def test_screen_into_page_locked_rows(ctx, golden):
+    """pgx_screen_into writes the same rows as pgx_screen into a caller buffer (here page-locked, pgx_host_alloc);
+    a buffer too small gives PGX_E_LIMIT with the row count, and the rows stay on the device for pgx_screen_fetch."""
+    clusters, stars = pg.read_clusters(golden["clusters"]), pg.read_targets(golden["screen"])[:300]
+    ctx.set_clusters(clusters)
+    tmax = max(c.tmax_myr for c in clusters)
+    a, b, c = pg.draw_targets(stars)
+    want = ctx.screen(a, b, c, tmax)
+    buf = pg.HostRows(len(want) + 10)
+    got = ctx.screen_into(a, b, c, tmax, buf)
+    assert got.tobytes() == want.tobytes()
+    small = np.zeros(max(len(want) // 2, 1), pg.ROW_DTYPE)
+    with pytest.raises(pg.GpuError, match="size limit"):
+        ctx.screen_into(a, b, c, tmax, small)
+    assert ctx.fetch(len(want)).tobytes() == want.tobytes()
+    buf.close()

@@ -10,6 +10,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <cstddef>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -21,6 +22,7 @@
 #include "../host/ph_host.h"
 
 static_assert(sizeof(pgx::PhResultDev) == sizeof(PhResult), "PhResult layout");
+static_assert(offsetof(pgx::PhResultDev, d05) == offsetof(PhResult, d05), "PhResult layout");
 static_assert(sizeof(pgx::ScreenRowDev) == sizeof(PgxScreenRow), "PgxScreenRow layout");
 
 namespace {
@@ -177,6 +179,7 @@ int pgx_open(int device, PgxContext **out) {
         auto init = [&]() -> int {
             CK(cudaSetDevice(device));
             CK(cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device));
+            if (pgx::orbit_setup(device)) return fail(ctx, PGX_E_CUDA, "pgx_open: orbit force tables");
             CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
             for (auto &e : ctx->ev) CK(cudaEventCreate(&e));
             return 0;

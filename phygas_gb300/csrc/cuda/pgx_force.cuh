@@ -1,0 +1,95 @@
+// pgx_force.cuh -- the Allen & Santillan (1991) Milky Way force and the kick-drift-kick step, FP64 (internal header
+// of pgx_orbit.cu, which owns the halo power tables and fills them once per device).
+#pragma once
+#include "pgx_internal.cuh"
+
+namespace pgx {
+
+// x^(gamma - 1) of the halo term as x * x^a, a = (gamma - 1) - 1 = 0.02: x = 2^e m, m in [1, 2); m in sub-interval
+// j of 64 with centre c_j, m = c_j (1 + t), |t| <= 1/128; x^a = 2^(a e) c_j^a (1 + t)^a with the first two from
+// tables and (1 + t)^a by its binomial series to t^6 (the next term is below 5e-18 relative).  Ten FP64 operations
+// and a few integer ones, in place of a log and an exp (about 50 FP64-pipe slots on this GPU), and closer: each table
+// entry and the series are within a few ulp, where exp(a' ln x) inherits the log's absolute error times |a' ln x|.
+constexpr int kPow2Bias = 80, kPow2N = 96, kPowSub = 64, kPowTerms = 6;
+static __device__ double g_halo_pow2[kPow2N];      // 2^(a e), e = i - kPow2Bias
+static __device__ double g_halo_powc[kPowSub];     // c_j^a, c_j = 1 + (2 j + 1) / 128
+static __device__ double g_halo_invc[kPowSub];     // 1 / c_j
+static __device__ double g_halo_coef[kPowTerms + 1];   // binomial coefficients C(a, n)
+
+// the tables (one thread per entry; launched once per device, before any kernel that integrates an orbit)
+__global__ void k_halo_tables() {
+    const int i = threadIdx.x;
+    const double a = kHaloG1 - 1.0;
+    if (i < kPow2N) g_halo_pow2[i] = exp2(a * (double)(i - kPow2Bias));
+    if (i < kPowSub) {
+        const double c = 1.0 + (double)(2 * i + 1) / (2.0 * kPowSub);
+        g_halo_powc[i] = pow(c, a);
+        g_halo_invc[i] = 1.0 / c;
+    }
+    if (i == 0) {
+        double c = 1.0;
+        for (int n = 0; n <= kPowTerms; n++) {
+            g_halo_coef[n] = c;
+            c = c * (a - (double)n) / (double)(n + 1);
+        }
+    }
+}
+
+// x^a for x > 0 normal (here x in [8e-14, 8.4])
+__device__ __forceinline__ double halo_pow_a(double x) {
+    const long long bits = __double_as_longlong(x);
+    int e = (int)((bits >> 52) & 0x7ff) - 1023;
+    e = e < -kPow2Bias ? -kPow2Bias : (e > kPow2N - 1 - kPow2Bias ? kPow2N - 1 - kPow2Bias : e);
+    const int j = (int)((bits >> 46) & (kPowSub - 1));
+    const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
+    const double t = fma(m, __ldg(&g_halo_invc[j]), -1.0);
+    double s = __ldg(&g_halo_coef[kPowTerms]);
+#pragma unroll
+    for (int n = kPowTerms - 1; n >= 0; n--) s = fma(s, t, __ldg(&g_halo_coef[n]));
+    return __ldg(&g_halo_pow2[e + kPow2Bias]) * __ldg(&g_halo_powc[j]) * s;
+}
+
+// Acceleration of the Milky Way model at (x, y, z), FP64.
+//
+// Same model as the reference's milkyway_accel (src/potential.c:60-101), written for a GPU whose FP64 pipe is the
+// scarce resource: the three pow() and the divisions become reciprocal square roots and the table power above, using
+//   (r^2+b^2)^-3/2 = rsqrt(r^2+b^2)^3          (bulge)
+//   aR * x / R     = -GM x / D^3                 (disk, the R of the radial force cancels)
+//   x^g / (1 + x^(g-1)) = x p / (1 + p), p = x^(g-1) = x * x^(g-2)   (halo)
+// Mathematically identical; the last bits differ from glibc's as any libm's do.
+__device__ __forceinline__ void mw_accel(double x, double y, double z, double &ax, double &ay, double &az) {
+    const double R2 = fma(x, x, y * y);
+    const double r2 = fma(z, z, R2);
+    const double ib = rsqrt(r2 + kBulgeB2);
+    const double fb = -kBulgeGM * (ib * ib * ib);
+    const double zb2 = fma(z, z, kDiskB2);
+    const double iz = rsqrt(zb2);
+    const double s = fma(zb2, iz, kDiskA);                      // a + sqrt(z^2 + b^2)
+    const double iD = rsqrt(fma(s, s, R2));
+    const double fd = -kDiskGM * (iD * iD * iD);
+    double ir = rsqrt(r2);
+    double r = r2 * ir;
+    if (!(r > 1e-12)) { r = 1e-12; ir = 1e12; }
+    const double xh = fmin(r, kHaloCut) * kHaloInvA;
+    const double p = xh * halo_pow_a(xh);              // xh^(gamma - 1)
+    const double fh = -(kHaloGM * xh * p / (1.0 + p)) * (ir * ir * ir);
+    const double fr = fb + fh;
+    ax = (fr + fd) * x;
+    ay = (fr + fd) * y;
+    az = fma(fr, z, fd * z * s * iz);
+}
+
+// One orbit: position, velocity and the acceleration carried over (one force evaluation per step).
+struct Orbit {
+    double x, y, z, vx, vy, vz, ax, ay, az;
+    __device__ __forceinline__ void init() { mw_accel(x, y, z, ax, ay, az); }
+    // kick-drift-kick leapfrog (reference body_step, src/phygas.c:91-96)
+    __device__ __forceinline__ void kdk(double dt, double h) {
+        vx = fma(ax, h, vx); vy = fma(ay, h, vy); vz = fma(az, h, vz);
+        x = fma(vx, dt, x); y = fma(vy, dt, y); z = fma(vz, dt, z);
+        mw_accel(x, y, z, ax, ay, az);
+        vx = fma(ax, h, vx); vy = fma(ay, h, vy); vz = fma(az, h, vz);
+    }
+};
+
+}  // namespace pgx

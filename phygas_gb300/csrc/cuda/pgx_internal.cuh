@@ -21,49 +21,6 @@ constexpr double kStepMyr = 0.5;                                // PH_PRE_STEP_M
 constexpr int kSub = 10;                                        // PH_LIN_SUB
 constexpr double kEps = 1e-5;                                   // PH_LIN_EPS_POS == PH_LIN_EPS_VEL
 
-// Acceleration of the Milky Way model at (x, y, z), FP64.
-//
-// Same model as the reference's milkyway_accel (src/potential.c:60-101), written for a GPU whose FP64 pipe is the
-// scarce resource: the three pow() and the divisions become reciprocal square roots and one log/exp pair, using
-//   (r^2+b^2)^-3/2 = rsqrt(r^2+b^2)^3          (bulge)
-//   aR * x / R     = -GM x / D^3                 (disk, the R of the radial force cancels)
-//   x^g / (1 + x^(g-1)) = x p / (1 + p), p = x^(g-1) = exp((g-1) ln x)   (halo)
-// Mathematically identical; the last bits differ from glibc's as any libm's do.
-__device__ __forceinline__ void mw_accel(double x, double y, double z, double &ax, double &ay, double &az) {
-    const double R2 = fma(x, x, y * y);
-    const double r2 = fma(z, z, R2);
-    const double ib = rsqrt(r2 + kBulgeB2);
-    const double fb = -kBulgeGM * (ib * ib * ib);
-    const double zb2 = fma(z, z, kDiskB2);
-    const double iz = rsqrt(zb2);
-    const double s = fma(zb2, iz, kDiskA);                      // a + sqrt(z^2 + b^2)
-    const double iD = rsqrt(fma(s, s, R2));
-    const double fd = -kDiskGM * (iD * iD * iD);
-    double ir = rsqrt(r2);
-    double r = r2 * ir;
-    if (!(r > 1e-12)) { r = 1e-12; ir = 1e12; }
-    const double xh = fmin(r, kHaloCut) * kHaloInvA;
-    const double p = exp(kHaloG1 * log(xh));
-    const double fh = -(kHaloGM * xh * p / (1.0 + p)) * (ir * ir * ir);
-    const double fr = fb + fh;
-    ax = (fr + fd) * x;
-    ay = (fr + fd) * y;
-    az = fma(fr, z, fd * z * s * iz);
-}
-
-// One orbit: position, velocity and the acceleration carried over (one force evaluation per step).
-struct Orbit {
-    double x, y, z, vx, vy, vz, ax, ay, az;
-    __device__ __forceinline__ void init() { mw_accel(x, y, z, ax, ay, az); }
-    // kick-drift-kick leapfrog (reference body_step, src/phygas.c:91-96)
-    __device__ __forceinline__ void kdk(double dt, double h) {
-        vx = fma(ax, h, vx); vy = fma(ay, h, vy); vz = fma(az, h, vz);
-        x = fma(vx, dt, x); y = fma(vy, dt, y); z = fma(vz, dt, z);
-        mw_accel(x, y, z, ax, ay, az);
-        vx = fma(ax, h, vx); vy = fma(ay, h, vy); vz = fma(az, h, vz);
-    }
-};
-
 // A lower bound on the smallest eigenvalue of a symmetric positive semi-definite 3x3 matrix (xx xy xz yy yz zz),
 // FP64, by the trigonometric solution of the characteristic cubic (Smith, Comm. ACM 4, 168, 1961).  The margin covers
 // the rounding of q + 2p cos(phi + 2 pi/3) (a few ulps of the trace) and the sensitivity of acos near r = 1 (the

@@ -7,7 +7,7 @@ namespace pgx {
 
 // layout-identical to PhResult (include/phygas.h); checked by a static_assert in pgx_api.cu
 struct PhResultDev {
-    int n;
+    int n, pad;          // pad: PhResult's alignment gap, written as 0 so the results are fully defined bytes
     double d05, d50, d95, t05, t50, t95, v05, v50, v95, f_r50, f_rtot;
 };
 
@@ -62,6 +62,9 @@ struct ScreenRowDev {                // layout-identical to PgxScreenRow (includ
     int star, cluster, kb, pad;
     double sb, chi2, t_myr, d_nom_pc, sig_pc, p_r50, p_rtot, vrel_kms;
 };
+
+// the orbit force's tables, filled once per device (0 ok); before any orbit kernel, outside stream capture
+int orbit_setup(int dev);
 
 // ---- kernels ------------------------------------------------------------------------------------------------------
 __global__ void k_stm_orbits(int N, const double *ps0, const int *npts, int nmax, double *opos, double *ovel);

@@ -23,7 +23,7 @@
 #include <mutex>
 
 #include "phygas_gb300.h"
-#include "pgx_internal.cuh"
+#include "pgx_force.cuh"
 #include "pgx_kernels.h"
 
 namespace pgx {
@@ -280,6 +280,7 @@ __device__ void warp_reduce_pair(const double *__restrict__ best, const double *
     if (lane == 0) {
         PhResultDev o;
         o.n = m;
+        o.pad = 0;
         o.d05 = res[0]; o.d50 = res[1]; o.d95 = res[2];
         o.t05 = res[3]; o.t50 = res[4]; o.t95 = res[5];
         o.v05 = res[6]; o.v50 = res[7]; o.v95 = res[8];
@@ -391,6 +392,7 @@ __global__ void k_mc_prep(const McPairs *__restrict__ Pd) {
         if (P.clone_off[p + 1] - P.clone_off[p] > 0) continue;
         PhResultDev o;
         o.n = 0;
+        o.pad = 0;
         o.d05 = o.d50 = o.d95 = o.t05 = o.t50 = o.t95 = o.v05 = o.v50 = o.v95 = o.f_r50 = o.f_rtot = 0.0;
         P.res[p] = o;
     }
@@ -463,6 +465,7 @@ __global__ void k_pair_reduce_big(McPairs P) {
         if (threadIdx.x == 0) {
             PhResultDev o;
             o.n = 0;
+            o.pad = 0;
             o.d05 = o.d50 = o.d95 = o.t05 = o.t50 = o.t95 = o.v05 = o.v50 = o.v95 = o.f_r50 = o.f_rtot = 0.0;
             *out = o;
         }
@@ -513,6 +516,7 @@ __global__ void k_pair_reduce_big(McPairs P) {
     if (threadIdx.x == 0) {
         PhResultDev r;
         r.n = m;
+        r.pad = 0;
         r.d05 = res[0]; r.d50 = res[1]; r.d95 = res[2];
         r.t05 = res[3]; r.t50 = res[4]; r.t95 = res[5];
         r.v05 = res[6]; r.v50 = res[7]; r.v95 = res[8];
@@ -619,6 +623,7 @@ __global__ void __launch_bounds__(kMcThreads) k_pair_reduce_noalloc(int n_pairs,
         if (lane == 0) {
             PhResultDev z;
             z.n = m <= 0 ? 0 : -1;
+            z.pad = 0;
             z.d05 = z.d50 = z.d95 = z.t05 = z.t50 = z.t95 = z.v05 = z.v50 = z.v95 = z.f_r50 = z.f_rtot = 0.0;
             res[p] = z;
         }
@@ -649,7 +654,8 @@ int noalloc_setup(int dev, NoAllocDevice *&out) {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
     NoAllocDevice &d = g_noalloc_dev[dev];
     if (!d.ready) {
-        cudaError_t e = cudaGetSymbolAddress((void **)&d.cres, g_noalloc_cres);
+        cudaError_t e = orbit_setup(dev) ? cudaErrorUnknown : cudaSuccess;
+        if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&d.cres, g_noalloc_cres);
         if (e == cudaSuccess) e = cudaGetSymbolAddress((void **)&d.qhead, g_noalloc_qhead);
         int sms = 0, per_sm = 0;
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -710,3 +716,21 @@ extern "C" int pgx_pair_noalloc(void *stream, int n_pairs, int n_clones, const i
     }
     return 0;
 }
+
+namespace pgx {
+// The halo power tables of pgx_force.cuh, filled once per device (before the first orbit kernel on it; call it
+// outside any stream capture).
+int orbit_setup(int dev) {
+    static std::mutex mu;
+    static bool ready[64] = {};
+    if (dev < 0 || dev >= 64) return 1;
+    std::lock_guard<std::mutex> lk(mu);
+    if (ready[dev]) return 0;
+    k_halo_tables<<<1, 128>>>();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return 2;
+    ready[dev] = true;
+    return 0;
+}
+}  // namespace pgx

@@ -35,9 +35,12 @@ sys.path.insert(0, REPO)
 N_STARS, N_CLUSTERS, SEED = 20000, 4087, 1001
 CHI2_MAX, N_SAMP, R_KERNEL = 25.0, 64, 2.0
 # FP64 flops of one body step (one kick-drift-kick step of one orbit, its force evaluation included), from the
-# executed FP64 instructions of k_stm_orbits per body step: 40.4 DFMA + 7.5 DADD + 19.9 DMUL (ncu sass op counters,
-# FMA = 2 flops)
-FLOPS_PER_BODY_STEP = 108.0
+# executed FP64 instructions of k_stm_orbits per body step: 41.0 DFMA + 4.0 DADD + 31.0 DMUL (ncu sass op counters of
+# `python -m phygas_gb300.run_screen --stars 2000`, FMA = 2 flops)
+FLOPS_PER_BODY_STEP = 117.0
+# the same for one clone-step of the pair Monte Carlo (two body steps and the segment test), from k_pair_mc_t on
+# 1 pulsar x 64 clusters x 200 clones x 400 steps: 89.6 DFMA + 14.3 DADD + 70.8 DMUL per clone-step
+FLOPS_PER_CLONE_STEP = 264.3
 # DRAM traffic of one k_stm_orbits launch on this chunk (dram__bytes_read.sum + dram__bytes_write.sum from one ncu
 # capture of `python -m phygas_gb300.run_screen --stars 20000`): 4.9 MB read + 711.8 MB of orbit output written
 ORBIT_TRAFFIC_BYTES = 716.7e6
@@ -175,7 +178,7 @@ def pair_cpu_baseline(cp, pp, n_clones=200, clusters_per_proc=24, procs=None):
                       "slowest process %.1f s" % (procs * k, k, n_clones, clone_steps, max(runs))}
 
 
-def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu):
+def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
     """C3-style batch: draws on the host, the autotuner on a sample of it, then the batch timed on the GPU."""
     import numpy as np
     import phygas_gb300 as pg
@@ -213,6 +216,12 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu):
                        "dt 0.05 Myr" % (len(take), C3_PULSARS, len(pti)),
            "pairs": int(len(ti)), "clones": int(st["clones"]), "clone_steps": int(cs),
            "launch": "one captured CUDA graph (prep, persistent trace, reduce) per shape, replayed per batch",
+           "roofline": {"bound": "fp64", "kernel": "k_pair_mc_t",
+                        "achieved": FLOPS_PER_CLONE_STEP * cs / (statistics.mean(ms) * 1e-3) / 1e12,
+                        "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                        "frac": FLOPS_PER_CLONE_STEP * cs / (statistics.mean(ms) * 1e-3) / fp64_peak,
+                        "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
+                        "flops_per_clone_step": FLOPS_PER_CLONE_STEP},
            "autotune": {"chosen": {"warps_per_block": table[best][0], "clones_per_lane": table[best][1]},
                         "ms_on_sample": [{"warps_per_block": w, "clones_per_lane": c, "ms": t} for w, c, t in table]},
            "e2e": {"value": cs / (t_draw + statistics.mean(walls)), "unit": "clone-steps/s",
@@ -387,7 +396,7 @@ def main():
     pair_mc = None
     if not args.no_pair:
         try:
-            pair_mc = pair_mc_measure(ctx, stars, clusters, cp, r, rank == 0 and not args.no_cpu)
+            pair_mc = pair_mc_measure(ctx, stars, clusters, cp, r, rank == 0 and not args.no_cpu, fp64_peak)
         except Exception as e:          # reported beside the headline, not part of it
             log("pair Monte Carlo measurement failed: %s" % e)
 

@@ -48,13 +48,36 @@ PGX_HD bool trace_far32(float a, float dd, float m00, float m11, float tr, float
     return far && tr < 1.8e6f * lam;
 }
 
+// Reciprocal and reciprocal square root on the GPU's fast units: within 2 ulp (4 eps relative) by their documented
+// worst case (__fdividef for divisors in [2^-126, 2^126], rsqrtf for positive arguments).  Host builds use the exact
+// operations, which the same margins cover.
+PGX_HD float fast_rcp(float x) {
+#ifdef __CUDA_ARCH__
+    return __fdividef(1.f, x);
+#else
+    return 1.f / x;
+#endif
+}
+PGX_HD float fast_rsqrt(float x) {
+#ifdef __CUDA_ARCH__
+    return rsqrtf(x);
+#else
+    return 1.f / sqrtf(x);
+#endif
+}
+
 // A cheap test, run before the full bounds, that the FP64 path's point chi2 v is >= cut: then the point can be
 // neither a kept pair's minimum nor under the cut, and needs no bounds.  True when the trace bound rejects the point,
 // or by the triangle inequality in the M^-1 norm: the points the FP64 path evaluates (m0 and its nearest point u) lie
 // on the FP64 segment m0 -> m1, within dx = 3 eps max(|m0|, |m1|) of the FP32 segment, whose points all have
-// |x| >= |m0| - |dr|.  With q0 = m0^T M^-1 m0 and c = dr^T M^-1 dr as FP32 LDL^T forms (each within rho + 6 eps of
-// the exact one) and lam <= lambda_min(M):  v >= (1 - r64) (sqrt(q0 (1 - rho - 6 eps)) - sqrt(c (1 + rho + 6 eps)) -
-// dx / sqrt(lam))^2, with r64 <= 3 kAdj64 (tr / lam)^2 the FP64 adjugate's rounding (det(M) >= lam^2 tr / 3).
+// |x| >= |m0| - |dr|.  With q0 = m0^T M^-1 m0 and c = dr^T M^-1 dr as FP32 LDL^T forms and lam <= lambda_min(M):
+// v >= (1 - r64) (sqrt(q0 (1 - r)) - sqrt(c (1 + r)) - dx / sqrt(lam))^2, r64 <= 3 kAdj64 (tr / lam)^2 the FP64
+// adjugate's rounding (det(M) >= lam^2 tr / 3).
+// The reciprocals and square roots run on the fast units (4 eps each), so the error terms of point_bound32 grow:
+// the factorization's backward error becomes 13 eps sqrt(M_ii M_jj) (5 eps in each l, 6 in the pivots), with the
+// storage's 3 and the substitution's 4 at most 20 eps tr(M) -- kSkipC1 = 24 -- and the form's own rounding 8 eps
+// (12 below); each square root via x rsqrtf(x) is within 5 eps.
+constexpr float kSkipC1 = 24.f;
 PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float R2, float lmt, float lmc,
                          const float (&m0)[3], const float (&m1)[3], float cut) {
     const float M0 = St[0] + Sc[0] + R2, M1 = St[1] + Sc[1], M2 = St[2] + Sc[2];
@@ -67,27 +90,32 @@ PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float R2, f
     const float m00 = fmaf(m0[0], m0[0], fmaf(m0[1], m0[1], m0[2] * m0[2]));
     const float m11 = fmaf(m1[0], m1[0], fmaf(m1[1], m1[1], m1[2] * m1[2]));
     if (trace_far32(a, dd, m00, m11, tr, lam, cut)) return true;
-    if (!(lam > 0.f)) return false;
-    const float i1 = 1.f / M0;
+    if (!(lam > 1e-30f && M0 > 1e-30f && tr < 1e30f)) return false;
+    const float i1 = fast_rcp(M0);
     const float l10 = M1 * i1, l20 = M2 * i1;
     const float D2 = fmaf(-l10, M1, M3);
-    const float i2 = 1.f / D2;
+    if (!(D2 > 1e-30f)) return false;
+    const float i2 = fast_rcp(D2);
     const float uu = fmaf(-l20, M1, M4);
     const float l21 = uu * i2;
     const float D3 = fmaf(-l21, uu, fmaf(-l20, M2, M5));
-    const float i3 = 1.f / D3;
-    const float tl = tr / lam;
-    const float rho = kC1 * kEps32 * tl;
-    if (!(M0 > 0.f && D2 > 0.f && D3 > 0.f && rho <= 0.25f)) return false;
+    if (!(D3 > 1e-30f)) return false;
+    const float i3 = fast_rcp(D3);
+    const float il = fast_rcp(lam);
+    const float tl = tr * il * (1.f + 8.f * kEps32);
+    const float rho = kSkipC1 * kEps32 * tl;
+    if (!(rho <= 0.25f)) return false;
     const float q0 = ldl_form(l10, l20, l21, i1, i2, i3, m0[0], m0[1], m0[2]);
     const float c = ldl_form(l10, l20, l21, i1, i2, i3, dx, dy, dz);
-    const float big = sqrtf(fmaxf(m00, m11));
-    const float r = rho + 8.f * kEps32;
-    const float d = sqrtf(q0 * (1.f - r)) * (1.f - 2.f * kEps32) - sqrtf(c * (1.f + r)) * (1.f + 2.f * kEps32) -
-                    (3.f * kEps32 * big + 1e-12f) / sqrtf(lam) * (1.f + 4.f * kEps32);
+    const float r = rho + 12.f * kEps32;
+    const float big2 = fmaxf(fmaxf(m00, m11), 1e-30f);
+    const float big = big2 * fast_rsqrt(big2) * (1.f + 8.f * kEps32);
+    const float qa = fmaxf(q0 * (1.f - r), 1e-30f), ca = fmaxf(c * (1.f + r), 1e-30f);
+    const float d = qa * fast_rsqrt(qa) * (1.f - 8.f * kEps32) - ca * fast_rsqrt(ca) * (1.f + 8.f * kEps32) -
+                    (3.f * kEps32 * big + 1e-12f) * fast_rsqrt(lam) * (1.f + 8.f * kEps32);
     if (!(d > 0.f)) return false;
     const float r64 = kAdj64 * 3.f * (1.f + 16.f * kEps32) * tl * tl;
-    return d * d * (1.f - r64) * (1.f - 4.f * kEps32) >= cut;
+    return d * d * (1.f - r64) * (1.f - 8.f * kEps32) >= cut;
 }
 
 // Bounds on the FP64 path's point chi2 v = min(q(m0), q(ms)) -- the forms at the step's start and at the segment's

@@ -222,8 +222,10 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
                         "frac": FLOPS_PER_CLONE_STEP * cs / (statistics.mean(ms) * 1e-3) / fp64_peak,
                         "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
                         "flops_per_clone_step": FLOPS_PER_CLONE_STEP},
-           "autotune": {"chosen": {"warps_per_block": table[best][0], "clones_per_lane": table[best][1]},
-                        "ms_on_sample": [{"warps_per_block": w, "clones_per_lane": c, "ms": t} for w, c, t in table]},
+           "autotune": {"chosen": {"warps_per_block": table[best][0], "clones_per_lane": table[best][1],
+                                   "min_blocks_per_sm": table[best][2]},
+                        "ms_on_sample": [{"warps_per_block": w, "clones_per_lane": c, "min_blocks_per_sm": b, "ms": t}
+                                         for w, c, b, t in table]},
            "e2e": {"value": cs / (t_draw + statistics.mean(walls)), "unit": "clone-steps/s",
                    "host_draw_s": t_draw, "prefilter_s": t_pref, "gpu_call_s": statistics.mean(walls),
                    "h2d_bytes_per_step": int(12 * 8 * st["clones"] + 28 * len(ti)),

@@ -118,15 +118,16 @@ int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *p
              const double *dt, const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out);
 
 /* Launch-shape autotuner of the clone kernel (no counterpart in the reference): runs the batch (the arguments of
- * pgx_pair) with every shape this build has -- warps per block x clones traced per lane -- and keeps the fastest for
+ * pgx_pair) with every shape this build has -- warps per block x clones traced per lane x resident blocks per SM
+ * asked of the compiler (a register cap) -- and keeps the fastest for
  * this context's later pgx_pair calls.  ms[pgx_pair_shapes()] (or NULL) gets each shape's device time; *best (or NULL)
  * its index.  Every shape must give the same bits: a shape whose results differ fails the call (PGX_E_CUDA).
  * Batches whose pairs all have at most 1024 clones run as one captured CUDA graph (prep, persistent trace, reduce)
  * replayed with the batch's parameters; the tuner's runs also capture each shape's graph. */
 int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,
                   const double *dt, const double *r50_pc, const double *rtot_pc, double *ms, int *best);
-/* number of launch shapes; the first n as (warps per block, clones per lane) */
-int pgx_pair_shapes(int n, int *warps, int *clones_per_lane);
+/* number of launch shapes; the first n as (warps per block, clones per lane, minimum resident blocks per SM) */
+int pgx_pair_shapes(int n, int *warps, int *clones_per_lane, int *min_blocks);
 
 /* pgx_pair for callers that cannot allocate GPU memory (no counterpart in the reference): code running inside
  * another framework's device memory pool, loops that must not stall on the allocator, hosts that can only hand

@@ -111,7 +111,7 @@ SIGNATURES = [
                                       _I, _D, _D, _D]),
     ("pgx_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, C.c_void_p, _D]),
     ("pgx_tune_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, _D, _I]),
-    ("pgx_pair_shapes", C.c_int, [C.c_int, _I, _I]),
+    ("pgx_pair_shapes", C.c_int, [C.c_int, _I, _I, _I]),
     ("pgx_stats", C.c_int, [C.c_void_p, _P(PgxStats)]),
     ("pgx_peaks", C.c_int, [C.c_void_p, _D, _D]),
     ("pgx_check_bounds", C.c_int, [C.c_void_p, C.c_int, _D, _D, _D, C.c_double, _D, _P(C.c_float),
@@ -344,7 +344,7 @@ class Context:
 
     def tune_pair(self, clone_off, ps, steps, dt, r50_pc, rtot_pc):
         """Time every launch shape of the clone kernel on this batch and keep the fastest (pgx_tune_pair):
-        -> (index of the chosen shape, [(warps per block, clones per lane, ms), ...])."""
+        -> (index of the chosen shape, [(warps per block, clones per lane, min blocks per SM, ms), ...])."""
         args = [np.ascontiguousarray(clone_off, np.int32), np.ascontiguousarray(ps, np.float64),
                 np.ascontiguousarray(steps, np.int32), np.ascontiguousarray(dt, np.float64),
                 np.ascontiguousarray(r50_pc, np.float64), np.ascontiguousarray(rtot_pc, np.float64)]
@@ -353,15 +353,15 @@ class Context:
         self._check(lib().pgx_tune_pair(self.h, len(args[2]), _ptr(args[0], C.c_int), _ptr(args[1]),
                                         _ptr(args[2], C.c_int), _ptr(args[3]), _ptr(args[4]), _ptr(args[5]),
                                         _ptr(ms), C.byref(best)), "pgx_tune_pair")
-        return best.value, [(w, c, t) for (w, c), t in zip(shapes, ms.tolist())]
+        return best.value, [(w, c, b, t) for (w, c, b), t in zip(shapes, ms.tolist())]
 
 
 def pair_shapes():
-    """The clone kernel's launch shapes: [(warps per block, clones per lane), ...]."""
-    n = lib().pgx_pair_shapes(0, None, None)
-    w, c = np.zeros(n, np.int32), np.zeros(n, np.int32)
-    lib().pgx_pair_shapes(n, _ptr(w, C.c_int), _ptr(c, C.c_int))
-    return list(zip(w.tolist(), c.tolist()))
+    """The clone kernel's launch shapes: [(warps per block, clones per lane, min resident blocks per SM), ...]."""
+    n = lib().pgx_pair_shapes(0, None, None, None)
+    w, c, b = np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32)
+    lib().pgx_pair_shapes(n, _ptr(w, C.c_int), _ptr(c, C.c_int), _ptr(b, C.c_int))
+    return list(zip(w.tolist(), c.tolist(), b.tolist()))
 
 
 class HostRows:

@@ -631,8 +631,8 @@ int pair_run(PgxContext *ctx, int variant, int n_pairs, const int *clone_off, co
     CK(cudaSetDevice(ctx->device));
     const int M = clone_off[n_pairs];
     if (clone_off[0] != 0 || M < 0 || (M > 0 && !ps)) return fail(ctx, PGX_E_ARG, "pgx_pair: clone_off");
-    int warps = 4, cpl = 1;
-    pgx::mc_variant_shape(variant, warps, cpl);
+    int warps = 4, cpl = 1, minb = 1;
+    pgx::mc_variant_shape(variant, warps, cpl, minb);
     int mmax = 0;
     for (int p = 0; p < n_pairs; p++) {
         const int m = clone_off[p + 1] - clone_off[p];
@@ -760,9 +760,9 @@ int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const doub
     return 0;
 }
 
-int pgx_pair_shapes(int n, int *warps, int *clones_per_lane) {
+int pgx_pair_shapes(int n, int *warps, int *clones_per_lane, int *min_blocks) {
     const int nv = pgx::mc_variants();
-    for (int v = 0; v < n && v < nv; v++) pgx::mc_variant_shape(v, warps[v], clones_per_lane[v]);
+    for (int v = 0; v < n && v < nv; v++) pgx::mc_variant_shape(v, warps[v], clones_per_lane[v], min_blocks[v]);
     return nv;
 }
 

@@ -75,7 +75,7 @@ __global__ void k_pair_mc(McPairs P);
 // clones per lane), full persistent grid, and the prep + trace + reduce kernels as one sequence on a stream (pairs of
 // at most 1024 clones)
 int mc_variants();
-void mc_variant_shape(int v, int &warps, int &cpl);
+void mc_variant_shape(int v, int &warps, int &cpl, int &min_blocks);
 cudaError_t mc_variant_grid(int v, int sms, int &grid);
 cudaError_t launch_mc(int v, int grid, int prep_grid, int reduce_grid, cudaStream_t st, const McPairs *Pd);
 __global__ void k_pair_reduce_big(McPairs P);

@@ -344,11 +344,12 @@ __global__ void __launch_bounds__(kMcThreads) k_pair_mc(McPairs P) {
 
 // Persistent clone tracing for batches replayed from a captured graph: parameters read from device memory, and the
 // launch shape a template: WARPS warps per block, CPL clones per lane traced in lockstep (items of up to 32 * CPL
-// clones; a lane past its item's end repeats its first clone and discards the copy).  Tracing only -- the pairs are
+// clones; a lane past its item's end repeats its first clone and discards the copy), and MINB resident blocks per SM
+// asked of the compiler (fewer registers per thread, more warps to hide the FP64 pipe's latency).  Tracing only -- the pairs are
 // reduced by k_pair_reduce_dev afterwards, which keeps this kernel's registers to the orbits'.  The clones'
 // arithmetic is the same in every variant, so every variant gives the same bits.
-template <int WARPS, int CPL>
-__global__ void __launch_bounds__(WARPS * 32) k_pair_mc_t(const McPairs *__restrict__ Pd) {
+template <int WARPS, int CPL, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB) k_pair_mc_t(const McPairs *__restrict__ Pd) {
     const McPairs P = *Pd;
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -411,20 +412,22 @@ __global__ void __launch_bounds__(kMcThreads) k_pair_reduce_dev(const McPairs *_
 
 namespace {
 struct McVariant {
-    int warps, cpl;
+    int warps, cpl, min_blocks;
     void (*fn)(const McPairs *);
 };
 const McVariant kMcVariants[] = {
-    {4, 1, k_pair_mc_t<4, 1>}, {2, 1, k_pair_mc_t<2, 1>}, {8, 1, k_pair_mc_t<8, 1>},
-    {4, 2, k_pair_mc_t<4, 2>}, {2, 2, k_pair_mc_t<2, 2>}, {8, 2, k_pair_mc_t<8, 2>},
+    {4, 1, 1, k_pair_mc_t<4, 1, 1>}, {2, 1, 1, k_pair_mc_t<2, 1, 1>}, {8, 1, 1, k_pair_mc_t<8, 1, 1>},
+    {4, 2, 1, k_pair_mc_t<4, 2, 1>}, {2, 2, 1, k_pair_mc_t<2, 2, 1>}, {8, 2, 1, k_pair_mc_t<8, 2, 1>},
+    {4, 1, 5, k_pair_mc_t<4, 1, 5>}, {4, 1, 6, k_pair_mc_t<4, 1, 6>}, {8, 1, 3, k_pair_mc_t<8, 1, 3>},
 };
 }  // namespace
 
 int mc_variants() { return (int)(sizeof kMcVariants / sizeof kMcVariants[0]); }
 
-void mc_variant_shape(int v, int &warps, int &cpl) {
+void mc_variant_shape(int v, int &warps, int &cpl, int &min_blocks) {
     warps = kMcVariants[v].warps;
     cpl = kMcVariants[v].cpl;
+    min_blocks = kMcVariants[v].min_blocks;
 }
 
 // resident blocks of variant v for a full persistent grid (blocks per SM x SMs)

@@ -151,7 +151,7 @@ def test_every_launch_shape_gives_the_same_bits(ctx):
         checks = {q: ot.parse_pair_dump(ot.run([ot.ORACLE_DUMP, "pair", cp, tp, str(ti[q]), str(ci[q]),
                                                 str(ci[q] + 1), str(ncl[q]), "0.05"]))[0] for q in (0, 7, 39)}
     best, table = ctx.tune_pair(*batch)
-    assert 0 <= best < len(table) and all(t > 0 for _, _, t in table)
+    assert 0 <= best < len(table) and all(t > 0 for _, _, _, t in table)
     res, clones = ctx.pair(*batch, want_clones=True)
     again = ctx.pair(*batch)
     assert res.tobytes() == again.tobytes()
@@ -161,4 +161,4 @@ def test_every_launch_shape_gives_the_same_bits(ctx):
         ref = np.array(p["clones"])
         got = clones[:, off[q]:off[q + 1]].T
         assert np.all(np.abs(got - ref) <= ot.REL_TOL * np.abs(ref) + 1e-12), q
-    print("launch shapes:", table, "chosen", table[best][:2])
+    print("launch shapes:", table, "chosen", table[best][:3])

@@ -81,6 +81,13 @@ int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n);
 int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *prefix,
                     double tmax, double chi2_max, int precision, PgxScreenRow *rows, long cap, long *n_rows);
 void *pgx_host_alloc(size_t bytes);
+/* The whole star list t[nt] in chunks of `chunk` stars, pipelined: the draws of chunk i + 1 (ph_lin_target_init's,
+ * on `threads` host threads) run while the GPU screens chunk i, whose rows are copied into page-locked memory and
+ * handed to emit(arg, first star of the chunk, rows, count) -- star indices in the rows are relative to the chunk's
+ * first star; the pointer is valid until emit returns.  A non-zero return from emit stops the run. */
+int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n_samp, int threads, double tmax,
+                      double chi2_max, int precision,
+                      int (*emit)(void *arg, int first, const PgxScreenRow *rows, long n), void *arg);
 void pgx_host_free(void *p);
 
 /* Host draws for the records API (reference ph_lin_target_init / the draws of ph_lin_cluster, src/phygas.c:274-344,

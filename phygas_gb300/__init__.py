@@ -101,6 +101,8 @@ SIGNATURES = [
     ("pgx_screen_into", C.c_int, [C.c_void_p, C.c_int, _D, _D, _U64, C.c_double, C.c_double, C.c_int, C.c_void_p,
                                   C.c_long, _P(C.c_long)]),
     ("pgx_host_alloc", C.c_void_p, [C.c_size_t]),
+    ("pgx_screen_chunks", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                    C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     ("pgx_host_free", None, [C.c_void_p]),
     ("pgx_draw_targets", C.c_int, [_P(PhTarget), C.c_int, C.c_int, C.c_int, _D, _D, _U64]),
     ("pgx_draw_clusters", C.c_int, [_P(PhCluster), C.c_int, C.c_int, C.c_int, _D, _D]),
@@ -311,6 +313,28 @@ class Context:
                     "pgx_screen_into")
         return arr[:n.value]
 
+    def screen_chunks(self, targets, chunk, tmax, emit, chi2_max=25.0, precision=PGX_MIXED, n_samp=64, threads=0):
+        """pgx_screen_chunks: the targets in chunks, host draws of the next chunk overlapping the GPU work on this
+        one; emit(first_star, rows) gets each chunk's rows (a view into page-locked memory, valid during the call;
+        star indices relative to first_star)."""
+        targets = as_array(targets, PhTarget)
+        err = []
+
+        def cb(_arg, first, ptr, n):
+            try:
+                rows = np.ctypeslib.as_array((C.c_char * (n * ROW_DTYPE.itemsize)).from_address(ptr)) if n else b""
+                emit(first, np.frombuffer(rows, ROW_DTYPE, n) if n else np.zeros(0, ROW_DTYPE))
+                return 0
+            except Exception as e:           # stop the run, re-raise after it
+                err.append(e)
+                return 1
+        fn = EMIT_FN(cb)
+        rc = lib().pgx_screen_chunks(self.h, targets, len(targets), chunk, n_samp, threads, tmax, chi2_max,
+                                     precision, C.cast(fn, C.c_void_p), None)
+        if err:
+            raise err[0]
+        self._check(rc, "pgx_screen_chunks")
+
     def stage(self, ps0, sig, prefix):
         self._keep = (np.ascontiguousarray(ps0, np.float64), np.ascontiguousarray(sig, np.float64),
                       np.ascontiguousarray(prefix, np.uint64))
@@ -362,6 +386,9 @@ def pair_shapes():
     w, c, b = np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32)
     lib().pgx_pair_shapes(n, _ptr(w, C.c_int), _ptr(c, C.c_int), _ptr(b, C.c_int))
     return list(zip(w.tolist(), c.tolist(), b.tolist()))
+
+
+EMIT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_long)
 
 
 class HostRows:

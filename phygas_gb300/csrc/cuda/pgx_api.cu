@@ -14,6 +14,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "phygas_gb300.h"
@@ -584,6 +585,57 @@ int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *si
     *n_rows = n;
     if (n > cap) return fail(ctx, PGX_E_LIMIT, "pgx_screen_into: %ld rows, room for %ld", n, cap);
     return pgx_screen_fetch(ctx, rows, n);
+}
+
+int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n_samp, int threads, double tmax,
+                      double cut, int precision, int (*emit)(void *arg, int first, const PgxScreenRow *rows, long n),
+                      void *arg) {
+    if (!ctx) return PGX_E_ARG;
+    if (nt < 0 || (nt > 0 && !t) || chunk <= 0 || chunk > (1 << 20) || n_samp < 0 || !emit)
+        return fail(ctx, PGX_E_ARG, "pgx_screen_chunks: bad args");
+    if (nt == 0) return 0;
+    const int th = threads > 0 ? threads : pgh_default_threads();
+    const int nch = (nt + chunk - 1) / chunk;
+    // two draw buffers: the host thread fills chunk i + 1 while the GPU screens chunk i
+    struct Draw {
+        std::vector<double> ps0, sig;
+        std::vector<uint64_t> pre;
+        int first = 0, n = 0;
+    } buf[2];
+    for (auto &b : buf) {
+        b.ps0.resize((size_t)6 * chunk);
+        b.sig.resize((size_t)36 * chunk);
+        b.pre.resize(chunk);
+    }
+    auto draw = [&](int c, Draw &b) {
+        b.first = c * chunk;
+        b.n = std::min(chunk, nt - b.first);
+        pgh_draw_targets(t + b.first, b.n, n_samp, th, b.ps0.data(), b.sig.data(), b.pre.data());
+    };
+    // page-locked rows, grown when a chunk keeps more pairs than they hold
+    PgxScreenRow *rows = nullptr;
+    long cap = 0;
+    int rc = 0;
+    draw(0, buf[0]);
+    for (int c = 0; c < nch && rc == 0; c++) {
+        Draw &cur = buf[c & 1];
+        std::thread ahead;
+        if (c + 1 < nch) ahead = std::thread(draw, c + 1, std::ref(buf[(c + 1) & 1]));
+        long n = 0;
+        rc = pgx_screen_into(ctx, cur.n, cur.ps0.data(), cur.sig.data(), cur.pre.data(), tmax, cut, precision, rows,
+                             cap, &n);
+        if (rc == PGX_E_LIMIT) {
+            pgx_host_free(rows);
+            cap = n + n / 4 + 4096;
+            rows = (PgxScreenRow *)pgx_host_alloc(sizeof(PgxScreenRow) * (size_t)cap);
+            rc = rows ? pgx_screen_fetch(ctx, rows, n) : fail(ctx, PGX_E_NOMEM, "pgx_screen_chunks: host rows");
+            if (!rows) cap = 0;
+        }
+        if (rc == 0 && emit(arg, cur.first, rows, n)) rc = fail(ctx, PGX_E_ARG, "pgx_screen_chunks: emit stopped");
+        if (ahead.joinable()) ahead.join();
+    }
+    pgx_host_free(rows);
+    return rc;
 }
 
 void *pgx_host_alloc(size_t bytes) {

@@ -20,6 +20,30 @@ static double now_s(void) {
     return (double)ts.tv_sec + ts.tv_nsec * 1e-9;
 }
 
+typedef struct {
+    const PhTarget *tg;
+    const PhCluster *cl;
+    long kept;
+    double t0;
+    int done;
+} Printer;
+
+/* one chunk's rows, in (star, cluster) order */
+static int print_rows(void *arg, int first, const PgxScreenRow *rows, long n) {
+    Printer *P = arg;
+    for (long h = 0; h < n; h++) {
+        const PgxScreenRow *r = &rows[h];
+        const PhTarget *t = &P->tg[first + r->star];
+        const PhCluster *c = &P->cl[r->cluster];
+        printf("%s %s %c %.3f %.3f %.2f %.2f %.4f %.4f %.2f %.3f %.3f\n", t->id, c->name, c->kind, r->chi2, r->t_myr,
+               r->d_nom_pc, r->sig_pc, r->p_r50, r->p_rtot, r->vrel_kms, c->age16, c->age84);
+    }
+    P->kept += n;
+    P->done = first;
+    fprintf(stderr, "%d+ targets, %ld pairs kept, %.1f s\n", first, P->kept, now_s() - P->t0);
+    return 0;
+}
+
 static int env_int(const char *name, int def) {
     const char *v = getenv(name);
     int x = v ? atoi(v) : 0;
@@ -69,29 +93,11 @@ int main(int argc, char **argv) {
         fprintf(stderr, "control run: velocities taken from the star %d lines away\n", nt / 2);
     }
     const int chunk = env_int("PHYGAS_CHUNK", 20000);
-    double *ps0 = malloc(sizeof(double) * 6 * chunk), *sig = malloc(sizeof(double) * 36 * chunk);
-    uint64_t *pre = malloc(sizeof(uint64_t) * chunk);
-    long kept = 0;
-    t0 = now_s();
-    for (int j0 = 0; j0 < nt; j0 += chunk) {
-        int n = nt - j0 < chunk ? nt - j0 : chunk;
-        pgx_draw_targets(tg + j0, n, n_samp, 0, ps0, sig, pre);
-        PgxScreenRow *rows;
-        long nr;
-        if (pgx_screen(ctx, n, ps0, sig, pre, tmax, chi2_max, precision, &rows, &nr)) {
-            fprintf(stderr, "phygas_screen: screen: %s\n", pgx_last_error(ctx));
-            return 1;
-        }
-        for (long h = 0; h < nr; h++) {
-            const PgxScreenRow *r = &rows[h];
-            const PhTarget *t = &tg[j0 + r->star];
-            const PhCluster *c = &cl[r->cluster];
-            printf("%s %s %c %.3f %.3f %.2f %.2f %.4f %.4f %.2f %.3f %.3f\n", t->id, c->name, c->kind, r->chi2,
-                   r->t_myr, r->d_nom_pc, r->sig_pc, r->p_r50, r->p_rtot, r->vrel_kms, c->age16, c->age84);
-        }
-        kept += nr;
-        pgx_free(rows);
-        fprintf(stderr, "%d targets, %ld pairs kept, %.4f s per target\n", j0 + n, kept, (now_s() - t0) / (j0 + n));
+    Printer P = {tg, cl, 0, now_s(), 0};
+    /* the draws of the next chunk run while the GPU screens this one (pgx_screen_chunks) */
+    if (pgx_screen_chunks(ctx, tg, nt, chunk, n_samp, 0, tmax, chi2_max, precision, print_rows, &P)) {
+        fprintf(stderr, "phygas_screen: screen: %s\n", pgx_last_error(ctx));
+        return 1;
     }
     pgx_close(ctx);
     return 0;

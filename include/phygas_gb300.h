@@ -81,10 +81,12 @@ int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n);
 int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *prefix,
                     double tmax, double chi2_max, int precision, PgxScreenRow *rows, long cap, long *n_rows);
 void *pgx_host_alloc(size_t bytes);
-/* The whole star list t[nt] in chunks of `chunk` stars, pipelined: the draws of chunk i + 1 (ph_lin_target_init's,
- * on `threads` host threads) run while the GPU screens chunk i, whose rows are copied into page-locked memory and
- * handed to emit(arg, first star of the chunk, rows, count) -- star indices in the rows are relative to the chunk's
- * first star; the pointer is valid until emit returns.  A non-zero return from emit stops the run. */
+/* The whole star list t[nt] in chunks of `chunk` stars, pipelined: while the GPU screens chunk i, the draws of chunk
+ * i + 1 (ph_lin_target_init's, on `threads` host threads) run, the rows of chunk i - 1 are copied into page-locked
+ * memory on a second stream, and emit(arg, first star of chunk i - 1, rows, count) runs on the calling thread.  Star
+ * indices in the rows are relative to the chunk's first star; the pointer is valid until emit returns.  Chunks are
+ * emitted in order.  A non-zero return from emit stops the run.  The page-locked and device row buffers (two chunks
+ * of each) stay with the context for the next call. */
 int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n_samp, int threads, double tmax,
                       double chi2_max, int precision,
                       int (*emit)(void *arg, int first, const PgxScreenRow *rows, long n), void *arg);

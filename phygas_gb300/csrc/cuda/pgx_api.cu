@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstddef>
+#include <condition_variable>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -50,6 +51,10 @@ struct PgxContext {
     Buf s_ps0, s_sig21, s_prefix;
     Buf opos, ovel, t64, t32, tlm;
     Buf chi2T, kbT, sbT, cnt, off, total, kept, fin, rows;
+    // pgx_screen_chunks: two chunks' rows on the device and in page-locked host memory, reused across calls
+    Buf rows_b[2];
+    PgxScreenRow *h_rows[2] = {};
+    long h_cap[2] = {};
     pgx::MixedBufs mixed;
     long n_rows = 0;
     // pair Monte Carlo
@@ -204,9 +209,11 @@ void pgx_close(PgxContext *ctx) {
                    &ctx->p_off, &ctx->p_ps, &ctx->p_steps, &ctx->p_dt, &ctx->p_r50, &ctx->p_rt, &ctx->p_items,
                    &ctx->p_q, &ctx->p_done, &ctx->p_cres, &ctx->p_res, &ctx->p_params, &ctx->x_ps0, &ctx->x_sig21,
                    &ctx->x_npts,
-                   &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32};
+                   &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32, &ctx->rows_b[0], &ctx->rows_b[1]};
     for (Buf *b : bufs)
         if (b->p) cudaFree(b->p);
+    for (auto *h : ctx->h_rows)
+        if (h) cudaFreeHost(h);
     pgx::mixed_free(ctx->mixed);
     for (auto &g : ctx->mc_exec)
         if (g) cudaGraphExecDestroy(g);
@@ -594,9 +601,13 @@ int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int
     if (nt < 0 || (nt > 0 && !t) || chunk <= 0 || chunk > (1 << 20) || n_samp < 0 || !emit)
         return fail(ctx, PGX_E_ARG, "pgx_screen_chunks: bad args");
     if (nt == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
     const int th = threads > 0 ? threads : pgh_default_threads();
     const int nch = (nt + chunk - 1) / chunk;
-    // two draw buffers: the host thread fills chunk i + 1 while the GPU screens chunk i
+    // Three stages run at once: the host draws of chunk c + 1 (a helper thread), the GPU work of chunk c (a worker
+    // thread: stage, exec, then a device copy of its rows into slot c % 2 and their copy to page-locked host memory
+    // on a second stream), and emit(c - 1) on the calling thread.  Slot s is reused for chunk c + 2 only after
+    // emit(c) has returned.
     struct Draw {
         std::vector<double> ps0, sig;
         std::vector<uint64_t> pre;
@@ -612,29 +623,105 @@ int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int
         b.n = std::min(chunk, nt - b.first);
         pgh_draw_targets(t + b.first, b.n, n_samp, th, b.ps0.data(), b.sig.data(), b.pre.data());
     };
-    // page-locked rows, grown when a chunk keeps more pairs than they hold
-    PgxScreenRow *rows = nullptr;
-    long cap = 0;
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev_rows[2] = {}, ev_host[2] = {};
+    CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     int rc = 0;
-    draw(0, buf[0]);
-    for (int c = 0; c < nch && rc == 0; c++) {
-        Draw &cur = buf[c & 1];
-        std::thread ahead;
-        if (c + 1 < nch) ahead = std::thread(draw, c + 1, std::ref(buf[(c + 1) & 1]));
-        long n = 0;
-        rc = pgx_screen_into(ctx, cur.n, cur.ps0.data(), cur.sig.data(), cur.pre.data(), tmax, cut, precision, rows,
-                             cap, &n);
-        if (rc == PGX_E_LIMIT) {
-            pgx_host_free(rows);
-            cap = n + n / 4 + 4096;
-            rows = (PgxScreenRow *)pgx_host_alloc(sizeof(PgxScreenRow) * (size_t)cap);
-            rc = rows ? pgx_screen_fetch(ctx, rows, n) : fail(ctx, PGX_E_NOMEM, "pgx_screen_chunks: host rows");
-            if (!rows) cap = 0;
-        }
-        if (rc == 0 && emit(arg, cur.first, rows, n)) rc = fail(ctx, PGX_E_ARG, "pgx_screen_chunks: emit stopped");
-        if (ahead.joinable()) ahead.join();
+    for (int i = 0; i < 2 && rc == 0; i++) {
+        if (cudaEventCreateWithFlags(&ev_rows[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_host[i], cudaEventDisableTiming) != cudaSuccess)
+            rc = fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: events");
     }
-    pgx_host_free(rows);
+    std::mutex mu;
+    std::condition_variable cv;
+    int produced = 0, consumed = 0, worker_rc = 0;
+    bool worker_done = false, stop = false;
+    long n_of[2] = {0, 0};
+    int first_of[2] = {0, 0};
+    auto worker = [&]() {
+        int wrc = cudaSetDevice(ctx->device) == cudaSuccess ? 0 : fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: device");
+        if (wrc == 0) draw(0, buf[0]);
+        for (int c = 0; c < nch && wrc == 0; c++) {
+            Draw &cur = buf[c & 1];
+            std::thread ahead;
+            if (c + 1 < nch) ahead = std::thread(draw, c + 1, std::ref(buf[(c + 1) & 1]));
+            long n = 0;
+            wrc = pgx_screen_stage(ctx, cur.n, cur.ps0.data(), cur.sig.data(), cur.pre.data());
+            if (wrc == 0) wrc = pgx_screen_exec(ctx, tmax, cut, precision, &n);
+            const int slot = c & 1;
+            if (wrc == 0) {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return consumed >= c - 1 || stop; });
+                if (stop) wrc = -1;
+            }
+            if (wrc == 0 && ctx->h_cap[slot] < n) {
+                pgx_host_free(ctx->h_rows[slot]);
+                ctx->h_cap[slot] = 0;
+                const long cap = n + n / 4 + 4096;
+                ctx->h_rows[slot] = (PgxScreenRow *)pgx_host_alloc(sizeof(PgxScreenRow) * (size_t)cap);
+                if (ctx->h_rows[slot]) ctx->h_cap[slot] = cap;
+                else wrc = fail(ctx, PGX_E_NOMEM, "pgx_screen_chunks: %ld page-locked rows", cap);
+            }
+            const size_t bytes = (size_t)n * sizeof(PgxScreenRow);
+            if (wrc == 0 && n > 0) wrc = ensure(ctx, ctx->rows_b[slot], bytes);
+            if (wrc == 0 && n > 0) {
+                const cudaError_t e[4] = {
+                    cudaMemcpyAsync(ctx->rows_b[slot].p, ctx->rows.p, bytes, cudaMemcpyDeviceToDevice, ctx->st),
+                    cudaEventRecord(ev_rows[slot], ctx->st), cudaStreamWaitEvent(cs, ev_rows[slot], 0),
+                    cudaMemcpyAsync(ctx->h_rows[slot], ctx->rows_b[slot].p, bytes, cudaMemcpyDeviceToHost, cs)};
+                for (cudaError_t x : e)
+                    if (x != cudaSuccess && wrc == 0)
+                        wrc = fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: row copy: %s", cudaGetErrorString(x));
+            }
+            if (wrc == 0 && cudaEventRecord(ev_host[slot], cs) != cudaSuccess)
+                wrc = fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: event record");
+            if (ahead.joinable()) ahead.join();
+            if (wrc == 0) {
+                std::lock_guard<std::mutex> lk(mu);
+                n_of[slot] = n;
+                first_of[slot] = cur.first;
+                produced = c + 1;
+                cv.notify_all();
+            }
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        worker_rc = wrc;
+        worker_done = true;
+        cv.notify_all();
+    };
+    std::thread gpu;
+    if (rc == 0) gpu = std::thread(worker);
+    for (int c = 0; c < nch && rc == 0; c++) {
+        long n;
+        int first;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv.wait(lk, [&] { return produced > c || worker_done; });
+            if (produced <= c) break;                     // the worker stopped: its code is returned below
+            n = n_of[c & 1];
+            first = first_of[c & 1];
+        }
+        if (cudaEventSynchronize(ev_host[c & 1]) != cudaSuccess) {
+            rc = PGX_E_CUDA;
+        } else if (emit(arg, first, ctx->h_rows[c & 1], n)) {
+            rc = PGX_E_ARG;
+        }
+        std::lock_guard<std::mutex> lk(mu);
+        consumed = c + 1;
+        if (rc) stop = true;
+        cv.notify_all();
+    }
+    if (gpu.joinable()) gpu.join();
+    // codes set here, after the worker has ended, so that the message is this function's
+    if (rc == PGX_E_ARG) rc = fail(ctx, PGX_E_ARG, "pgx_screen_chunks: emit stopped");
+    else if (rc == PGX_E_CUDA) rc = fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: row copy failed");
+    else if (rc == 0 && worker_rc > 0) rc = worker_rc;
+    cudaStreamSynchronize(cs);
+    for (int i = 0; i < 2; i++) {
+        if (ev_rows[i]) cudaEventDestroy(ev_rows[i]);
+        if (ev_host[i]) cudaEventDestroy(ev_host[i]);
+    }
+    cudaStreamDestroy(cs);
     return rc;
 }
 

@@ -139,3 +139,34 @@ def test_screen_into_page_locked_rows(ctx, golden):
         ctx.screen_into(a, b, c, tmax, small)
     assert ctx.fetch(len(want)).tobytes() == want.tobytes()
     buf.close()
+
+
+def test_screen_chunks_pipeline_matches_one_screen(ctx, golden):
+    """pgx_screen_chunks (host draws, GPU screen and row copies overlapped, emit on the calling thread) gives each
+    chunk's rows in order, equal to screening the whole list at once after renumbering the stars; the buffers it
+    keeps serve a second call with other chunk sizes; a non-zero emit stops the run with an error."""
+    clusters, stars = pg.read_clusters(golden["clusters"]), pg.read_targets(golden["screen"])[:300]
+    ctx.set_clusters(clusters)
+    tmax = max(c.tmax_myr for c in clusters)
+    for prec in PRECISIONS:
+        want = ctx.screen(*pg.draw_targets(stars), tmax, 25.0, prec)
+        for chunk in (128, 37, 300):
+            got, firsts = [], []
+
+            def emit(first, rows):
+                r = np.array(rows, copy=True)
+                r["star"] += first
+                firsts.append(first)
+                got.append(r)
+            ctx.screen_chunks(stars, chunk, tmax, emit, 25.0, prec)
+            assert firsts == list(range(0, len(stars), chunk))
+            assert np.concatenate(got).tobytes() == want.tobytes(), (prec, chunk)
+    calls = []
+
+    def stop(first, rows):
+        calls.append(first)
+        return 1 / 0
+    with pytest.raises(ZeroDivisionError):
+        ctx.screen_chunks(stars, 50, tmax, stop)
+    assert calls == [0]
+    assert len(ctx.screen(*pg.draw_targets(stars[:40]), tmax)) >= 0      # the context is still usable

@@ -1,6 +1,7 @@
 // pgx_force.cuh -- the Allen & Santillan (1991) Milky Way force and the kick-drift-kick step, FP64 (internal header
 // of pgx_orbit.cu, which owns the halo power tables and fills them once per device).
 #pragma once
+#include "pgx_bits.cuh"
 #include "pgx_internal.cuh"
 
 namespace pgx {
@@ -49,34 +50,56 @@ __device__ __forceinline__ double halo_pow_a(double x) {
     return __ldg(&g_halo_pow2[e + kPow2Bias]) * __ldg(&g_halo_powc[j]) * s;
 }
 
+// x^-1/2 and 1/d in FP64 from the FP32 unit's seed and one third-order step (pgx_bits.cuh: within an ulp or two,
+// 5 and 3 FP64 operations); an argument outside [2^-125, 2^125) -- none in a force evaluation of a bound orbit --
+// takes the library's function instead.
+__device__ __forceinline__ double rsqrt_h3(double x) {
+    const uint32_t hi = f64_hi(x);
+    if (!seed_ok(hi)) return rsqrt(x);
+    return rsqrt_refine(x, widen_seed(rsqrtf(seed_arg(hi))));
+}
+__device__ __forceinline__ double rcp_h3(double d) {
+    const uint32_t hi = f64_hi(d);
+    if (!seed_ok(hi)) return 1.0 / d;
+    return rcp_refine(d, widen_seed(__frcp_rn(seed_arg(hi))));
+}
+
 // Acceleration of the Milky Way model at (x, y, z), FP64.
 //
 // Same model as the reference's milkyway_accel (src/potential.c:60-101), written for a GPU whose FP64 pipe is the
-// scarce resource: the three pow() and the divisions become reciprocal square roots and the table power above, using
+// scarce resource: the three pow() and the divisions become the reciprocal square roots and reciprocal above and the
+// table power, using
 //   (r^2+b^2)^-3/2 = rsqrt(r^2+b^2)^3          (bulge)
 //   aR * x / R     = -GM x / D^3                 (disk, the R of the radial force cancels)
+//   az(disk)       = -GM z (a + s) / (s D^3), s = sqrt(z^2 + b^2): (a + s) / s = 1 + a / s
 //   x^g / (1 + x^(g-1)) = x p / (1 + p), p = x^(g-1) = x * x^(g-2)   (halo)
-// Mathematically identical; the last bits differ from glibc's as any libm's do.
+// Mathematically identical; the last bits differ from glibc's as any libm's do.  62 FP64 operations.
 __device__ __forceinline__ void mw_accel(double x, double y, double z, double &ax, double &ay, double &az) {
     const double R2 = fma(x, x, y * y);
     const double r2 = fma(z, z, R2);
-    const double ib = rsqrt(r2 + kBulgeB2);
-    const double fb = -kBulgeGM * (ib * ib * ib);
+    const double ib = rsqrt_h3(r2 + kBulgeB2);
     const double zb2 = fma(z, z, kDiskB2);
-    const double iz = rsqrt(zb2);
+    const double iz = rsqrt_h3(zb2);
     const double s = fma(zb2, iz, kDiskA);                      // a + sqrt(z^2 + b^2)
-    const double iD = rsqrt(fma(s, s, R2));
+    const double iD = rsqrt_h3(fma(s, s, R2));
     const double fd = -kDiskGM * (iD * iD * iD);
-    double ir = rsqrt(r2);
-    double r = r2 * ir;
-    if (!(r > 1e-12)) { r = 1e-12; ir = 1e12; }
+    double r, ir;
+    if (r2 > 1e-24) {
+        ir = rsqrt_h3(r2);
+        r = r2 * ir;
+    } else {
+        r = 1e-12;
+        ir = 1e12;
+    }
     const double xh = fmin(r, kHaloCut) * kHaloInvA;
     const double p = xh * halo_pow_a(xh);              // xh^(gamma - 1)
-    const double fh = -(kHaloGM * xh * p / (1.0 + p)) * (ir * ir * ir);
-    const double fr = fb + fh;
-    ax = (fr + fd) * x;
-    ay = (fr + fd) * y;
-    az = fma(fr, z, fd * z * s * iz);
+    const double q = p * rcp_h3(1.0 + p);
+    const double fh = -kHaloGM * xh * q * ((ir * ir) * ir);
+    const double fr = fma(-kBulgeGM * ib, ib * ib, fh);       // bulge + halo radial terms
+    const double g = fr + fd;
+    ax = g * x;
+    ay = g * y;
+    az = z * fma(fd * kDiskA, iz, g);
 }
 
 // One orbit: position, velocity and the acceleration carried over (one force evaluation per step).

@@ -98,39 +98,6 @@ __device__ __forceinline__ void sep32(const float4 &t0, const float4 &t1, const 
     m[2] = (t0.z - c0.z) + (t1.y - c1.y);
 }
 
-// Walks the points of one (star, cluster) pair in order, calling f(k, bound) for every point the cheap test
-// (point_skip32) keeps.
-template <class F>
-__device__ __forceinline__ void walk32(const ScreenTables &T, int s, int c, float cut, F &&f) {
-    const size_t NT = T.nt, NC = T.nc;
-    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
-    const float R2 = T.R2f[c];
-    const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
-    const size_t tstride = NT * 3, cstride = NC * 3;
-    float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
-    float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2);
-    float mcur[3];
-    sep32(t0, t1, c0, c1, mcur);
-    for (int k = 0; k < n; k++) {
-        const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
-        const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
-        const float lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
-        const bool more = k + 1 < n;
-        float mnext[3] = {mcur[0], mcur[1], mcur[2]};
-        if (more) {
-            const float4 *tn = tp + (size_t)(k + 1) * tstride, *cn = cp + (size_t)(k + 1) * cstride;
-            t0 = tn[0]; t1 = tn[1]; t2 = tn[2];
-            c0 = __ldg(cn); c1 = __ldg(cn + 1); c2 = __ldg(cn + 2);
-            sep32(t0, t1, c0, c1, mnext);
-        }
-        Bound b;
-        if (!point_skip32(St, Sc, R2, lmt, lmc, mcur, mnext, cut) &&
-            point_bound32(St, Sc, R2, lmt, lmc, mcur, mnext, more, cut, b))
-            f(k, b);
-        mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
-    }
-}
-
 // ---- K1: FP32 filter over every pair -------------------------------------------------------------------------
 // A point k can be the FP64 minimum of a kept pair only if lb_k < cut and lb_k <= min_j ub_j (otherwise some point
 // is certainly lower, or none is under the cut): the pair's candidates.  The walk keeps them in kCandSlots slots:
@@ -145,7 +112,7 @@ constexpr unsigned kNoPoint = 0xffffu;
 constexpr int kScanStars = 128;         // stars per block (one per thread)
 constexpr int kQueue = 64;              // per warp: points waiting for their full bounds
 
-// The bounds of point k of pair (s, c), as walk32 computes them: false when the point is skipped or rejected.
+// The full bounds of point k of pair (s, c), for a point the skip test did not settle: false when rejected.
 __device__ __forceinline__ bool point_at32(const ScreenTables &T, int s, int c, int k, float cut, Bound &b) {
     const size_t NT = T.nt, NC = T.nc;
     const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
@@ -404,23 +371,51 @@ __global__ void k_mx_ovf_emit(int np, const int *__restrict__ ovf, const int *__
 }
 
 // ---- K3: the overflowed pairs walked again: their candidate points, counted, then written --------------------------
-__global__ void k_mx_cand(ScreenTables T, float cut, int na, const int *__restrict__ A,
-                          const PossPair *__restrict__ P, int *__restrict__ cnt, const int *__restrict__ off,
-                          int2 *__restrict__ E) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= na) return;
+// One warp per pair, lane j taking points j, j + 32, ...: each point gets the scan's tests (the cheap skip test, then
+// the full bounds) and is a candidate when lb < cut and lb <= the pair's min ub.  A ballot numbers the candidates of
+// each 32 points, so they are written in point order.
+__device__ __forceinline__ bool point_cand32(const ScreenTables &T, int s, int c, int k, int n, float cut, float um) {
+    const size_t NT = T.nt, NC = T.nc;
+    const bool more = k + 1 < n;
+    const float4 *tp = T.t32 + ((size_t)k * NT + s) * 3, *cp = T.c32 + ((size_t)k * NC + c) * 3;
+    const float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
+    const float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2);
+    float m0[3], m1[3];
+    sep32(t0, t1, c0, c1, m0);
+    if (more) {
+        const float4 *tn = tp + NT * 3, *cn = cp + NC * 3;
+        sep32(tn[0], tn[1], __ldg(cn), __ldg(cn + 1), m1);
+    } else {
+        m1[0] = m0[0]; m1[1] = m0[1]; m1[2] = m0[2];
+    }
+    const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+    const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
+    const float R2 = T.R2f[c], lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
+    Bound b;
+    return !point_skip32(St, Sc, R2, lmt, lmc, m0, m1, cut) &&
+           point_bound32(St, Sc, R2, lmt, lmc, m0, m1, more, cut, b) && b.lb < cut && b.lb <= um;
+}
+
+constexpr int kCandWarps = 4;
+
+__global__ void __launch_bounds__(kCandWarps * 32) k_mx_cand(ScreenTables T, float cut, int na,
+                                                             const int *__restrict__ A,
+                                                             const PossPair *__restrict__ P, int *__restrict__ cnt,
+                                                             const int *__restrict__ off, int2 *__restrict__ E) {
+    const int i = blockIdx.x * kCandWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= na) return;                                          // the whole warp: uniform
     const int p = A[i];
     const PossPair r = P[p];
-    if (!E) {
-        int n = 0;
-        walk32(T, r.s, r.c, cut, [&](int, const Bound &b) { n += (b.lb < cut && b.lb <= r.ubmin); });
-        cnt[p] = n;
-    } else {
-        int e = off[p];
-        walk32(T, r.s, r.c, cut, [&](int k, const Bound &b) {
-            if (b.lb < cut && b.lb <= r.ubmin) E[e++] = make_int2(p, k);
-        });
+    const int n = T.ns < T.cn[r.c] ? T.ns : T.cn[r.c];
+    int e = E ? off[p] : 0;
+    for (int k0 = 0; k0 < n; k0 += 32) {
+        const int k = k0 + lane;
+        const bool hit = k < n && point_cand32(T, r.s, r.c, k, n, cut, r.ubmin);
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (E && hit) E[e + __popc(m & ((1u << lane) - 1u))] = make_int2(p, k);
+        e += __popc(m);
     }
+    if (!E && lane == 0) cnt[p] = e;
 }
 
 // ---- K4..K6: FP64 rechecks --------------------------------------------------------------------------------------
@@ -552,7 +547,8 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
             return rc;
         launches += 2 + 3;
         if (na > 0) {
-            k_mx_cand<<<(na + 127) / 128, 128, 0, st>>>(T, cutf, na, A, P, pc, nullptr, nullptr);
+            k_mx_cand<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, nullptr,
+                                                                                     nullptr);
             launches += 1;
         }
         if ((rc = exclusive_scan(st, np, pc, po, ppart, tot + 1, err))) return rc;
@@ -570,7 +566,7 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
         k_mx_list_emit<<<(np + 255) / 256, 256, 0, st>>>(np, P, po, E);
         launches += 1;
         if (na > 0) {
-            k_mx_cand<<<(na + 127) / 128, 128, 0, st>>>(T, cutf, na, A, P, pc, po, E);
+            k_mx_cand<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, po, E);
             launches += 1;
         }
         if (ne > 0) {

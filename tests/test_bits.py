@@ -61,3 +61,70 @@ def test_u64_to_f32_scaled_matches_the_cast():
         r = subprocess.run([exe], stdout=subprocess.PIPE, text=True)
     assert r.returncode == 0, r.stdout
     assert "bad 0" in r.stdout
+
+
+REFINE = r"""
+#include <cmath>
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+#include "pgx_bits.cuh"
+static uint64_t sm = 777;
+static uint64_t next() {
+    uint64_t z = (sm += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+static double uni() { return (double)(next() >> 11) * 0x1p-53; }
+// the FP32 unit's result, anywhere within 2 ulp of the correctly rounded value
+static float f32_result(double exact, int ulps) {
+    float f = (float)exact;
+    for (int i = 0; i < ulps; i++) f = std::nextafter(f, 0.f);
+    for (int i = 0; i < -ulps; i++) f = std::nextafter(f, 1e30f);
+    return f;
+}
+static double worst_rs = 0, worst_rc = 0;
+static double ulps(double got, long double want) {
+    const double w = (double)want;
+    const double u = std::nextafter(std::fabs(w), 1e300) - std::fabs(w);
+    return (double)(std::fabs((long double)got - want) / u);
+}
+static void one(double x) {
+    const uint32_t hi = pgx::f64_hi(x);
+    if (!pgx::seed_ok(hi)) return;
+    const float a = pgx::seed_arg(hi);
+    for (int k = -2; k <= 2; k++) {
+        const double rs = pgx::rsqrt_refine(x, pgx::widen_seed(f32_result(1.0 / std::sqrt((double)a), k)));
+        const double rc = pgx::rcp_refine(x, pgx::widen_seed(f32_result(1.0 / (double)a, k)));
+        const double e1 = ulps(rs, 1.0L / std::sqrt((long double)x)), e2 = ulps(rc, 1.0L / (long double)x);
+        if (e1 > worst_rs) worst_rs = e1;
+        if (e2 > worst_rc) worst_rc = e2;
+    }
+}
+int main() {
+    for (long i = 0; i < 2000000; i++) {
+        one(std::ldexp(1.0 + uni(), (int)(next() % 250) - 125));    // every binade of the valid range
+        one(1.0 + 9.0 * uni());                                     // 1 + p of the halo
+        one(std::exp(std::log(1e-3) + uni() * std::log(1e9)));      // squared radii of the force, kpc^2
+    }
+    for (int e = -125; e < 125; e++)                                 // binade edges
+        for (int d = -3; d <= 3; d++) one(std::nextafter(std::ldexp(1.0, e), d < 0 ? 0.0 : 1e300) * (1.0 + d * 1e-16));
+    std::printf("worst rsqrt %.3f ulp, worst rcp %.3f ulp\n", worst_rs, worst_rc);
+    return !(worst_rs <= 2.0 && worst_rc <= 2.0);
+}
+"""
+
+
+def test_force_reciprocals_within_two_ulp():
+    """The FP64 reciprocal square root and reciprocal of the force (pgx_bits.cuh: seed from an FP32 result anywhere
+    within 2 ulp, one third-order step) stay within 2 ulp of the exact values (80-bit host arithmetic) over every
+    binade of their range, the force's radii and the halo's 1 + p."""
+    inc = os.path.join(ot.REPO, "phygas_gb300", "csrc", "cuda")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "refine.cpp"), os.path.join(d, "refine")
+        open(src, "w").write(REFINE)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", inc, src, "-o", exe], check=True)
+        r = subprocess.run([exe], stdout=subprocess.PIPE, text=True)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout

@@ -91,6 +91,15 @@ int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int
                       double chi2_max, int precision,
                       int (*emit)(void *arg, int first, const PgxScreenRow *rows, long n), void *arg);
 void pgx_host_free(void *p);
+/* pgx_screen_chunks with each chunk's rows as the reference CLI's text lines (src/phygas_screen.c:60-61),
+ *   "%s %s %c %.3f %.3f %.2f %.2f %.4f %.4f %.2f %.3f %.3f\n" of target id, cluster name, cluster kind, chi2, t_myr,
+ *   d_nom_pc, sig_pc, p_r50, p_rtot, vrel_kms, cluster age16, cluster age84,
+ * formatted on the GPU byte for byte as the C library's printf formats them, and handed to
+ * emit(arg, first star of the chunk, text, bytes, rows).  cl[nc] are the resident table's clusters, in its order
+ * (nc must equal the table's count): the names, kinds and ages of the lines. */
+int pgx_screen_chunks_text(PgxContext *ctx, const PhTarget *t, int nt, const PhCluster *cl, int nc, int chunk,
+                           int n_samp, int threads, double tmax, double chi2_max, int precision,
+                           int (*emit)(void *arg, int first, const char *text, size_t bytes, long n_rows), void *arg);
 
 /* Host draws for the records API (reference ph_lin_target_init / the draws of ph_lin_cluster, src/phygas.c:274-344,
  * seeds ph_seed("lin", id)), on `threads` host threads (<= 0: all cores). */

@@ -104,6 +104,8 @@ SIGNATURES = [
     ("pgx_screen_chunks", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                     C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     ("pgx_host_free", None, [C.c_void_p]),
+    ("pgx_screen_chunks_text", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, _P(PhCluster), C.c_int, C.c_int, C.c_int,
+                                         C.c_int, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     ("pgx_draw_targets", C.c_int, [_P(PhTarget), C.c_int, C.c_int, C.c_int, _D, _D, _U64]),
     ("pgx_draw_clusters", C.c_int, [_P(PhCluster), C.c_int, C.c_int, C.c_int, _D, _D]),
     ("pgx_seed_prefix", C.c_uint64, [C.c_char_p]),
@@ -335,6 +337,29 @@ class Context:
             raise err[0]
         self._check(rc, "pgx_screen_chunks")
 
+    def screen_chunks_text(self, targets, clusters, chunk, tmax, emit, chi2_max=25.0, precision=PGX_MIXED, n_samp=64,
+                           threads=0):
+        """pgx_screen_chunks_text: as screen_chunks, each chunk's rows as the reference CLI's text lines formatted on
+        the GPU; emit(first_star, text, n_rows) gets a memoryview of the chunk's text (valid during the call).
+        `clusters` are the resident table's clusters, in its order."""
+        targets, clusters = as_array(targets, PhTarget), as_array(clusters, PhCluster)
+        err = []
+
+        def cb(_arg, first, ptr, nbytes, n):
+            try:
+                view = memoryview((C.c_char * nbytes).from_address(ptr)).cast("B") if nbytes else memoryview(b"")
+                emit(first, view, n)
+                return 0
+            except Exception as e:           # stop the run, re-raise after it
+                err.append(e)
+                return 1
+        fn = TEXT_FN(cb)
+        rc = lib().pgx_screen_chunks_text(self.h, targets, len(targets), clusters, len(clusters), chunk, n_samp,
+                                          threads, tmax, chi2_max, precision, C.cast(fn, C.c_void_p), None)
+        if err:
+            raise err[0]
+        self._check(rc, "pgx_screen_chunks_text")
+
     def stage(self, ps0, sig, prefix):
         self._keep = (np.ascontiguousarray(ps0, np.float64), np.ascontiguousarray(sig, np.float64),
                       np.ascontiguousarray(prefix, np.uint64))
@@ -389,6 +414,7 @@ def pair_shapes():
 
 
 EMIT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_long)
+TEXT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_long)
 
 
 class HostRows:

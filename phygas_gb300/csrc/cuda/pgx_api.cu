@@ -21,6 +21,7 @@
 #include "phygas_gb300.h"
 #include "pgx_kernels.h"
 #include "pgx_mixed.h"
+#include "pgx_text.h"
 #include "../host/ph_host.h"
 
 static_assert(sizeof(pgx::PhResultDev) == sizeof(PhResult), "PhResult layout");
@@ -51,10 +52,13 @@ struct PgxContext {
     Buf s_ps0, s_sig21, s_prefix;
     Buf opos, ovel, t64, t32, tlm;
     Buf chi2T, kbT, sbT, cnt, off, total, kept, fin, rows;
-    // pgx_screen_chunks: two chunks' rows on the device and in page-locked host memory, reused across calls
+    // pgx_screen_chunks(_text): two chunks' rows or text on the device and in page-locked host memory, reused
+    // across calls, and the labels of the text lines
     Buf rows_b[2];
-    PgxScreenRow *h_rows[2] = {};
-    long h_cap[2] = {};
+    char *h_buf[2] = {};
+    size_t h_cap[2] = {};
+    Buf lab_ids, lab_names, lab_kinds, lab_age16, lab_age84;
+    pgx::TextBufs text_bufs;
     pgx::MixedBufs mixed;
     long n_rows = 0;
     // pair Monte Carlo
@@ -209,11 +213,13 @@ void pgx_close(PgxContext *ctx) {
                    &ctx->p_off, &ctx->p_ps, &ctx->p_steps, &ctx->p_dt, &ctx->p_r50, &ctx->p_rt, &ctx->p_items,
                    &ctx->p_q, &ctx->p_done, &ctx->p_cres, &ctx->p_res, &ctx->p_params, &ctx->x_ps0, &ctx->x_sig21,
                    &ctx->x_npts,
-                   &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32, &ctx->rows_b[0], &ctx->rows_b[1]};
+                   &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32, &ctx->rows_b[0], &ctx->rows_b[1],
+                   &ctx->lab_ids, &ctx->lab_names, &ctx->lab_kinds, &ctx->lab_age16, &ctx->lab_age84};
     for (Buf *b : bufs)
         if (b->p) cudaFree(b->p);
-    for (auto *h : ctx->h_rows)
+    for (auto *h : ctx->h_buf)
         if (h) cudaFreeHost(h);
+    pgx::text_free(ctx->text_bufs);
     pgx::mixed_free(ctx->mixed);
     for (auto &g : ctx->mc_exec)
         if (g) cudaGraphExecDestroy(g);
@@ -594,34 +600,43 @@ int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *si
     return pgx_screen_fetch(ctx, rows, n);
 }
 
-int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n_samp, int threads, double tmax,
-                      double cut, int precision, int (*emit)(void *arg, int first, const PgxScreenRow *rows, long n),
-                      void *arg) {
-    if (!ctx) return PGX_E_ARG;
-    if (nt < 0 || (nt > 0 && !t) || chunk <= 0 || chunk > (1 << 20) || n_samp < 0 || !emit)
-        return fail(ctx, PGX_E_ARG, "pgx_screen_chunks: bad args");
-    if (nt == 0) return 0;
+}  // extern "C"
+
+namespace {
+// Rows or text out of the chunk pipeline (pgx_screen_chunks, pgx_screen_chunks_text).
+struct ChunkOut {
+    int (*rows)(void *arg, int first, const PgxScreenRow *rows, long n) = nullptr;
+    int (*text)(void *arg, int first, const char *text, size_t bytes, long n_rows) = nullptr;
+    void *arg = nullptr;
+};
+
+// Three stages run at once: the host draws of chunk c + 1 (a helper thread), the GPU work of chunk c (a worker
+// thread: stage, exec, then the rows copied into device slot c % 2 -- or formatted there as text -- and from there
+// to page-locked host memory on a second stream), and the output of chunk c - 1 on the calling thread.  Slot s is
+// reused for chunk c + 2 only after the output of chunk c has returned.
+int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n_samp, int threads, double tmax,
+                    double cut, int precision, const ChunkOut &out) {
+    const bool text = out.text != nullptr;
     CK(cudaSetDevice(ctx->device));
     const int th = threads > 0 ? threads : pgh_default_threads();
     const int nch = (nt + chunk - 1) / chunk;
-    // Three stages run at once: the host draws of chunk c + 1 (a helper thread), the GPU work of chunk c (a worker
-    // thread: stage, exec, then a device copy of its rows into slot c % 2 and their copy to page-locked host memory
-    // on a second stream), and emit(c - 1) on the calling thread.  Slot s is reused for chunk c + 2 only after
-    // emit(c) has returned.
     struct Draw {
         std::vector<double> ps0, sig;
         std::vector<uint64_t> pre;
+        std::vector<char> ids;
         int first = 0, n = 0;
     } buf[2];
     for (auto &b : buf) {
         b.ps0.resize((size_t)6 * chunk);
         b.sig.resize((size_t)36 * chunk);
         b.pre.resize(chunk);
+        if (text) b.ids.resize((size_t)40 * chunk);
     }
     auto draw = [&](int c, Draw &b) {
         b.first = c * chunk;
         b.n = std::min(chunk, nt - b.first);
         pgh_draw_targets(t + b.first, b.n, n_samp, th, b.ps0.data(), b.sig.data(), b.pre.data());
+        for (int i = 0; text && i < b.n; i++) memcpy(&b.ids[(size_t)40 * i], t[b.first + i].id, 40);
     };
     cudaStream_t cs = nullptr;
     cudaEvent_t ev_rows[2] = {}, ev_host[2] = {};
@@ -630,16 +645,28 @@ int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int
     for (int i = 0; i < 2 && rc == 0; i++) {
         if (cudaEventCreateWithFlags(&ev_rows[i], cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_host[i], cudaEventDisableTiming) != cudaSuccess)
-            rc = fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: events");
+            rc = fail(ctx, PGX_E_CUDA, "screen chunks: events");
     }
     std::mutex mu;
     std::condition_variable cv;
     int produced = 0, consumed = 0, worker_rc = 0;
     bool worker_done = false, stop = false;
     long n_of[2] = {0, 0};
+    size_t bytes_of[2] = {0, 0};
     int first_of[2] = {0, 0};
+    // host buffer of slot s with room for `bytes` (page-locked, grown by a quarter)
+    auto host_room = [&](int s, size_t bytes) {
+        if (ctx->h_cap[s] >= bytes) return 0;
+        pgx_host_free(ctx->h_buf[s]);
+        ctx->h_cap[s] = 0;
+        const size_t cap = bytes + bytes / 4 + 65536;
+        ctx->h_buf[s] = (char *)pgx_host_alloc(cap);
+        if (!ctx->h_buf[s]) return fail(ctx, PGX_E_NOMEM, "screen chunks: %zu bytes of page-locked memory", cap);
+        ctx->h_cap[s] = cap;
+        return 0;
+    };
     auto worker = [&]() {
-        int wrc = cudaSetDevice(ctx->device) == cudaSuccess ? 0 : fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: device");
+        int wrc = cudaSetDevice(ctx->device) == cudaSuccess ? 0 : fail(ctx, PGX_E_CUDA, "screen chunks: device");
         if (wrc == 0) draw(0, buf[0]);
         for (int c = 0; c < nch && wrc == 0; c++) {
             Draw &cur = buf[c & 1];
@@ -654,31 +681,50 @@ int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int
                 cv.wait(lk, [&] { return consumed >= c - 1 || stop; });
                 if (stop) wrc = -1;
             }
-            if (wrc == 0 && ctx->h_cap[slot] < n) {
-                pgx_host_free(ctx->h_rows[slot]);
-                ctx->h_cap[slot] = 0;
-                const long cap = n + n / 4 + 4096;
-                ctx->h_rows[slot] = (PgxScreenRow *)pgx_host_alloc(sizeof(PgxScreenRow) * (size_t)cap);
-                if (ctx->h_rows[slot]) ctx->h_cap[slot] = cap;
-                else wrc = fail(ctx, PGX_E_NOMEM, "pgx_screen_chunks: %ld page-locked rows", cap);
+            size_t bytes = (size_t)n * sizeof(PgxScreenRow);
+            Buf &dev = ctx->rows_b[slot];
+            if (wrc == 0 && text && n > 0) {
+                // the chunk's star ids, then the lines formatted into the device slot
+                wrc = ensure(ctx, ctx->lab_ids, (size_t)40 * cur.n);
+                if (wrc == 0 && cudaMemcpyAsync(ctx->lab_ids.p, cur.ids.data(), (size_t)40 * cur.n,
+                                                cudaMemcpyHostToDevice, ctx->st) != cudaSuccess)
+                    wrc = fail(ctx, PGX_E_CUDA, "screen chunks: star ids");
+                const pgx::TextLabels L = {P<char>(ctx->lab_ids), P<char>(ctx->lab_names), P<char>(ctx->lab_kinds),
+                                           P<double>(ctx->lab_age16), P<double>(ctx->lab_age84)};
+                for (int attempt = 0; wrc == 0 && attempt < 2; attempt++) {
+                    std::string err;
+                    size_t need = 0;
+                    const int frc = pgx::format_rows(ctx->st, n, P<pgx::ScreenRowDev>(ctx->rows), L, ctx->text_bufs,
+                                                     P<char>(dev), dev.cap, &need, err);
+                    if (frc == 0) {
+                        bytes = need;
+                        break;
+                    }
+                    if (frc != PGX_E_LIMIT || attempt == 1) wrc = fail(ctx, frc, "row text: %s", err.c_str());
+                    else wrc = ensure(ctx, dev, need);
+                }
+            } else if (wrc == 0 && n > 0) {
+                wrc = ensure(ctx, dev, bytes);
+                if (wrc == 0 && cudaMemcpyAsync(dev.p, ctx->rows.p, bytes, cudaMemcpyDeviceToDevice, ctx->st) !=
+                                    cudaSuccess)
+                    wrc = fail(ctx, PGX_E_CUDA, "screen chunks: row copy");
             }
-            const size_t bytes = (size_t)n * sizeof(PgxScreenRow);
-            if (wrc == 0 && n > 0) wrc = ensure(ctx, ctx->rows_b[slot], bytes);
+            if (wrc == 0) wrc = host_room(slot, bytes);
             if (wrc == 0 && n > 0) {
-                const cudaError_t e[4] = {
-                    cudaMemcpyAsync(ctx->rows_b[slot].p, ctx->rows.p, bytes, cudaMemcpyDeviceToDevice, ctx->st),
-                    cudaEventRecord(ev_rows[slot], ctx->st), cudaStreamWaitEvent(cs, ev_rows[slot], 0),
-                    cudaMemcpyAsync(ctx->h_rows[slot], ctx->rows_b[slot].p, bytes, cudaMemcpyDeviceToHost, cs)};
+                const cudaError_t e[3] = {cudaEventRecord(ev_rows[slot], ctx->st),
+                                          cudaStreamWaitEvent(cs, ev_rows[slot], 0),
+                                          cudaMemcpyAsync(ctx->h_buf[slot], dev.p, bytes, cudaMemcpyDeviceToHost, cs)};
                 for (cudaError_t x : e)
                     if (x != cudaSuccess && wrc == 0)
-                        wrc = fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: row copy: %s", cudaGetErrorString(x));
+                        wrc = fail(ctx, PGX_E_CUDA, "screen chunks: copy to the host: %s", cudaGetErrorString(x));
             }
             if (wrc == 0 && cudaEventRecord(ev_host[slot], cs) != cudaSuccess)
-                wrc = fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: event record");
+                wrc = fail(ctx, PGX_E_CUDA, "screen chunks: event record");
             if (ahead.joinable()) ahead.join();
             if (wrc == 0) {
                 std::lock_guard<std::mutex> lk(mu);
                 n_of[slot] = n;
+                bytes_of[slot] = n > 0 ? bytes : 0;
                 first_of[slot] = cur.first;
                 produced = c + 1;
                 cv.notify_all();
@@ -693,19 +739,21 @@ int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int
     if (rc == 0) gpu = std::thread(worker);
     for (int c = 0; c < nch && rc == 0; c++) {
         long n;
+        size_t bytes;
         int first;
         {
             std::unique_lock<std::mutex> lk(mu);
             cv.wait(lk, [&] { return produced > c || worker_done; });
             if (produced <= c) break;                     // the worker stopped: its code is returned below
             n = n_of[c & 1];
+            bytes = bytes_of[c & 1];
             first = first_of[c & 1];
         }
-        if (cudaEventSynchronize(ev_host[c & 1]) != cudaSuccess) {
-            rc = PGX_E_CUDA;
-        } else if (emit(arg, first, ctx->h_rows[c & 1], n)) {
+        const char *h = ctx->h_buf[c & 1];
+        if (cudaEventSynchronize(ev_host[c & 1]) != cudaSuccess) rc = PGX_E_CUDA;
+        else if (text ? out.text(out.arg, first, h, bytes, n)
+                      : out.rows(out.arg, first, reinterpret_cast<const PgxScreenRow *>(h), n))
             rc = PGX_E_ARG;
-        }
         std::lock_guard<std::mutex> lk(mu);
         consumed = c + 1;
         if (rc) stop = true;
@@ -713,8 +761,8 @@ int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int
     }
     if (gpu.joinable()) gpu.join();
     // codes set here, after the worker has ended, so that the message is this function's
-    if (rc == PGX_E_ARG) rc = fail(ctx, PGX_E_ARG, "pgx_screen_chunks: emit stopped");
-    else if (rc == PGX_E_CUDA) rc = fail(ctx, PGX_E_CUDA, "pgx_screen_chunks: row copy failed");
+    if (rc == PGX_E_ARG) rc = fail(ctx, PGX_E_ARG, "screen chunks: the output callback stopped the run");
+    else if (rc == PGX_E_CUDA) rc = fail(ctx, PGX_E_CUDA, "screen chunks: copy to the host failed");
     else if (rc == 0 && worker_rc > 0) rc = worker_rc;
     cudaStreamSynchronize(cs);
     for (int i = 0; i < 2; i++) {
@@ -723,6 +771,53 @@ int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int
     }
     cudaStreamDestroy(cs);
     return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int pgx_screen_chunks(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n_samp, int threads, double tmax,
+                      double cut, int precision, int (*emit)(void *arg, int first, const PgxScreenRow *rows, long n),
+                      void *arg) {
+    if (!ctx) return PGX_E_ARG;
+    if (nt < 0 || (nt > 0 && !t) || chunk <= 0 || chunk > (1 << 20) || n_samp < 0 || !emit)
+        return fail(ctx, PGX_E_ARG, "pgx_screen_chunks: bad args");
+    if (nt == 0) return 0;
+    ChunkOut out;
+    out.rows = emit;
+    out.arg = arg;
+    return screen_pipeline(ctx, t, nt, chunk, n_samp, threads, tmax, cut, precision, out);
+}
+
+int pgx_screen_chunks_text(PgxContext *ctx, const PhTarget *t, int nt, const PhCluster *cl, int nc, int chunk,
+                           int n_samp, int threads, double tmax, double cut, int precision,
+                           int (*emit)(void *arg, int first, const char *text, size_t bytes, long n_rows), void *arg) {
+    if (!ctx) return PGX_E_ARG;
+    if (nt < 0 || (nt > 0 && !t) || !cl || nc != ctx->nc || chunk <= 0 || chunk > (1 << 20) || n_samp < 0 || !emit)
+        return fail(ctx, PGX_E_ARG, "pgx_screen_chunks_text: bad args (%d clusters given, %d resident)", nc, ctx->nc);
+    if (nt == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    // the clusters' labels: name, kind, age16, age84
+    std::vector<char> names((size_t)40 * nc), kinds(nc);
+    std::vector<double> a16(nc), a84(nc);
+    for (int i = 0; i < nc; i++) {
+        memcpy(&names[(size_t)40 * i], cl[i].name, 40);
+        kinds[i] = cl[i].kind;
+        a16[i] = cl[i].age16;
+        a84[i] = cl[i].age84;
+    }
+    RET(ensure(ctx, ctx->lab_names, names.size()));
+    RET(ensure(ctx, ctx->lab_kinds, kinds.size()));
+    RET(ensure(ctx, ctx->lab_age16, (size_t)8 * nc));
+    RET(ensure(ctx, ctx->lab_age84, (size_t)8 * nc));
+    CK(cudaMemcpy(ctx->lab_names.p, names.data(), names.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->lab_kinds.p, kinds.data(), kinds.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->lab_age16.p, a16.data(), (size_t)8 * nc, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->lab_age84.p, a84.data(), (size_t)8 * nc, cudaMemcpyHostToDevice));
+    ChunkOut out;
+    out.text = emit;
+    out.arg = arg;
+    return screen_pipeline(ctx, t, nt, chunk, n_samp, threads, tmax, cut, precision, out);
 }
 
 void *pgx_host_alloc(size_t bytes) {

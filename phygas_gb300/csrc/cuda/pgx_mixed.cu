@@ -29,7 +29,6 @@
 
 namespace pgx {
 
-namespace {
 int grow(DevBuf &b, size_t bytes, std::string &err) {
     if (bytes == 0) bytes = 16;
     if (b.cap >= bytes) return 0;
@@ -49,6 +48,8 @@ int check(cudaError_t e, std::string &err, const char *what) {
     err = std::string(what) + ": " + cudaGetErrorString(e);
     return PGX_E_CUDA;
 }
+
+namespace {
 template <class T> T *Pb(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
 }  // namespace
 

@@ -18,6 +18,11 @@ struct MixedBufs {
 };
 
 void mixed_free(MixedBufs &m);
+// a device buffer of at least `bytes` (grown by a quarter more when it has to grow); a CUDA status as a PGX code
+int grow(DevBuf &b, size_t bytes, std::string &err);
+int check(cudaError_t e, std::string &err, const char *what);
+// exclusive scan of n ints into out, the total into *total (device); part: n / 1024 + 2 ints of scratch
+int exclusive_scan(cudaStream_t st, int n, const int *in, int *out, int *part, int *total, std::string &err);
 // slot-ordered tracks (longest first) -> cluster-ordered table columns
 int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, const double *t64_slot,
                    const float4 *t32_slot, const float *lm_slot, double *c64, float4 *c32, float *clm, MixedBufs &m);

@@ -4,9 +4,10 @@
  *
  * Same arguments, same stdout rows in the same order (star, then cluster; every pair with chi2 < chi2_max):
  *   target cluster kind chi2 t_myr d_nom_pc sig_pc p_r50 p_rtot vrel_kms age16 age84
- * Progress on stderr.  The draws run on all host cores; the orbits, the scan and the 512-draw probabilities on the
- * GPU (libphygas_gb300).  PHYGAS_PRECISION=fp64 selects the plain FP64 screen instead of the default mixed-precision
- * one (their rows are identical); PHYGAS_CHUNK sets the stars per GPU chunk (default 20000).
+ * Progress on stderr.  The draws run on all host cores; the orbits, the scan, the 512-draw probabilities and the
+ * formatting of the lines on the GPU (libphygas_gb300).  PHYGAS_PRECISION=fp64 selects the plain FP64 screen
+ * instead of the default mixed-precision one (their rows are identical); PHYGAS_CHUNK sets the stars per GPU chunk
+ * (default 20000).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -21,25 +22,15 @@ static double now_s(void) {
 }
 
 typedef struct {
-    const PhTarget *tg;
-    const PhCluster *cl;
     long kept;
     double t0;
-    int done;
 } Printer;
 
-/* one chunk's rows, in (star, cluster) order */
-static int print_rows(void *arg, int first, const PgxScreenRow *rows, long n) {
+/* one chunk's lines, in (star, cluster) order, formatted on the GPU (pgx_screen_chunks_text) */
+static int print_text(void *arg, int first, const char *text, size_t bytes, long n) {
     Printer *P = arg;
-    for (long h = 0; h < n; h++) {
-        const PgxScreenRow *r = &rows[h];
-        const PhTarget *t = &P->tg[first + r->star];
-        const PhCluster *c = &P->cl[r->cluster];
-        printf("%s %s %c %.3f %.3f %.2f %.2f %.4f %.4f %.2f %.3f %.3f\n", t->id, c->name, c->kind, r->chi2, r->t_myr,
-               r->d_nom_pc, r->sig_pc, r->p_r50, r->p_rtot, r->vrel_kms, c->age16, c->age84);
-    }
+    if (bytes && fwrite(text, 1, bytes, stdout) != bytes) return 1;
     P->kept += n;
-    P->done = first;
     fprintf(stderr, "%d+ targets, %ld pairs kept, %.1f s\n", first, P->kept, now_s() - P->t0);
     return 0;
 }
@@ -93,9 +84,9 @@ int main(int argc, char **argv) {
         fprintf(stderr, "control run: velocities taken from the star %d lines away\n", nt / 2);
     }
     const int chunk = env_int("PHYGAS_CHUNK", 20000);
-    Printer P = {tg, cl, 0, now_s(), 0};
-    /* the draws of the next chunk run while the GPU screens this one (pgx_screen_chunks) */
-    if (pgx_screen_chunks(ctx, tg, nt, chunk, n_samp, 0, tmax, chi2_max, precision, print_rows, &P)) {
+    Printer P = {0, now_s()};
+    /* the draws of the next chunk run while the GPU screens this one and the previous chunk's lines are written */
+    if (pgx_screen_chunks_text(ctx, tg, nt, cl, nc, chunk, n_samp, 0, tmax, chi2_max, precision, print_text, &P)) {
         fprintf(stderr, "phygas_screen: screen: %s\n", pgx_last_error(ctx));
         return 1;
     }

@@ -128,3 +128,71 @@ def test_force_reciprocals_within_two_ulp():
         r = subprocess.run([exe], stdout=subprocess.PIPE, text=True)
     print(r.stdout)
     assert r.returncode == 0, r.stdout
+
+
+FMT = r"""
+#include <cmath>
+#include <cfloat>
+#include <initializer_list>
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+#include "pgx_fmt.cuh"
+static uint64_t sm = 99;
+static uint64_t next() {
+    uint64_t z = (sm += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+static long bad = 0, tested = 0;
+static void check(double x, int nd) {
+    char want[400], got[400];
+    snprintf(want, sizeof want, "%.*f", nd, x);
+    const int n = pgx::fmt_fixed(got, x, nd);
+    got[n] = 0;
+    tested++;
+    if (strcmp(want, got) || pgx::fmt_fixed(nullptr, x, nd) != n)
+        if (bad++ < 10) printf("x=%a nd=%d want %s got %s\n", x, nd, want, got);
+}
+static double from_bits(uint64_t b) { double d; memcpy(&d, &b, 8); return d; }
+int main() {
+    for (int nd : {0, 1, 2, 3, 4, 6, 9}) {
+        for (double x : {0.0, -0.0, 0.5, 1.5, 2.5, 0.125, 0.375, 0.0625, 1e-4, 5e-5, 9.9995, 99.995, -0.0004,
+                         -0.0005, DBL_MAX, -DBL_MAX, DBL_MIN, 4.9e-324, (double)INFINITY, -(double)INFINITY,
+                         (double)NAN, -(double)NAN, 9.2e14, 1e20, 1.8446744073709552e19})
+            check(x, nd);
+        for (int e = -1074; e <= 1023; e++) {          // every binade, and its neighbours
+            const double p = ldexp(1.0, e);
+            check(p, nd); check(-p, nd); check(nextafter(p, 0.0), nd); check(nextafter(p, 1e300), nd);
+        }
+        for (int k = 0; k < 20000; k++) {              // exact ties: odd multiples of 2^-j
+            const double x = ldexp((double)(2 * (next() % 100000) + 1), -(int)(1 + next() % 20));
+            check(x, nd); check(-x, nd);
+        }
+        for (long i = 0; i < 150000; i++) {
+            check(from_bits(next()), nd);              // any bit pattern
+            const double u = (double)(next() >> 11) * 0x1p-53;
+            check(u * 1000.0, nd);                      // the rows' magnitudes
+            check(ldexp(u, (int)(next() % 80) - 40), nd);
+            check(std::round(u * 1e6) / 1e4, nd);       // near decimal boundaries
+        }
+    }
+    printf("tested %ld bad %ld\n", tested, bad);
+    return bad != 0;
+}
+"""
+
+
+def test_fixed_point_text_matches_printf():
+    """The row writer's %.Nf (pgx_fmt.cuh, integer arithmetic only, the same code the GPU runs) gives the C
+    library's printf text byte for byte: every binade from subnormals to DBL_MAX, exact ties (round half to even),
+    negative values that round to zero, infinities and NaNs, random bit patterns and row-sized values."""
+    inc = os.path.join(ot.REPO, "phygas_gb300", "csrc", "cuda")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "fmt.cpp"), os.path.join(d, "fmt")
+        open(src, "w").write(FMT)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", inc, src, "-o", exe], check=True)
+        r = subprocess.run([exe], stdout=subprocess.PIPE, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "bad 0" in r.stdout

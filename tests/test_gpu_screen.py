@@ -170,3 +170,35 @@ def test_screen_chunks_pipeline_matches_one_screen(ctx, golden):
         ctx.screen_chunks(stars, 50, tmax, stop)
     assert calls == [0]
     assert len(ctx.screen(*pg.draw_targets(stars[:40]), tmax)) >= 0      # the context is still usable
+
+
+def _lines(rows, stars, clusters, first=0):
+    """the reference CLI's line for each row, formatted by Python (exact decimal rounding, as printf)"""
+    out = []
+    for r in rows:
+        t, c = stars[first + int(r["star"])], clusters[int(r["cluster"])]
+        out.append("%s %s %s %.3f %.3f %.2f %.2f %.4f %.4f %.2f %.3f %.3f\n" % (
+            t.id.decode(), c.name.decode(), c.kind.decode(), r["chi2"], r["t_myr"], r["d_nom_pc"], r["sig_pc"],
+            r["p_r50"], r["p_rtot"], r["vrel_kms"], c.age16, c.age84))
+    return "".join(out).encode()
+
+
+def test_screen_chunks_text_is_printf_of_the_rows(ctx, golden):
+    """pgx_screen_chunks_text: each chunk's lines, formatted on the GPU, are byte for byte the printf text of the
+    rows pgx_screen returns (Python's %-formatting rounds the exact binary value as the C library does)."""
+    clusters, stars = pg.read_clusters(golden["clusters"]), pg.read_targets(golden["screen"])[:300]
+    ctx.set_clusters(clusters)
+    tmax = max(c.tmax_myr for c in clusters)
+    rows = ctx.screen(*pg.draw_targets(stars), tmax)
+    want = _lines(rows, stars, clusters)
+    for chunk in (300, 64):
+        got, counts = [], []
+
+        def emit(first, text, n):
+            got.append(bytes(text))
+            counts.append(n)
+        ctx.screen_chunks_text(stars, clusters, chunk, tmax, emit)
+        assert sum(counts) == len(rows)
+        assert b"".join(got) == want, chunk
+    with pytest.raises(pg.GpuError):
+        ctx.screen_chunks_text(stars, clusters[:10], 64, tmax, lambda *a: None)     # not the resident table

@@ -35,12 +35,12 @@ sys.path.insert(0, REPO)
 N_STARS, N_CLUSTERS, SEED = 20000, 4087, 1001
 CHI2_MAX, N_SAMP, R_KERNEL = 25.0, 64, 2.0
 # FP64 flops of one body step (one kick-drift-kick step of one orbit, its force evaluation included), from the
-# executed FP64 instructions of k_stm_orbits per body step: 41.0 DFMA + 4.0 DADD + 31.0 DMUL (ncu sass op counters of
-# `python -m phygas_gb300.run_screen --stars 2000`, FMA = 2 flops)
-FLOPS_PER_BODY_STEP = 117.0
-# the same for one clone-step of the pair Monte Carlo (two body steps and the segment test), from k_pair_mc_t on
-# 1 pulsar x 64 clusters x 200 clones x 400 steps: 89.6 DFMA + 14.3 DADD + 70.8 DMUL per clone-step
-FLOPS_PER_CLONE_STEP = 264.3
+# executed FP64 instructions of k_stm_orbits per body step: 36.0 DFMA + 3.0 DADD + 29.0 DMUL (ncu sass op counters of
+# the 2,000-star screen of `python -m phygas_gb300.run_pairs`, FMA = 2 flops)
+FLOPS_PER_BODY_STEP = 104.0
+# the same for one clone-step of the pair Monte Carlo (two body steps and the segment test), from k_pair_mc_t on the
+# batch of `python -m phygas_gb300.run_pairs` (4,052 pairs, 1.49e9 clone-steps): 79.0 DFMA + 12.2 DADD + 65.5 DMUL
+FLOPS_PER_CLONE_STEP = 235.7
 # DRAM traffic of one k_stm_orbits launch on this chunk (dram__bytes_read.sum + dram__bytes_write.sum from one ncu
 # capture of `python -m phygas_gb300.run_screen --stars 20000`): 4.9 MB read + 711.8 MB of orbit output written
 ORBIT_TRAFFIC_BYTES = 716.7e6
@@ -248,6 +248,28 @@ SERVE_JOBS, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 20, 1.0, 3, 1004
 E2E_CHUNKS = 4
 
 
+def cli_measure(cp, tp, reps=2):
+    """The screen CLI end to end (process start, inputs read, cluster table, the pipelined chunks, the lines
+    formatted on the GPU and written to /dev/null): wall time, best of `reps`."""
+    import phygas_gb300 as pg
+    walls, err = [], ""
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        with open(os.devnull, "w") as dn:
+            r = subprocess.run([pg.SCREEN_CLI, cp, tp], stdout=dn, stderr=subprocess.PIPE, text=True)
+        walls.append(time.perf_counter() - t0)
+        err = r.stderr
+        if r.returncode:
+            raise RuntimeError("phygas_screen: %s" % err.strip()[-200:])
+    kept = 0
+    for line in err.splitlines():
+        if "pairs kept" in line:
+            kept = int(line.split(",")[1].split()[0])
+    return {"cmd": "phygas_screen clusters.txt stars.txt > /dev/null (%d stars x %d clusters)" % (N_STARS, N_CLUSTERS),
+            "wall_s": min(walls), "rows": kept, "pairs_per_s": N_STARS * N_CLUSTERS / min(walls),
+            "text": "lines formatted on the GPU (pgx_screen_chunks_text)"}
+
+
 def serving_measure(cp, tp):
     import phygas_gb300 as pg
     from phygas_gb300 import synth
@@ -412,6 +434,13 @@ def main():
         except Exception as e:          # reported beside the headline, not part of it
             log("pair Monte Carlo measurement failed: %s" % e)
 
+    cli = None
+    if rank == 0:
+        try:
+            cli = cli_measure(cp, tp)
+        except Exception as e:          # reported beside the headline, not part of it
+            log("cli measurement failed: %s" % e)
+
     serving = None
     if rank == 0 and not args.no_serve:
         try:
@@ -459,6 +488,7 @@ def main():
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
             "pair_mc": pair_mc,
+            "cli": cli,
             "serving": serving,
         }
         print(json.dumps(out))

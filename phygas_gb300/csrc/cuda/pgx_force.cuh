@@ -7,19 +7,20 @@
 namespace pgx {
 
 // x^(gamma - 1) of the halo term as x * x^a, a = (gamma - 1) - 1 = 0.02: x = 2^e m, m in [1, 2); m in sub-interval
-// j of 64 with centre c_j, m = c_j (1 + t), |t| <= 1/128; x^a = 2^(a e) c_j^a (1 + t)^a with the first two from
-// tables and (1 + t)^a by its binomial series to t^6 (the next term is below 5e-18 relative).  Ten FP64 operations
-// and a few integer ones, in place of a log and an exp (about 50 FP64-pipe slots on this GPU), and closer: each table
-// entry and the series are within a few ulp, where exp(a' ln x) inherits the log's absolute error times |a' ln x|.
-constexpr int kPow2Bias = 80, kPow2N = 96, kPowSub = 64, kPowTerms = 6;
+// j of 1024 with centre c_j, m = c_j (1 + t), |t| <= 2^-11; x^a = 2^(a e) c_j^a (1 + t)^a with the first two from
+// tables and (1 + t)^a by its binomial series to t^4 (the next term, |C(a, 5)| t^5 <= 0.0039 2^-55, is below 2^-63
+// relative).  Eight FP64 operations and a few integer ones, in place of a log and an exp (about 50 FP64-pipe slots
+// on this GPU), and closer: each table entry and the series are within a few ulp, where exp(a' ln x) inherits the
+// log's absolute error times |a' ln x|.
+constexpr int kPow2Bias = 80, kPow2N = 96, kPowSubLog = 10, kPowSub = 1 << kPowSubLog, kPowTerms = 4;
 static __device__ double g_halo_pow2[kPow2N];      // 2^(a e), e = i - kPow2Bias
-static __device__ double g_halo_powc[kPowSub];     // c_j^a, c_j = 1 + (2 j + 1) / 128
+static __device__ double g_halo_powc[kPowSub];     // c_j^a, c_j = 1 + (2 j + 1) / 2048
 static __device__ double g_halo_invc[kPowSub];     // 1 / c_j
 static __device__ double g_halo_coef[kPowTerms + 1];   // binomial coefficients C(a, n)
 
 // the tables (one thread per entry; launched once per device, before any kernel that integrates an orbit)
 __global__ void k_halo_tables() {
-    const int i = threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const double a = kHaloG1 - 1.0;
     if (i < kPow2N) g_halo_pow2[i] = exp2(a * (double)(i - kPow2Bias));
     if (i < kPowSub) {
@@ -35,13 +36,14 @@ __global__ void k_halo_tables() {
         }
     }
 }
+constexpr int kHaloTableThreads = kPowSub > kPow2N ? kPowSub : kPow2N;
 
 // x^a for x > 0 normal (here x in [8e-14, 8.4])
 __device__ __forceinline__ double halo_pow_a(double x) {
     const long long bits = __double_as_longlong(x);
     int e = (int)((bits >> 52) & 0x7ff) - 1023;
     e = e < -kPow2Bias ? -kPow2Bias : (e > kPow2N - 1 - kPow2Bias ? kPow2N - 1 - kPow2Bias : e);
-    const int j = (int)((bits >> 46) & (kPowSub - 1));
+    const int j = (int)((bits >> (52 - kPowSubLog)) & (kPowSub - 1));
     const double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
     const double t = fma(m, __ldg(&g_halo_invc[j]), -1.0);
     double s = __ldg(&g_halo_coef[kPowTerms]);
@@ -106,7 +108,9 @@ __device__ __forceinline__ void mw_accel(double x, double y, double z, double &a
 struct Orbit {
     double x, y, z, vx, vy, vz, ax, ay, az;
     __device__ __forceinline__ void init() { mw_accel(x, y, z, ax, ay, az); }
-    // kick-drift-kick leapfrog (reference body_step, src/phygas.c:91-96)
+    // kick-drift-kick leapfrog (reference body_step, src/phygas.c:91-96).  Two half kicks per step, as the reference
+    // rounds them: merging a step's closing kick with the next one's opening kick would save three FP64 operations
+    // but moves the last bits of the orbits enough to change printed digits of the reference's published rows.
     __device__ __forceinline__ void kdk(double dt, double h) {
         vx = fma(ax, h, vx); vy = fma(ay, h, vy); vz = fma(az, h, vz);
         x = fma(vx, dt, x); y = fma(vy, dt, y); z = fma(vz, dt, z);

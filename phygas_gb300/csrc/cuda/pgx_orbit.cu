@@ -729,7 +729,7 @@ int orbit_setup(int dev) {
     if (dev < 0 || dev >= 64) return 1;
     std::lock_guard<std::mutex> lk(mu);
     if (ready[dev]) return 0;
-    k_halo_tables<<<1, 128>>>();
+    k_halo_tables<<<1, kHaloTableThreads>>>();
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return 2;

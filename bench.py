@@ -245,7 +245,7 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
 # once with the plain FP64 screen, the same stream both times.
 SERVE_JOBS, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 20, 1.0, 3, 1004
 # chunks of the benchmark's stars per end-to-end run (the pipeline's fill is spread over them)
-E2E_CHUNKS = 4
+E2E_CHUNKS = 8
 
 
 def cli_measure(cp, tp, reps=2):

@@ -13,7 +13,8 @@
 //                    Per pair: its candidate points -- those that can be the FP64 minimum of a kept pair
 //                    (LB_k < cut, LB_k <= min UB) -- in four slots, or "more than four".
 //   k_mx_count / k_mx_emit   stable compaction, per star, of the pairs that may be kept
-//   k_mx_list_*      the listed candidates written out; k_mx_cand walks the overflowed pairs again for theirs
+//   k_mx_list_*      the listed candidates written out; k_mx_cand walks the overflowed pairs again for theirs,
+//                    keeping up to 32 per pair for k_mx_cand_copy (k_mx_cand_big walks a pair with more a third time)
 //   k_mx_eval64      one thread per candidate point: the FP64 point chi2 (full warps on the scarce FP64 pipe)
 //   k_mx_best        per possible pair: FP64 argmin over its candidates (smallest value, first point of equals)
 //   k_mx_kept_*      stable compaction of the pairs under the cut
@@ -55,7 +56,7 @@ template <class T> T *Pb(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
 
 void mixed_free(MixedBufs &m) {
     DevBuf *all[] = {&m.order, &m.ub, &m.kmin, &m.flag, &m.cnt, &m.off, &m.total, &m.kept, &m.cand, &m.cand_off,
-                     &m.ent, &m.entq, &m.aux};
+                     &m.ent, &m.entq, &m.aux, &m.ovf};
     for (DevBuf *b : all)
         if (b->p) { cudaFree(b->p); b->p = nullptr; b->cap = 0; }
 }
@@ -371,7 +372,7 @@ __global__ void k_mx_ovf_emit(int np, const int *__restrict__ ovf, const int *__
     if (p < np && ovf[p]) A[off[p]] = p;
 }
 
-// ---- K3: the overflowed pairs walked again: their candidate points, counted, then written --------------------------
+// ---- K3: the overflowed pairs walked again for their candidate points, once -------------------------------------
 // One warp per pair, lane j taking points j, j + 32, ...: each point gets the scan's tests (the cheap skip test, then
 // the full bounds) and is a candidate when lb < cut and lb <= the pair's min ub.  A ballot numbers the candidates of
 // each 32 points, so they are written in point order.
@@ -398,25 +399,61 @@ __device__ __forceinline__ bool point_cand32(const ScreenTables &T, int s, int c
 }
 
 constexpr int kCandWarps = 4;
+constexpr int kCandCap = 32;            // candidates an overflowed pair keeps from its single walk
 
+// The walk: the candidates' point numbers into X[i][0, kCandCap), their count into cnt[p] (a pair with more is
+// walked again by k_mx_cand_big)
 __global__ void __launch_bounds__(kCandWarps * 32) k_mx_cand(ScreenTables T, float cut, int na,
                                                              const int *__restrict__ A,
                                                              const PossPair *__restrict__ P, int *__restrict__ cnt,
-                                                             const int *__restrict__ off, int2 *__restrict__ E) {
+                                                             int *__restrict__ X) {
     const int i = blockIdx.x * kCandWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= na) return;                                          // the whole warp: uniform
     const int p = A[i];
     const PossPair r = P[p];
     const int n = T.ns < T.cn[r.c] ? T.ns : T.cn[r.c];
-    int e = E ? off[p] : 0;
+    int e = 0;
     for (int k0 = 0; k0 < n; k0 += 32) {
         const int k = k0 + lane;
         const bool hit = k < n && point_cand32(T, r.s, r.c, k, n, cut, r.ubmin);
         const unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (E && hit) E[e + __popc(m & ((1u << lane) - 1u))] = make_int2(p, k);
+        const int at = e + __popc(m & ((1u << lane) - 1u));
+        if (hit && at < kCandCap) X[(size_t)i * kCandCap + at] = k;
         e += __popc(m);
     }
-    if (!E && lane == 0) cnt[p] = e;
+    if (lane == 0) cnt[p] = e;
+}
+
+// the kept candidates of the overflowed pairs into their places in E
+__global__ void k_mx_cand_copy(int na, const int *__restrict__ A, const int *__restrict__ cnt,
+                               const int *__restrict__ off, const int *__restrict__ X, int2 *__restrict__ E) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = (int)(t / kCandCap), j = (int)(t % kCandCap);
+    if (i >= na) return;
+    const int p = A[i], n = cnt[p];
+    if (n <= kCandCap && j < n) E[off[p] + j] = make_int2(p, X[(size_t)i * kCandCap + j]);
+}
+
+// pairs with more than kCandCap candidates: walked again, writing all of them
+__global__ void __launch_bounds__(kCandWarps * 32) k_mx_cand_big(ScreenTables T, float cut, int na,
+                                                                 const int *__restrict__ A,
+                                                                 const PossPair *__restrict__ P,
+                                                                 const int *__restrict__ cnt,
+                                                                 const int *__restrict__ off, int2 *__restrict__ E) {
+    const int i = blockIdx.x * kCandWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= na) return;
+    const int p = A[i];
+    if (cnt[p] <= kCandCap) return;                               // the whole warp: uniform
+    const PossPair r = P[p];
+    const int n = T.ns < T.cn[r.c] ? T.ns : T.cn[r.c];
+    int e = off[p];
+    for (int k0 = 0; k0 < n; k0 += 32) {
+        const int k = k0 + lane;
+        const bool hit = k < n && point_cand32(T, r.s, r.c, k, n, cut, r.ubmin);
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) E[e + __popc(m & ((1u << lane) - 1u))] = make_int2(p, k);
+        e += __popc(m);
+    }
 }
 
 // ---- K4..K6: FP64 rechecks --------------------------------------------------------------------------------------
@@ -547,9 +584,11 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
             (rc = check(cudaStreamSynchronize(st), err, "overflowed sync")))
             return rc;
         launches += 2 + 3;
+        int *X = nullptr;
         if (na > 0) {
-            k_mx_cand<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, nullptr,
-                                                                                     nullptr);
+            if ((rc = grow(m.ovf, (size_t)na * kCandCap * 4, err))) return rc;
+            X = Pb<int>(m.ovf);
+            k_mx_cand<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, X);
             launches += 1;
         }
         if ((rc = exclusive_scan(st, np, pc, po, ppart, tot + 1, err))) return rc;
@@ -567,8 +606,10 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
         k_mx_list_emit<<<(np + 255) / 256, 256, 0, st>>>(np, P, po, E);
         launches += 1;
         if (na > 0) {
-            k_mx_cand<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, po, E);
-            launches += 1;
+            k_mx_cand_copy<<<(unsigned)(((long)na * kCandCap + 255) / 256), 256, 0, st>>>(na, A, pc, po, X, E);
+            k_mx_cand_big<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, po,
+                                                                                         E);
+            launches += 2;
         }
         if (ne > 0) {
             k_mx_eval64<<<(ne + 127) / 128, 128, 0, st>>>(T, cut, ne, P, E, ev, es);

@@ -13,7 +13,7 @@ struct DevBuf {
 
 // work buffers of the mixed-precision screen, owned by the context
 struct MixedBufs {
-    DevBuf order, ub, kmin, flag, cnt, off, total, kept, cand, cand_off, ent, entq, aux;
+    DevBuf order, ub, kmin, flag, cnt, off, total, kept, cand, cand_off, ent, entq, aux, ovf;
     std::string err;
 };
 

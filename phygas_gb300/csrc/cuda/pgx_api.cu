@@ -46,7 +46,7 @@ struct PgxContext {
     std::string err;
     // resident cluster table (original cluster order)
     int nc = 0, ncp = 0;
-    Buf c64, c32, clm, cn, cR2, cR2f, cr50, crt, cname;
+    Buf c64, c32, clm, cn, cR2, cr50, crt, cname;
     // the staged star chunk and the screen's work buffers
     int nt = 0;
     Buf s_ps0, s_sig21, s_prefix;
@@ -158,7 +158,7 @@ pgx::ScreenTables tables(PgxContext *ctx, int ns) {
     T.t64 = P<double>(ctx->t64); T.t32 = P<float4>(ctx->t32); T.lm_t = P<float>(ctx->tlm);
     T.seed_prefix = P<uint64_t>(ctx->s_prefix);
     T.c64 = P<double>(ctx->c64); T.c32 = P<float4>(ctx->c32); T.lm_c = P<float>(ctx->clm); T.cn = P<int>(ctx->cn);
-    T.R2 = P<double>(ctx->cR2); T.R2f = P<float>(ctx->cR2f); T.r50 = P<double>(ctx->cr50); T.rtot = P<double>(ctx->crt);
+    T.R2 = P<double>(ctx->cR2); T.r50 = P<double>(ctx->cr50); T.rtot = P<double>(ctx->crt);
     T.cname = P<char>(ctx->cname);
     return T;
 }
@@ -207,7 +207,7 @@ int pgx_open(int device, PgxContext **out) {
 void pgx_close(PgxContext *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
-    Buf *bufs[] = {&ctx->c64, &ctx->c32, &ctx->clm, &ctx->tlm, &ctx->x_lm, &ctx->cn, &ctx->cR2, &ctx->cR2f, &ctx->cr50, &ctx->crt, &ctx->cname, &ctx->s_ps0,
+    Buf *bufs[] = {&ctx->c64, &ctx->c32, &ctx->clm, &ctx->tlm, &ctx->x_lm, &ctx->cn, &ctx->cR2, &ctx->cr50, &ctx->crt, &ctx->cname, &ctx->s_ps0,
                    &ctx->s_sig21, &ctx->s_prefix, &ctx->opos, &ctx->ovel, &ctx->t64, &ctx->t32, &ctx->chi2T,
                    &ctx->kbT, &ctx->sbT, &ctx->cnt, &ctx->off, &ctx->total, &ctx->kept, &ctx->fin, &ctx->rows,
                    &ctx->p_off, &ctx->p_ps, &ctx->p_steps, &ctx->p_dt, &ctx->p_r50, &ctx->p_rt, &ctx->p_items,
@@ -418,7 +418,6 @@ int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double
     RET(ensure(ctx, ctx->clm, (size_t)nmax * nc * 4));
     RET(ensure(ctx, ctx->cn, (size_t)nc * 4));
     RET(ensure(ctx, ctx->cR2, (size_t)nc * 8));
-    RET(ensure(ctx, ctx->cR2f, (size_t)nc * 4));
     RET(ensure(ctx, ctx->cr50, (size_t)nc * 8));
     RET(ensure(ctx, ctx->crt, (size_t)nc * 8));
     RET(ensure(ctx, ctx->cname, (size_t)nc * 40));
@@ -433,25 +432,22 @@ int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double
                             P<float>(ctx->x_lm), P<double>(ctx->c64), P<float4>(ctx->c32), P<float>(ctx->clm),
                             ctx->mixed));
     std::vector<double> R2(nc), r50(nc), rt(nc);
-    std::vector<float> R2f(nc);
     for (int i = 0; i < nc; i++) {
         double R = (r_kernel > 0 ? r_kernel * r50_pc[i] : rtot_pc[i]) / 1000.0;
         R2[i] = R * R;
-        R2f[i] = (float)R2[i];
         r50[i] = r50_pc[i] / 1000.0;
         rt[i] = rtot_pc[i] / 1000.0;
     }
     CK(cudaMemcpyAsync(ctx->cn.p, npts.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->cR2.p, R2.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemcpyAsync(ctx->cR2f.p, R2f.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->cr50.p, r50.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->crt.p, rt.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->cname.p, names, (size_t)nc * 40, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     ctx->nc = nc;
     ctx->ncp = nmax;
-    MRET(pgx::mixed_cluster_aux(ctx->st, nc, nmax, P<float4>(ctx->c32), P<int>(ctx->cn), P<double>(ctx->cR2),
-                               ctx->mixed));
+    MRET(pgx::mixed_cluster_aux(ctx->st, nc, nmax, P<int>(ctx->cn), P<double>(ctx->c64), P<double>(ctx->cR2),
+                               P<float4>(ctx->c32), P<float>(ctx->clm), ctx->mixed));
     CK(cudaStreamSynchronize(ctx->st));
     return 0;
 }
@@ -1067,7 +1063,6 @@ int pair_tables(PgxContext *ctx, const PhLin *tl, const PhLin *cl, const PhClust
     T.c64 = (const double *)base + (size_t)nmax * 12;
     T.t32 = nullptr; T.c32 = nullptr; T.lm_t = nullptr; T.lm_c = nullptr;
     T.R2 = (const double *)a; T.r50 = (const double *)(a + 8); T.rtot = (const double *)(a + 16);
-    T.R2f = nullptr;
     T.seed_prefix = (const uint64_t *)(a + 24); T.cn = (const int *)(a + 32); T.cname = a + 40;
     return 0;
 }

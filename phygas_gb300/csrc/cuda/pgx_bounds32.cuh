@@ -80,12 +80,12 @@ PGX_HD float fast_rsqrt(float x) {
 // storage's 3 and the substitution's 4 at most 20 eps tr(M) -- kSkipC1 = 24 -- and the form's own rounding 8 eps
 // (12 below); each square root via x rsqrtf(x) is within 5 eps.
 constexpr float kSkipC1 = 24.f;
-PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float R2, float lmt, float lmc,
+PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float lmt, float lmc,
                          const float (&m0)[3], const float (&m1)[3], float cut) {
-    const float M0 = St[0] + Sc[0] + R2, M1 = St[1] + Sc[1], M2 = St[2] + Sc[2];
-    const float M3 = St[3] + Sc[3] + R2, M4 = St[4] + Sc[4], M5 = St[5] + Sc[5] + R2;
+    const float M0 = St[0] + Sc[0], M1 = St[1] + Sc[1], M2 = St[2] + Sc[2];
+    const float M3 = St[3] + Sc[3], M4 = St[4] + Sc[4], M5 = St[5] + Sc[5];
     const float tr = M0 + M3 + M5;
-    const float lam = (R2 + lmt + lmc) * (1.f - 16.f * kEps32);
+    const float lam = (lmt + lmc) * (1.f - 16.f * kEps32);
     const float dx = m1[0] - m0[0], dy = m1[1] - m0[1], dz = m1[2] - m0[2];
     const float m00 = fmaf(m0[0], m0[0], fmaf(m0[1], m0[1], m0[2] * m0[2]));
     const float m11 = fmaf(m1[0], m1[0], fmaf(m1[1], m1[1], m1[2] * m1[2]));
@@ -122,8 +122,10 @@ PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float R2, f
 // rejected by the reference's trace bound with margins (see below): then v, if the FP64 path evaluates it at all,
 // is above the cut, and the point can neither be the minimum of a kept pair nor bring a pair under the cut.
 //
-// lam = R^2 + lmin(S_t) + lmin(S_c) <= lambda_min(M) (Weyl; the lmin are FP64 lower bounds from the covariance
-// kernel).  Bounds on the exact forms, then the FP64 path's own rounding on top:
+// The cluster side carries the kernel radius: Sc = S_c + R^2 I, each entry the FP32 rounding of the FP64 sum (one
+// rounding, where St + S_c + R^2 in FP32 took three), and lmc <= lmin(S_c) + R^2, so M = St + Sc.
+// lam = lmt + lmc <= lambda_min(M) (Weyl; the lmin are FP64 lower bounds from the covariance kernel, rounded down).
+// Bounds on the exact forms, then the FP64 path's own rounding on top:
 //  * Rayleigh, robust to any conditioning: for any vector w, x^T M^-1 x >= (w.x)^2 / w^T M w (Cauchy-Schwarz), and
 //    on the segment w.x >= min(w.m0, w.m1); with w = m0, m1 and the FP32 nearest point u this bounds the whole
 //    segment from below (w^T M w needs no inversion: error <= 10 eps (sum sqrt(M_ii) |w_i|)^2).
@@ -136,14 +138,14 @@ PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float R2, f
 //    never more than the segment's own length (both points lie on it).
 //  * The FP64 adjugate evaluation adds relative error <= kAdj64 T^3 / det(M), det(M) >= lam^2 tr(M) / 3.
 // lb <= v <= ub: lb = max(Rayleigh, min(lb(q0), lb(qs))), ub = min(ub(q0), ub(qs)) (+inf without LDL^T).
-PGX_HD bool point_bound32(const float (&St)[6], const float (&Sc)[6], float R2, float lmt, float lmc,
+PGX_HD bool point_bound32(const float (&St)[6], const float (&Sc)[6], float lmt, float lmc,
                                               const float (&m0)[3], const float (&m1)[3], bool more, float cut,
                                               Bound &b) {
     const float inf = __builtin_huge_valf();
-    const float M0 = St[0] + Sc[0] + R2, M1 = St[1] + Sc[1], M2 = St[2] + Sc[2];
-    const float M3 = St[3] + Sc[3] + R2, M4 = St[4] + Sc[4], M5 = St[5] + Sc[5] + R2;
+    const float M0 = St[0] + Sc[0], M1 = St[1] + Sc[1], M2 = St[2] + Sc[2];
+    const float M3 = St[3] + Sc[3], M4 = St[4] + Sc[4], M5 = St[5] + Sc[5];
     const float tr = M0 + M3 + M5;
-    const float lam = (R2 + lmt + lmc) * (1.f - 16.f * kEps32);
+    const float lam = (lmt + lmc) * (1.f - 16.f * kEps32);
     const float dx = m1[0] - m0[0], dy = m1[1] - m0[1], dz = m1[2] - m0[2];
     const float a = fmaf(m0[0], dx, fmaf(m0[1], dy, m0[2] * dz));
     const float dd = fmaf(dx, dx, fmaf(dy, dy, dz * dz));

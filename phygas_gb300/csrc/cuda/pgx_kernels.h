@@ -39,11 +39,10 @@ struct ScreenTables {
     const float *lm_t;               // [k][nt]: lower bound on lambda_min(S) of the star track (FP32, rounded down)
     const uint64_t *seed_prefix;     // per star: FNV-1a state after "id|"
     const double *c64;
-    const float4 *c32;
-    const float *lm_c;               // [k][nc]: the same for the cluster table
+    const float4 *c32;               // the cluster table in FP32 with the kernel radius folded in: S + R^2 I
+    const float *lm_c;               // [k][nc]: lower bound on lambda_min(S) + R^2 (FP32, rounded down)
     const int *cn;
     const double *R2, *r50, *rtot;
-    const float *R2f;                // R2 rounded to FP32 (the mixed-precision filter)
     const char *cname;               // nc * 40 bytes
 };
 

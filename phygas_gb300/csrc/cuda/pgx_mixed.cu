@@ -90,7 +90,30 @@ int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, con
     return check(cudaStreamSynchronize(st), m.err, "gather sync");
 }
 
-int mixed_cluster_aux(cudaStream_t, int, int, const float4 *, const int *, const double *, MixedBufs &) { return 0; }
+// The FP32 cluster table carries the kernel radius: S + R^2 I rounded once from FP64, and lmin + R^2 rounded down
+// (point_skip32 / point_bound32 read M = St + Sc and lam = lmt + lmc).  The FP64 table is left as it is.
+__global__ void k_fold_r2(int nc, int nmax, const int *__restrict__ cn, const double *__restrict__ c64,
+                          const double *__restrict__ R2, float4 *__restrict__ c32, float *__restrict__ clm) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)nc * nmax) return;
+    const int c = (int)(idx % nc), k = (int)(idx / nc);
+    if (k >= cn[c]) return;
+    const size_t NC = nc;
+    const double r2 = R2[c];
+    const double *S = c64 + ((size_t)k * 12 + 6) * NC + c;      // xx xy xz yy yz zz
+    float4 *q = c32 + ((size_t)k * NC + c) * 3;
+    q[1].z = (float)(S[0] + r2);
+    q[2].y = (float)(S[3 * NC] + r2);
+    q[2].w = (float)(S[5 * NC] + r2);
+    clm[(size_t)k * NC + c] = __double2float_rd((double)clm[(size_t)k * NC + c] + r2);
+}
+
+int mixed_cluster_aux(cudaStream_t st, int nc, int nmax, const int *cn, const double *c64, const double *R2,
+                      float4 *c32, float *clm, MixedBufs &m) {
+    const size_t work = (size_t)nc * nmax;
+    k_fold_r2<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(nc, nmax, cn, c64, R2, c32, clm);
+    return check(cudaGetLastError(), m.err, "k_fold_r2");
+}
 
 // separation of star and cluster at one point from the split FP32 positions
 __device__ __forceinline__ void sep32(const float4 &t0, const float4 &t1, const float4 &c0, const float4 &c1,
@@ -132,7 +155,7 @@ __device__ __forceinline__ bool point_at32(const ScreenTables &T, int s, int c, 
     }
     const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
     const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
-    return point_bound32(St, Sc, T.R2f[c], T.lm_t[(size_t)k * NT + s], __ldg(T.lm_c + (size_t)k * NC + c), m0, m1,
+    return point_bound32(St, Sc, T.lm_t[(size_t)k * NT + s], __ldg(T.lm_c + (size_t)k * NC + c), m0, m1,
                          more, cut, b);
 }
 
@@ -187,7 +210,6 @@ __global__ void __launch_bounds__(kScanStars) k_mx_scan32(ScreenTables T, float 
     };
     const size_t NT = T.nt, NC = T.nc;
     const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
-    const float R2 = T.R2f[c];
     const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
     float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
     float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2);
@@ -205,7 +227,7 @@ __global__ void __launch_bounds__(kScanStars) k_mx_scan32(ScreenTables T, float 
             c0 = __ldg(cn); c1 = __ldg(cn + 1); c2 = __ldg(cn + 2);
             sep32(t0, t1, c0, c1, mnext);
         }
-        const bool need = active && !point_skip32(St, Sc, R2, lmt, lmc, mcur, mnext, cut);
+        const bool need = active && !point_skip32(St, Sc, lmt, lmc, mcur, mnext, cut);
         const unsigned mask = __ballot_sync(0xffffffffu, need);
         if (need) s_q[w][qn + __popc(mask & ((1u << lane) - 1u))] = lane | (k << 5);
         qn += __popc(mask);
@@ -392,10 +414,10 @@ __device__ __forceinline__ bool point_cand32(const ScreenTables &T, int s, int c
     }
     const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
     const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
-    const float R2 = T.R2f[c], lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
+    const float lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
     Bound b;
-    return !point_skip32(St, Sc, R2, lmt, lmc, m0, m1, cut) &&
-           point_bound32(St, Sc, R2, lmt, lmc, m0, m1, more, cut, b) && b.lb < cut && b.lb <= um;
+    return !point_skip32(St, Sc, lmt, lmc, m0, m1, cut) &&
+           point_bound32(St, Sc, lmt, lmc, m0, m1, more, cut, b) && b.lb < cut && b.lb <= um;
 }
 
 constexpr int kCandWarps = 4;
@@ -648,9 +670,10 @@ const KeptPair *mixed_kept(MixedBufs &m) { return (const KeptPair *)m.kept.p; }
 //  * __logf: absolute error <= 2^-21.41 on [0.5, 2], else 3 ulp, so r^2 = -2 ln u1 is within
 //    D = 9.6e-7 + 3.6e-7 r^2;  radius = r^2 rsqrtf(r^2) (rsqrtf: 2 ulp) within 3e-7 relative of sqrt(r^2), and
 //    |sqrt(r^2) - sqrt(r^2_64)| <= min(D / sqrt(r^2), sqrt(D)) <= min(D rsqrtf 1.000001, 1e-3 + 6e-4 radius);
-//  * cos(2 pi u2) = -cos(theta), theta = (U2 - 1/2) 6.283185f in [-pi, pi] (6.283185f < 2 pi): the angle is within
-//    1.19e-6 of 2 pi (u2 - 1/2) (conversion, subtraction, the constant, the product) and __cosf adds <= 2^-21.19
-//    absolute, so the cosine is within 1.61e-6;
+//  * cos(2 pi u2) = -cos(theta), theta = (U2 - 1/2) 6.283185f in [-pi, pi] (6.283185f < 2 pi), with U2 from the top
+//    32 bits of u2's generator output alone (|U2 - u2| <= 2^-32 + 2^-24 u2 < 2^-23, within the absolute error the
+//    bound allows the conversion): the angle is within 1.19e-6 of 2 pi (u2 - 1/2) (conversion, subtraction,
+//    the constant, the product) and __cosf adds <= 2^-21.19 absolute, so the cosine is within 1.61e-6;
 //  * z = -radius cos: |z - z_64| <= 1.000003 e_radius + 1.68e-6 radius.
 // x = m + L z by three fused multiply-adds from FP32 m and L: every component within
 // 4 eps (|m| + |L| max|z|) + |L| max|z - z_64| of the FP64 path's.
@@ -663,7 +686,7 @@ __device__ __forceinline__ void gauss32(uint64_t a, uint64_t b, float &z, float 
     const float r2 = fmaxf(-2.f * __logf(u1), 0.f);
     const float rs = rsqrtf(fmaxf(r2, 1e-30f));
     rad = r2 * rs;
-    z = -rad * __cosf((u53_unit(b >> 11) - 0.5f) * 6.283185f);
+    z = -rad * __cosf(((float)(uint32_t)(b >> 32) * 0x1p-32f - 0.5f) * 6.283185f);
     const float D = fmaf(3.6e-7f, r2, 9.6e-7f);
     const float erad = fmaf(3e-7f, rad, fminf(D * rs * 1.000001f, fmaf(6e-4f, rad, 1e-3f)));
     err = fmaf(erad, 1.000003f, 1.68e-6f * rad);
@@ -808,20 +831,24 @@ __global__ void k_mx_check_bounds(int n, const double *__restrict__ pos, const d
     float m0[3], m1[3], St[6], Sc[6];
     sep32(q[0][0], q[0][1], q[1][0], q[1][1], m0);
     sep32(q[2][0], q[2][1], q[3][0], q[3][1], m1);
-    for (int j = 0; j < 6; j++) { St[j] = (float)s[j]; Sc[j] = (float)s[6 + j]; }
+    // the cluster side as the table holds it: S_c + R^2 I rounded once, lmin(S_c) + R^2 rounded down
+    for (int j = 0; j < 6; j++) {
+        St[j] = (float)s[j];
+        Sc[j] = (float)(j == 0 || j == 3 || j == 5 ? s[6 + j] + R2[i] : s[6 + j]);
+    }
     const double lt = sym3_min_eig_lb(s[0], s[1], s[2], s[3], s[4], s[5]);
     const double lc = sym3_min_eig_lb(s[6], s[7], s[8], s[9], s[10], s[11]);
+    const float lmt = __double2float_rd(lt - 1e-12 * fabs(lt));
+    const float lmc = __double2float_rd((double)__double2float_rd(lc - 1e-12 * fabs(lc)) + R2[i]);
     Bound b;
-    const bool dec = point_bound32(St, Sc, (float)R2[i], __double2float_rd(lt - 1e-12 * fabs(lt)),
-                                   __double2float_rd(lc - 1e-12 * fabs(lc)), m0, m1, true, (float)cut, b);
+    const bool dec = point_bound32(St, Sc, lmt, lmc, m0, m1, true, (float)cut, b);
     double M[6], d0[3], d1[3], sv;
     for (int j = 0; j < 6; j++) M[j] = s[j] + s[6 + j];
     for (int j = 0; j < 3; j++) { d0[j] = p[j] - p[3 + j]; d1[j] = p[6 + j] - p[9 + j]; }
     v64[i] = point_chi2_64(M, R2[i], d0, d1, true, cut, sv);
     lb[i] = dec ? b.lb : 0.f;
     ub[i] = dec ? b.ub : 0.f;
-    rej[i] = !dec ? 1 : (point_skip32(St, Sc, (float)R2[i], __double2float_rd(lt - 1e-12 * fabs(lt)),
-                                      __double2float_rd(lc - 1e-12 * fabs(lc)), m0, m1, (float)cut) ? 2 : 0);
+    rej[i] = !dec ? 1 : (point_skip32(St, Sc, lmt, lmc, m0, m1, (float)cut) ? 2 : 0);
 }
 
 int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *S, const double *R2, double cut,

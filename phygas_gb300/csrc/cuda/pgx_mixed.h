@@ -26,9 +26,9 @@ int exclusive_scan(cudaStream_t st, int n, const int *in, int *out, int *part, i
 // slot-ordered tracks (longest first) -> cluster-ordered table columns
 int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, const double *t64_slot,
                    const float4 *t32_slot, const float *lm_slot, double *c64, float4 *c32, float *clm, MixedBufs &m);
-// per-cluster quantities the FP32 filter reads (kept resident with the table)
-int mixed_cluster_aux(cudaStream_t st, int nc, int nmax, const float4 *c32, const int *cn, const double *R2,
-                      MixedBufs &m);
+// the kernel radius folded into the FP32 cluster table the filter reads: S + R^2 I and lmin + R^2 (once per table)
+int mixed_cluster_aux(cudaStream_t st, int nc, int nmax, const int *cn, const double *c64, const double *R2,
+                      float4 *c32, float *clm, MixedBufs &m);
 // FP32 filter + FP64 recheck: the kept pairs in (star, cluster) order, identical to the FP64 path's
 int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &m, cudaEvent_t ev_scan, int *total,
                  PgxStats *stats);

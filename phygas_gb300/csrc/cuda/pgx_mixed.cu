@@ -672,8 +672,9 @@ const KeptPair *mixed_kept(MixedBufs &m) { return (const KeptPair *)m.kept.p; }
 //    |sqrt(r^2) - sqrt(r^2_64)| <= min(D / sqrt(r^2), sqrt(D)) <= min(D rsqrtf 1.000001, 1e-3 + 6e-4 radius);
 //  * cos(2 pi u2) = -cos(theta), theta = (U2 - 1/2) 6.283185f in [-pi, pi] (6.283185f < 2 pi), with U2 from the top
 //    32 bits of u2's generator output alone (|U2 - u2| <= 2^-32 + 2^-24 u2 < 2^-23, within the absolute error the
-//    bound allows the conversion): the angle is within 1.19e-6 of 2 pi (u2 - 1/2) (conversion, subtraction,
-//    the constant, the product) and __cosf adds <= 2^-21.19 absolute, so the cosine is within 1.61e-6;
+//    bound allows the conversion): the angle, one fused multiply-add, is within 1.19e-6 of 2 pi (u2 - 1/2)
+//    (conversion 7.5e-7, the constant 1.6e-7, one rounding 1.9e-7) and __cosf adds <= 2^-21.19 absolute, so the
+//    cosine is within 1.61e-6;
 //  * z = -radius cos: |z - z_64| <= 1.000003 e_radius + 1.68e-6 radius.
 // x = m + L z by three fused multiply-adds from FP32 m and L: every component within
 // 4 eps (|m| + |L| max|z|) + |L| max|z - z_64| of the FP64 path's.
@@ -681,19 +682,29 @@ __device__ __forceinline__ float u53_unit(uint64_t k) {
     return fmaf((float)(uint32_t)(k >> 21), 0x1p-32f, (float)(uint32_t)(k & 0x1fffffu) * 0x1p-53f);
 }
 
+// The bound of one Gaussian, err = 1.000003 e_radius + 1.68e-6 radius with
+// e_radius = 3e-7 radius + min(1.000001 D rs, 1e-3 + 6e-4 radius), is evaluated with the factors folded into the
+// constants: err = kG1 radius + min(D' rs, kG3 radius + kG4), D' = kG5 r^2 + kG6.  Each folded constant is rounded
+// up and carries a further 1 + 1e-6 for the roundings of the fused evaluation (five operations, 2^-24 each).
+constexpr float kG1 = (3e-7f * 1.000003f + 1.68e-6f) * 1.000001f, kG3 = 6e-4f * 1.000003f * 1.000001f,
+                kG4 = 1e-3f * 1.000003f * 1.000001f, kG5 = 3.6e-7f * 1.000001f * 1.000003f * 1.000001f,
+                kG6 = 9.6e-7f * 1.000001f * 1.000003f * 1.000001f;
+// angle theta = (U2 - 1/2) 6.283185f as one fused multiply-add on the converted top 32 bits: 6.283185f 2^-32 is
+// exact and 3.1415925f is half of 6.283185f, so one rounding replaces the subtraction's and the product's
+constexpr float kAngleScale = 6.283185f * 0x1p-32f, kAngleShift = 3.1415925f;
+
 __device__ __forceinline__ void gauss32(uint64_t a, uint64_t b, float &z, float &rad, float &err) {
     const float u1 = fmaxf(u53_unit(a >> 11), 0x1p-64f);       // the reference's floor for u1 = 0
     const float r2 = fmaxf(-2.f * __logf(u1), 0.f);
     const float rs = rsqrtf(fmaxf(r2, 1e-30f));
     rad = r2 * rs;
-    z = -rad * __cosf(((float)(uint32_t)(b >> 32) * 0x1p-32f - 0.5f) * 6.283185f);
-    const float D = fmaf(3.6e-7f, r2, 9.6e-7f);
-    const float erad = fmaf(3e-7f, rad, fminf(D * rs * 1.000001f, fmaf(6e-4f, rad, 1e-3f)));
-    err = fmaf(erad, 1.000003f, 1.68e-6f * rad);
+    z = -rad * __cosf(fmaf((float)(uint32_t)(b >> 32), kAngleScale, -kAngleShift));
+    err = fmaf(kG1, rad, fminf(fmaf(kG5, r2, kG6) * rs, fmaf(kG3, rad, kG4)));
 }
 
 struct Fin32 {
-    float mx, my, mz, l00, l10, l20, l11, l21, l22, r50s, rts, mabs, lsum, e50, etot;
+    float mx, my, mz, l00, l10, l20, l11, l21, l22, r50s, rts, e50, etot;
+    float eA, eE, eM;          // ex = eA max(radius) + eE max(err) + eM (draw32)
 };
 
 // the pair's FP32 constants: lane j converts field j of fin, the warp shares them (one conversion per warp)
@@ -709,8 +720,13 @@ __device__ __forceinline__ Fin32 fin32(const FinishIn &fin, int lane) {
     g.l20 = __shfl_sync(0xffffffffu, fv, 5); g.l11 = __shfl_sync(0xffffffffu, fv, 6);
     g.l21 = __shfl_sync(0xffffffffu, fv, 7); g.l22 = __shfl_sync(0xffffffffu, fv, 8);
     g.r50s = __shfl_sync(0xffffffffu, fv, 11); g.rts = __shfl_sync(0xffffffffu, fv, 12);
-    g.mabs = fabsf(g.mx) + fabsf(g.my) + fabsf(g.mz);
-    g.lsum = fabsf(g.l00) + fabsf(g.l10) + fabsf(g.l20) + fabsf(g.l11) + fabsf(g.l21) + fabsf(g.l22);
+    const float mabs = fabsf(g.mx) + fabsf(g.my) + fabsf(g.mz);
+    const float lsum = fabsf(g.l00) + fabsf(g.l10) + fabsf(g.l20) + fabsf(g.l11) + fabsf(g.l21) + fabsf(g.l22);
+    // ex = 4 eps mabs + lsum (4 eps amax + emax (1 + 2 eps)), amax = 1.000001 max(radius) + emax, expanded; the
+    // factor 1.000001 on each covers the roundings here and of the two fused multiply-adds in draw32
+    g.eA = lsum * (4.f * kEps32 * 1.000001f) * 1.000001f;
+    g.eE = lsum * (1.f + 6.f * kEps32) * 1.000001f;
+    g.eM = mabs * (4.f * kEps32) * 1.000001f;
     g.e50 = 8.f * kEps32 * g.r50s;                 // rounding of r50^2 and of the comparison
     g.etot = 8.f * kEps32 * g.rts;
     return g;
@@ -725,9 +741,7 @@ __device__ __forceinline__ void draw32(const Fin32 &g, uint64_t w, float &x, flo
     x = fmaf(g.l00, z0, g.mx);
     y = fmaf(g.l11, z1, fmaf(g.l10, z0, g.my));
     z = fmaf(g.l22, z2, fmaf(g.l21, z1, fmaf(g.l20, z0, g.mz)));
-    const float emax = fmaxf(e0, fmaxf(e1, e2));
-    const float amax = fmaf(fmaxf(a0, fmaxf(a1, a2)), 1.000001f, emax);
-    ex = fmaf(4.f * kEps32, g.mabs, g.lsum * fmaf(4.f * kEps32, amax, emax * (1.f + 2.f * kEps32)));
+    ex = fmaf(g.eA, fmaxf(a0, fmaxf(a1, a2)), fmaf(g.eE, fmaxf(e0, fmaxf(e1, e2)), g.eM));
 }
 
 __global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__restrict__ fin,

@@ -337,6 +337,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-pair", action="store_true", help="skip the batched Monte Carlo measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-cli", action="store_true", help="skip the end-to-end run of the screen CLI")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -435,7 +436,7 @@ def main():
             log("pair Monte Carlo measurement failed: %s" % e)
 
     cli = None
-    if rank == 0:
+    if rank == 0 and not args.no_cli:
         try:
             cli = cli_measure(cp, tp)
         except Exception as e:          # reported beside the headline, not part of it

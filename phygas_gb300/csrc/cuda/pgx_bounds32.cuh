@@ -49,18 +49,24 @@ PGX_HD bool trace_far32(float a, float dd, float m00, float m11, float tr, float
 }
 
 // Reciprocal and reciprocal square root on the GPU's fast units: within 2 ulp (4 eps relative) by their documented
-// worst case (__fdividef for divisors in [2^-126, 2^126], rsqrtf for positive arguments).  Host builds use the exact
-// operations, which the same margins cover.
+// worst case (PTX rcp.approx.f32: 1 ulp; rsqrt.approx.f32: relative error 2^-22.9; both over the full range).  The
+// .ftz forms flush subnormal arguments and results, which never occur here: every argument is checked or clamped to
+// be at least 1e-30, and a reciprocal's argument at most 1e30, so arguments and results are normal -- and they issue
+// as one special-function instruction, without the subnormal scaling around it.  Host builds use the exact operations, which the same margins cover.
 PGX_HD float fast_rcp(float x) {
 #ifdef __CUDA_ARCH__
-    return __fdividef(1.f, x);
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 #else
     return 1.f / x;
 #endif
 }
 PGX_HD float fast_rsqrt(float x) {
 #ifdef __CUDA_ARCH__
-    return rsqrtf(x);
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
 #else
     return 1.f / sqrtf(x);
 #endif

@@ -423,12 +423,13 @@ __device__ __forceinline__ bool point_cand32(const ScreenTables &T, int s, int c
 constexpr int kCandWarps = 4;
 constexpr int kCandCap = 32;            // candidates an overflowed pair keeps from its single walk
 
-// The walk: the candidates' point numbers into X[i][0, kCandCap), their count into cnt[p] (a pair with more is
-// walked again by k_mx_cand_big)
+// The walk: the candidates' point numbers into X[i][0, kCandCap), their count into cnt[p]; a pair with more is
+// listed in big[0, *nbig) (in any order) and walked again by k_mx_cand_big
 __global__ void __launch_bounds__(kCandWarps * 32) k_mx_cand(ScreenTables T, float cut, int na,
                                                              const int *__restrict__ A,
                                                              const PossPair *__restrict__ P, int *__restrict__ cnt,
-                                                             int *__restrict__ X) {
+                                                             int *__restrict__ X, int *__restrict__ big,
+                                                             int *__restrict__ nbig) {
     const int i = blockIdx.x * kCandWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= na) return;                                          // the whole warp: uniform
     const int p = A[i];
@@ -443,7 +444,10 @@ __global__ void __launch_bounds__(kCandWarps * 32) k_mx_cand(ScreenTables T, flo
         if (hit && at < kCandCap) X[(size_t)i * kCandCap + at] = k;
         e += __popc(m);
     }
-    if (lane == 0) cnt[p] = e;
+    if (lane == 0) {
+        cnt[p] = e;
+        if (e > kCandCap) big[atomicAdd(nbig, 1)] = i;
+    }
 }
 
 // the kept candidates of the overflowed pairs into their places in E
@@ -456,16 +460,16 @@ __global__ void k_mx_cand_copy(int na, const int *__restrict__ A, const int *__r
     if (n <= kCandCap && j < n) E[off[p] + j] = make_int2(p, X[(size_t)i * kCandCap + j]);
 }
 
-// pairs with more than kCandCap candidates: walked again, writing all of them
-__global__ void __launch_bounds__(kCandWarps * 32) k_mx_cand_big(ScreenTables T, float cut, int na,
+// the listed pairs with more than kCandCap candidates: walked again, writing all of them (each into its own place,
+// so the list's order does not matter)
+__global__ void __launch_bounds__(kCandWarps * 32) k_mx_cand_big(ScreenTables T, float cut, int nbig,
+                                                                 const int *__restrict__ big,
                                                                  const int *__restrict__ A,
                                                                  const PossPair *__restrict__ P,
-                                                                 const int *__restrict__ cnt,
                                                                  const int *__restrict__ off, int2 *__restrict__ E) {
-    const int i = blockIdx.x * kCandWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (i >= na) return;
-    const int p = A[i];
-    if (cnt[p] <= kCandCap) return;                               // the whole warp: uniform
+    const int b = blockIdx.x * kCandWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (b >= nbig) return;                                        // the whole warp: uniform
+    const int p = A[big[b]];
     const PossPair r = P[p];
     const int n = T.ns < T.cn[r.c] ? T.ns : T.cn[r.c];
     int e = off[p];
@@ -606,17 +610,23 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
             (rc = check(cudaStreamSynchronize(st), err, "overflowed sync")))
             return rc;
         launches += 2 + 3;
-        int *X = nullptr;
+        int *X = nullptr, *big = nullptr, *nbig = tot + 4;
         if (na > 0) {
-            if ((rc = grow(m.ovf, (size_t)na * kCandCap * 4, err))) return rc;
+            if ((rc = grow(m.ovf, (size_t)na * (kCandCap + 1) * 4, err))) return rc;
             X = Pb<int>(m.ovf);
-            k_mx_cand<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, X);
+            big = X + (size_t)na * kCandCap;
+            if ((rc = check(cudaMemsetAsync(nbig, 0, 4, st), err, "memset"))) return rc;
+            k_mx_cand<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, X, big,
+                                                                                     nbig);
             launches += 1;
         }
         if ((rc = exclusive_scan(st, np, pc, po, ppart, tot + 1, err))) return rc;
-        if ((rc = check(cudaMemcpyAsync(&ne, tot + 1, 4, cudaMemcpyDeviceToHost, st), err, "entries")) ||
+        int counts[4] = {0, 0, 0, 0};                            // entries, -, -, pairs with > kCandCap candidates
+        if ((rc = check(cudaMemcpyAsync(counts, tot + 1, 16, cudaMemcpyDeviceToHost, st), err, "entries")) ||
             (rc = check(cudaStreamSynchronize(st), err, "entries sync")))
             return rc;
+        ne = counts[0];
+        const int n_big = na > 0 ? counts[3] : 0;
         launches += 3;
         if ((long long)ne > kMaxEntries) {
             err = "mixed precision: too many candidate points for the work buffers";
@@ -629,9 +639,12 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
         launches += 1;
         if (na > 0) {
             k_mx_cand_copy<<<(unsigned)(((long)na * kCandCap + 255) / 256), 256, 0, st>>>(na, A, pc, po, X, E);
-            k_mx_cand_big<<<(na + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, na, A, P, pc, po,
-                                                                                         E);
-            launches += 2;
+            launches += 1;
+            if (n_big > 0) {
+                k_mx_cand_big<<<(n_big + kCandWarps - 1) / kCandWarps, kCandWarps * 32, 0, st>>>(T, cutf, n_big, big,
+                                                                                                A, P, po, E);
+                launches += 1;
+            }
         }
         if (ne > 0) {
             k_mx_eval64<<<(ne + 127) / 128, 128, 0, st>>>(T, cut, ne, P, E, ev, es);
@@ -668,8 +681,8 @@ const KeptPair *mixed_kept(MixedBufs &m) { return (const KeptPair *)m.kept.p; }
 //  * u = k 2^-53 from the 53-bit integer k in FP32 within 2^-23 relative (two 32-bit conversions and a fused
 //    multiply-add), so |ln U - ln u| <= 1.2e-7;
 //  * __logf: absolute error <= 2^-21.41 on [0.5, 2], else 3 ulp, so r^2 = -2 ln u1 is within
-//    D = 9.6e-7 + 3.6e-7 r^2;  radius = r^2 rsqrtf(r^2) (rsqrtf: 2 ulp) within 3e-7 relative of sqrt(r^2), and
-//    |sqrt(r^2) - sqrt(r^2_64)| <= min(D / sqrt(r^2), sqrt(D)) <= min(D rsqrtf 1.000001, 1e-3 + 6e-4 radius);
+//    D = 9.6e-7 + 3.6e-7 r^2;  radius = r^2 rsqrt(r^2) (fast_rsqrt: 2 ulp) within 3e-7 relative of sqrt(r^2), and
+//    |sqrt(r^2) - sqrt(r^2_64)| <= min(D / sqrt(r^2), sqrt(D)) <= min(D rsqrt 1.000001, 1e-3 + 6e-4 radius);
 //  * cos(2 pi u2) = -cos(theta), theta = (U2 - 1/2) 6.283185f in [-pi, pi] (6.283185f < 2 pi), with U2 from the top
 //    32 bits of u2's generator output alone (|U2 - u2| <= 2^-32 + 2^-24 u2 < 2^-23, within the absolute error the
 //    bound allows the conversion): the angle, one fused multiply-add, is within 1.19e-6 of 2 pi (u2 - 1/2)
@@ -696,7 +709,7 @@ constexpr float kAngleScale = 6.283185f * 0x1p-32f, kAngleShift = 3.1415925f;
 __device__ __forceinline__ void gauss32(uint64_t a, uint64_t b, float &z, float &rad, float &err) {
     const float u1 = fmaxf(u53_unit(a >> 11), 0x1p-64f);       // the reference's floor for u1 = 0
     const float r2 = fmaxf(-2.f * __logf(u1), 0.f);
-    const float rs = rsqrtf(fmaxf(r2, 1e-30f));
+    const float rs = fast_rsqrt(fmaxf(r2, 1e-30f));
     rad = r2 * rs;
     z = -rad * __cosf(fmaf((float)(uint32_t)(b >> 32), kAngleScale, -kAngleShift));
     err = fmaf(kG1, rad, fminf(fmaf(kG5, r2, kG6) * rs, fmaf(kG3, rad, kG4)));

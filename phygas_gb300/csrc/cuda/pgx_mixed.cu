@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(kScanStars) k_mx_scan32(ScreenTables T, float 
                                                           unsigned long long *__restrict__ klist) {
     __shared__ int s_q[kScanStars / 32][kQueue];
     __shared__ float s_lb[kScanStars / 32][32], s_ub[kScanStars / 32][32];
+    __shared__ unsigned s_own[kScanStars / 32][32];                // per owner lane: its entries of the drain
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, c = blockIdx.x;
     const int s0 = blockIdx.y * kScanStars + w * 32;
     if (s0 >= T.nt) return;                                       // the whole warp: uniform
@@ -191,8 +192,11 @@ __global__ void __launch_bounds__(kScanStars) k_mx_scan32(ScreenTables T, float 
             over |= !placed || k >= (int)kNoPoint;
         }
     };
-    // full bounds for queue entries [0, cnt): entry = owner lane | k << 5
+    // full bounds for queue entries [0, cnt) (an entry is owner lane | k << 5), one per lane; then each owner lane
+    // folds its own entries, found from a bit mask per owner, in queue order (the order it queued them in)
     auto drain = [&](int cnt) {
+        __syncwarp();
+        s_own[w][lane] = 0u;
         __syncwarp();
         if (lane < cnt) {
             const int e = s_q[w][lane];
@@ -200,11 +204,12 @@ __global__ void __launch_bounds__(kScanStars) k_mx_scan32(ScreenTables T, float 
             const bool keep = point_at32(T, s0 + (e & 31), c, e >> 5, cut, b);
             s_lb[w][lane] = keep ? b.lb : inf;
             s_ub[w][lane] = keep ? b.ub : inf;
+            atomicOr(&s_own[w][e & 31], 1u << lane);
         }
         __syncwarp();
-        for (int j = 0; j < cnt; j++) {
-            const int e = s_q[w][j];
-            if ((e & 31) == lane) fold(e >> 5, s_lb[w][j], s_ub[w][j]);
+        for (unsigned mine = s_own[w][lane]; mine; mine &= mine - 1u) {
+            const int j = __ffs(mine) - 1;
+            fold(s_q[w][j] >> 5, s_lb[w][j], s_ub[w][j]);
         }
         __syncwarp();
     };

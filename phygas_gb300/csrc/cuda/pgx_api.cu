@@ -39,6 +39,14 @@ enum { EV_START, EV_ORBIT, EV_COV, EV_SCAN, EV_SELECT, EV_FINISH, EV_PAIR0, EV_P
 
 }  // namespace
 
+// One staged chunk of stars: inputs (SoA), orbit scratch, the tracks the screen reads, the ids of the text lines,
+// and the event that marks its tracks done
+struct TrackSlot {
+    int nt = 0, ns = 0;
+    Buf ps0, sig21, prefix, opos, ovel, t64, t32, tlm, ids;
+    cudaEvent_t done = nullptr;
+};
+
 struct PgxContext {
     int device = 0, sms = 0;
     cudaStream_t st = nullptr;
@@ -47,17 +55,19 @@ struct PgxContext {
     // resident cluster table (original cluster order)
     int nc = 0, ncp = 0;
     Buf c64, c32, clm, cn, cR2, cr50, crt, cname;
-    // the staged star chunk and the screen's work buffers
-    int nt = 0;
-    Buf s_ps0, s_sig21, s_prefix;
-    Buf opos, ovel, t64, t32, tlm;
+    // the staged star chunks: two track slots, so that one chunk's orbits can run on the side stream while the
+    // previous chunk is screened (pgx_screen_chunks); the single-chunk entry points use slot `cur`
+    TrackSlot trk[2];
+    int cur = 0;
+    cudaStream_t side = nullptr;               // higher priority: the orbits' blocks start as soon as SMs free up
+    // the screen's work buffers
     Buf chi2T, kbT, sbT, cnt, off, total, kept, fin, rows;
     // pgx_screen_chunks(_text): two chunks' rows or text on the device and in page-locked host memory, reused
     // across calls, and the labels of the text lines
     Buf rows_b[2];
     char *h_buf[2] = {};
     size_t h_cap[2] = {};
-    Buf lab_ids, lab_names, lab_kinds, lab_age16, lab_age84;
+    Buf lab_names, lab_kinds, lab_age16, lab_age84;
     pgx::TextBufs text_bufs;
     pgx::MixedBufs mixed;
     long n_rows = 0;
@@ -135,28 +145,30 @@ void to_soa(int n, const double *ps0, const double *sig, std::vector<double> &p6
 }
 
 // nominal + neighbour orbits of N objects (ps0 / sig21 device SoA, npts per slot or uniform) into t64 / t32
-int run_lin(PgxContext *ctx, int N, const double *d_ps0, const double *d_sig21, const int *d_npts, int nmax,
-            Buf &opos, Buf &ovel, double *t64, float4 *t32, float *lm, bool timed) {
+// orbit_blocks > 0: the orbits on at most that many blocks (grid-stride), to share the GPU with other work
+int run_lin(PgxContext *ctx, cudaStream_t st, int N, const double *d_ps0, const double *d_sig21, const int *d_npts,
+            int nmax, Buf &opos, Buf &ovel, double *t64, float4 *t32, float *lm, bool timed, int orbit_blocks = 0) {
     RET(ensure(ctx, opos, (size_t)nmax * 21 * N * sizeof(double)));
     RET(ensure(ctx, ovel, (size_t)nmax * 3 * N * sizeof(double)));
-    dim3 g((N + 127) / 128, 7);
-    pgx::k_stm_orbits<<<g, 128, 0, ctx->st>>>(N, d_ps0, d_npts, nmax, P<double>(opos), P<double>(ovel));
+    int g = (int)((7L * N + 127) / 128);
+    if (orbit_blocks > 0) g = std::min(g, orbit_blocks);
+    pgx::k_stm_orbits<<<g, 128, 0, st>>>(N, d_ps0, d_npts, nmax, P<double>(opos), P<double>(ovel));
     CKL();
-    if (timed) CK(cudaEventRecord(ctx->ev[EV_ORBIT], ctx->st));
+    if (timed) CK(cudaEventRecord(ctx->ev[EV_ORBIT], st));
     const size_t work = (size_t)N * nmax;
-    pgx::k_stm_cov<<<(unsigned)((work + 255) / 256), 256, 0, ctx->st>>>(N, nmax, d_npts, P<double>(opos),
-                                                                         P<double>(ovel), d_sig21, t64, t32, lm);
+    pgx::k_stm_cov<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(N, nmax, d_npts, P<double>(opos),
+                                                                     P<double>(ovel), d_sig21, t64, t32, lm);
     CKL();
-    if (timed) CK(cudaEventRecord(ctx->ev[EV_COV], ctx->st));
+    if (timed) CK(cudaEventRecord(ctx->ev[EV_COV], st));
     ctx->stats.kernels += 2;
     return 0;
 }
 
-pgx::ScreenTables tables(PgxContext *ctx, int ns) {
+pgx::ScreenTables tables(PgxContext *ctx, TrackSlot &k) {
     pgx::ScreenTables T;
-    T.nt = ctx->nt; T.ns = ns; T.nc = ctx->nc; T.ncp = ctx->ncp;
-    T.t64 = P<double>(ctx->t64); T.t32 = P<float4>(ctx->t32); T.lm_t = P<float>(ctx->tlm);
-    T.seed_prefix = P<uint64_t>(ctx->s_prefix);
+    T.nt = k.nt; T.ns = k.ns; T.nc = ctx->nc; T.ncp = ctx->ncp;
+    T.t64 = P<double>(k.t64); T.t32 = P<float4>(k.t32); T.lm_t = P<float>(k.tlm);
+    T.seed_prefix = P<uint64_t>(k.prefix);
     T.c64 = P<double>(ctx->c64); T.c32 = P<float4>(ctx->c32); T.lm_c = P<float>(ctx->clm); T.cn = P<int>(ctx->cn);
     T.R2 = P<double>(ctx->cR2); T.r50 = P<double>(ctx->cr50); T.rtot = P<double>(ctx->crt);
     T.cname = P<char>(ctx->cname);
@@ -168,6 +180,123 @@ float elapsed(PgxContext *ctx, int a, int b) {
     if (cudaEventElapsedTime(&ms, ctx->ev[a], ctx->ev[b]) != cudaSuccess) return 0.f;
     return ms;
 }
+
+// Host inputs of nt stars (and, for text lines, their 40-byte ids) into track slot s, copied on stream st.
+int stage_slot(PgxContext *ctx, int s, int nt, const double *ps0, const double *sig, const uint64_t *prefix,
+               const char *ids, cudaStream_t st) {
+    if (nt > (1 << 20)) return fail(ctx, PGX_E_LIMIT, "pgx_screen_stage: %d stars in one chunk (limit 2^20)", nt);
+    TrackSlot &k = ctx->trk[s];
+    std::vector<double> p6, s21;
+    to_soa(nt, ps0, sig, p6, s21);
+    RET(ensure(ctx, k.ps0, p6.size() * 8));
+    RET(ensure(ctx, k.sig21, s21.size() * 8));
+    RET(ensure(ctx, k.prefix, (size_t)nt * 8));
+    CK(cudaMemcpyAsync(k.ps0.p, p6.data(), p6.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(k.sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(k.prefix.p, prefix, (size_t)nt * 8, cudaMemcpyHostToDevice, st));
+    if (ids) {
+        RET(ensure(ctx, k.ids, (size_t)40 * nt));
+        CK(cudaMemcpyAsync(k.ids.p, ids, (size_t)40 * nt, cudaMemcpyHostToDevice, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    k.nt = nt;
+    k.ns = 0;
+    return 0;
+}
+
+// The orbits and covariances of slot s (nominal + 6 neighbours per star, S = A Sigma0 A^T) on stream st; the
+// slot's event marks them done
+int tracks_slot(PgxContext *ctx, int s, double tmax_myr, cudaStream_t st, bool timed, int orbit_blocks = 0) {
+    TrackSlot &k = ctx->trk[s];
+    const int ns = npts_of(tmax_myr), nt = k.nt;
+    RET(ensure(ctx, k.t64, (size_t)ns * 12 * nt * 8));
+    RET(ensure(ctx, k.t32, (size_t)ns * 3 * nt * 16));
+    RET(ensure(ctx, k.tlm, (size_t)ns * nt * 4));
+    RET(run_lin(ctx, st, nt, P<double>(k.ps0), P<double>(k.sig21), nullptr, ns, k.opos, k.ovel, P<double>(k.t64),
+                P<float4>(k.t32), P<float>(k.tlm), timed, orbit_blocks));
+    CK(cudaEventRecord(k.done, st));
+    k.ns = ns;
+    return 0;
+}
+
+// The screen of slot s on the main stream, after its tracks (which may run on another stream): the scan, the
+// selection of the kept pairs and their 512 draws; the rows stay on the device (ctx->rows, *n_rows of them).
+// tracks_timed: the tracks ran on the main stream right before, timed by EV_START / EV_ORBIT / EV_COV.
+int screen_slot(PgxContext *ctx, int s, double cut, int precision, long *n_rows, bool tracks_timed) {
+    TrackSlot &k = ctx->trk[s];
+    const int nt = k.nt, nc = ctx->nc, ns = k.ns;
+    CK(cudaStreamWaitEvent(ctx->st, k.done, 0));
+    if (!tracks_timed) {
+        ctx->stats = PgxStats();
+        for (int e : {EV_START, EV_ORBIT, EV_COV}) CK(cudaEventRecord(ctx->ev[e], ctx->st));
+    }
+    pgx::ScreenTables T = tables(ctx, k);
+    int total = 0;
+    if (precision == PGX_FP64) {
+        const size_t pairs = (size_t)nt * nc;
+        RET(ensure(ctx, ctx->chi2T, pairs * 8));
+        RET(ensure(ctx, ctx->kbT, pairs * 4));
+        RET(ensure(ctx, ctx->sbT, pairs * 8));
+        RET(ensure(ctx, ctx->cnt, (size_t)nt * 4));
+        RET(ensure(ctx, ctx->off, (size_t)nt * 4));
+        RET(ensure(ctx, ctx->total, 16));
+        dim3 g((nt + 127) / 128, std::min(nc, 65535));
+        pgx::k_scan64<<<g, 128, 0, ctx->st>>>(T, cut, P<double>(ctx->chi2T), P<int>(ctx->kbT), P<double>(ctx->sbT));
+        CKL();
+        CK(cudaEventRecord(ctx->ev[EV_SCAN], ctx->st));
+        pgx::k_count_kept<<<(nt + 127) / 128, 128, 0, ctx->st>>>(nt, nc, P<double>(ctx->chi2T), cut, P<int>(ctx->cnt));
+        CKL();
+        pgx::k_exclusive_scan<<<1, 1024, 0, ctx->st>>>(nt, P<int>(ctx->cnt), P<int>(ctx->off), P<int>(ctx->total));
+        CKL();
+        CK(cudaMemcpyAsync(&total, ctx->total.p, 4, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        RET(ensure(ctx, ctx->kept, (size_t)total * sizeof(pgx::KeptPair)));
+        if (total > 0) {
+            pgx::k_emit_kept<<<(nt + 127) / 128, 128, 0, ctx->st>>>(nt, nc, P<double>(ctx->chi2T), P<int>(ctx->kbT),
+                                                                    P<double>(ctx->sbT), cut, P<int>(ctx->off),
+                                                                    P<pgx::KeptPair>(ctx->kept));
+            CKL();
+        }
+        CK(cudaEventRecord(ctx->ev[EV_SELECT], ctx->st));
+        ctx->stats.kernels += 4;
+    } else {
+        MRET(pgx::mixed_select(ctx->st, T, cut, ctx->mixed, ctx->ev[EV_SCAN], &total, &ctx->stats));
+        CK(cudaEventRecord(ctx->ev[EV_SELECT], ctx->st));
+    }
+    RET(ensure(ctx, ctx->fin, (size_t)total * sizeof(pgx::FinishIn)));
+    RET(ensure(ctx, ctx->rows, (size_t)total * sizeof(pgx::ScreenRowDev)));
+    if (total > 0) {
+        const pgx::KeptPair *kp = precision == PGX_FP64 ? P<pgx::KeptPair>(ctx->kept) : pgx::mixed_kept(ctx->mixed);
+        pgx::k_finish_prep<<<(total + 127) / 128, 128, 0, ctx->st>>>(T, total, kp, P<pgx::FinishIn>(ctx->fin),
+                                                                     P<pgx::ScreenRowDev>(ctx->rows));
+        CKL();
+        if (precision == PGX_FP64) {
+            pgx::k_finish64<<<(unsigned)(((size_t)total * 32 + 255) / 256), 256, 0, ctx->st>>>(
+                total, P<pgx::FinishIn>(ctx->fin), P<pgx::ScreenRowDev>(ctx->rows));
+            CKL();
+        } else {
+            MRET(pgx::mixed_finish(ctx->st, total, P<pgx::FinishIn>(ctx->fin), P<pgx::ScreenRowDev>(ctx->rows),
+                                  ctx->mixed, &ctx->stats));
+        }
+        ctx->stats.kernels += 2;
+    }
+    CK(cudaEventRecord(ctx->ev[EV_FINISH], ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    PgxStats &S = ctx->stats;
+    S.ms_orbit = elapsed(ctx, EV_START, EV_ORBIT);
+    S.ms_cov = elapsed(ctx, EV_ORBIT, EV_COV);
+    S.ms_scan = elapsed(ctx, EV_COV, EV_SCAN);
+    S.ms_select = elapsed(ctx, EV_SCAN, EV_SELECT);
+    S.ms_finish = elapsed(ctx, EV_SELECT, EV_FINISH);
+    S.ms_total = elapsed(ctx, EV_START, EV_FINISH);
+    S.pairs = (long)nt * nc;
+    S.kept = total;
+    S.body_steps = (long)nt * 7 * (ns - 1) * PH_LIN_SUB;
+    ctx->n_rows = total;
+    if (n_rows) *n_rows = total;
+    return 0;
+}
+
 
 }  // namespace
 
@@ -191,7 +320,11 @@ int pgx_open(int device, PgxContext **out) {
             CK(cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device));
             if (pgx::orbit_setup(device)) return fail(ctx, PGX_E_CUDA, "pgx_open: orbit force tables");
             CK(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
+            int lo = 0, hi = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            CK(cudaStreamCreateWithPriority(&ctx->side, cudaStreamNonBlocking, hi));
             for (auto &e : ctx->ev) CK(cudaEventCreate(&e));
+            for (auto &k : ctx->trk) CK(cudaEventCreateWithFlags(&k.done, cudaEventDisableTiming));
             return 0;
         };
         rc = init();
@@ -207,16 +340,21 @@ int pgx_open(int device, PgxContext **out) {
 void pgx_close(PgxContext *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
-    Buf *bufs[] = {&ctx->c64, &ctx->c32, &ctx->clm, &ctx->tlm, &ctx->x_lm, &ctx->cn, &ctx->cR2, &ctx->cr50, &ctx->crt, &ctx->cname, &ctx->s_ps0,
-                   &ctx->s_sig21, &ctx->s_prefix, &ctx->opos, &ctx->ovel, &ctx->t64, &ctx->t32, &ctx->chi2T,
+    Buf *bufs[] = {&ctx->c64, &ctx->c32, &ctx->clm, &ctx->x_lm, &ctx->cn, &ctx->cR2, &ctx->cr50, &ctx->crt,
+                   &ctx->cname, &ctx->chi2T,
                    &ctx->kbT, &ctx->sbT, &ctx->cnt, &ctx->off, &ctx->total, &ctx->kept, &ctx->fin, &ctx->rows,
                    &ctx->p_off, &ctx->p_ps, &ctx->p_steps, &ctx->p_dt, &ctx->p_r50, &ctx->p_rt, &ctx->p_items,
                    &ctx->p_q, &ctx->p_done, &ctx->p_cres, &ctx->p_res, &ctx->p_params, &ctx->x_ps0, &ctx->x_sig21,
                    &ctx->x_npts,
                    &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32, &ctx->rows_b[0], &ctx->rows_b[1],
-                   &ctx->lab_ids, &ctx->lab_names, &ctx->lab_kinds, &ctx->lab_age16, &ctx->lab_age84};
+                   &ctx->lab_names, &ctx->lab_kinds, &ctx->lab_age16, &ctx->lab_age84};
     for (Buf *b : bufs)
         if (b->p) cudaFree(b->p);
+    for (auto &k : ctx->trk) {
+        for (Buf *b : {&k.ps0, &k.sig21, &k.prefix, &k.opos, &k.ovel, &k.t64, &k.t32, &k.tlm, &k.ids})
+            if (b->p) cudaFree(b->p);
+        if (k.done) cudaEventDestroy(k.done);
+    }
     for (auto *h : ctx->h_buf)
         if (h) cudaFreeHost(h);
     pgx::text_free(ctx->text_bufs);
@@ -226,6 +364,7 @@ void pgx_close(PgxContext *ctx) {
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->st) cudaStreamDestroy(ctx->st);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     delete ctx;
 }
 
@@ -371,8 +510,8 @@ int pgx_lin(PgxContext *ctx, int n, const double *ps0, const double *sig, const 
     CK(cudaMemcpyAsync(ctx->x_sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->x_npts.p, npts, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->st));
     ctx->stats = PgxStats();
-    RET(run_lin(ctx, n, P<double>(ctx->x_ps0), P<double>(ctx->x_sig21), P<int>(ctx->x_npts), nmax, ctx->x_opos,
-                ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), P<float>(ctx->x_lm), false));
+    RET(run_lin(ctx, ctx->st, n, P<double>(ctx->x_ps0), P<double>(ctx->x_sig21), P<int>(ctx->x_npts), nmax,
+                ctx->x_opos, ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), P<float>(ctx->x_lm), false));
     std::vector<double> t((size_t)nmax * 12 * n);
     CK(cudaMemcpyAsync(t.data(), ctx->x_t64.p, t.size() * 8, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
@@ -425,8 +564,8 @@ int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double
     CK(cudaMemcpyAsync(ctx->x_sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(ctx->x_npts.p, npts_slot.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, ctx->st));
     ctx->stats = PgxStats();
-    RET(run_lin(ctx, nc, P<double>(ctx->x_ps0), P<double>(ctx->x_sig21), P<int>(ctx->x_npts), nmax, ctx->x_opos,
-                ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), P<float>(ctx->x_lm), false));
+    RET(run_lin(ctx, ctx->st, nc, P<double>(ctx->x_ps0), P<double>(ctx->x_sig21), P<int>(ctx->x_npts), nmax,
+                ctx->x_opos, ctx->x_ovel, P<double>(ctx->x_t64), P<float4>(ctx->x_t32), P<float>(ctx->x_lm), false));
     // slot order -> cluster order (a column gather, once per table)
     MRET(pgx::gather_columns(ctx->st, nc, nmax, order.data(), P<double>(ctx->x_t64), P<float4>(ctx->x_t32),
                             P<float>(ctx->x_lm), P<double>(ctx->c64), P<float4>(ctx->c32), P<float>(ctx->clm),
@@ -455,101 +594,21 @@ int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double
 int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *prefix) {
     if (!ctx) return PGX_E_ARG;
     if (nt <= 0 || !ps0 || !sig || !prefix) return fail(ctx, PGX_E_ARG, "pgx_screen_stage: bad args");
-    if (nt > (1 << 20)) return fail(ctx, PGX_E_LIMIT, "pgx_screen_stage: %d stars in one chunk (limit 2^20)", nt);
     CK(cudaSetDevice(ctx->device));
-    std::vector<double> p6, s21;
-    to_soa(nt, ps0, sig, p6, s21);
-    RET(ensure(ctx, ctx->s_ps0, p6.size() * 8));
-    RET(ensure(ctx, ctx->s_sig21, s21.size() * 8));
-    RET(ensure(ctx, ctx->s_prefix, (size_t)nt * 8));
-    CK(cudaMemcpyAsync(ctx->s_ps0.p, p6.data(), p6.size() * 8, cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemcpyAsync(ctx->s_sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaMemcpyAsync(ctx->s_prefix.p, prefix, (size_t)nt * 8, cudaMemcpyHostToDevice, ctx->st));
-    CK(cudaStreamSynchronize(ctx->st));
-    ctx->nt = nt;
-    return 0;
+    return stage_slot(ctx, ctx->cur, nt, ps0, sig, prefix, nullptr, ctx->st);
 }
 
 int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision, long *n_rows) {
     if (!ctx) return PGX_E_ARG;
     if (ctx->nc <= 0) return fail(ctx, PGX_E_ARG, "pgx_screen_exec: no cluster table (pgx_screen_clusters)");
-    if (ctx->nt <= 0) return fail(ctx, PGX_E_ARG, "pgx_screen_exec: no stars staged (pgx_screen_stage)");
+    if (ctx->trk[ctx->cur].nt <= 0) return fail(ctx, PGX_E_ARG, "pgx_screen_exec: no stars staged (pgx_screen_stage)");
     if (!(tmax_myr > 0) || !(cut > 0)) return fail(ctx, PGX_E_ARG, "pgx_screen_exec: tmax %g chi2_max %g", tmax_myr, cut);
     if (precision != PGX_FP64 && precision != PGX_MIXED) return fail(ctx, PGX_E_ARG, "precision %d", precision);
     CK(cudaSetDevice(ctx->device));
-    const int nt = ctx->nt, nc = ctx->nc, ns = npts_of(tmax_myr);
     ctx->stats = PgxStats();
-    RET(ensure(ctx, ctx->t64, (size_t)ns * 12 * nt * 8));
-    RET(ensure(ctx, ctx->t32, (size_t)ns * 3 * nt * 16));
-    RET(ensure(ctx, ctx->tlm, (size_t)ns * nt * 4));
     CK(cudaEventRecord(ctx->ev[EV_START], ctx->st));
-    RET(run_lin(ctx, nt, P<double>(ctx->s_ps0), P<double>(ctx->s_sig21), nullptr, ns, ctx->opos, ctx->ovel,
-                P<double>(ctx->t64), P<float4>(ctx->t32), P<float>(ctx->tlm), true));
-    pgx::ScreenTables T = tables(ctx, ns);
-    int total = 0;
-    if (precision == PGX_FP64) {
-        const size_t pairs = (size_t)nt * nc;
-        RET(ensure(ctx, ctx->chi2T, pairs * 8));
-        RET(ensure(ctx, ctx->kbT, pairs * 4));
-        RET(ensure(ctx, ctx->sbT, pairs * 8));
-        RET(ensure(ctx, ctx->cnt, (size_t)nt * 4));
-        RET(ensure(ctx, ctx->off, (size_t)nt * 4));
-        RET(ensure(ctx, ctx->total, 16));
-        dim3 g((nt + 127) / 128, std::min(nc, 65535));
-        pgx::k_scan64<<<g, 128, 0, ctx->st>>>(T, cut, P<double>(ctx->chi2T), P<int>(ctx->kbT), P<double>(ctx->sbT));
-        CKL();
-        CK(cudaEventRecord(ctx->ev[EV_SCAN], ctx->st));
-        pgx::k_count_kept<<<(nt + 127) / 128, 128, 0, ctx->st>>>(nt, nc, P<double>(ctx->chi2T), cut, P<int>(ctx->cnt));
-        CKL();
-        pgx::k_exclusive_scan<<<1, 1024, 0, ctx->st>>>(nt, P<int>(ctx->cnt), P<int>(ctx->off), P<int>(ctx->total));
-        CKL();
-        CK(cudaMemcpyAsync(&total, ctx->total.p, 4, cudaMemcpyDeviceToHost, ctx->st));
-        CK(cudaStreamSynchronize(ctx->st));
-        RET(ensure(ctx, ctx->kept, (size_t)total * sizeof(pgx::KeptPair)));
-        if (total > 0) {
-            pgx::k_emit_kept<<<(nt + 127) / 128, 128, 0, ctx->st>>>(nt, nc, P<double>(ctx->chi2T), P<int>(ctx->kbT),
-                                                                    P<double>(ctx->sbT), cut, P<int>(ctx->off),
-                                                                    P<pgx::KeptPair>(ctx->kept));
-            CKL();
-        }
-        CK(cudaEventRecord(ctx->ev[EV_SELECT], ctx->st));
-        ctx->stats.kernels += 4;
-    } else {
-        MRET(pgx::mixed_select(ctx->st, T, cut, ctx->mixed, ctx->ev[EV_SCAN], &total, &ctx->stats));
-        CK(cudaEventRecord(ctx->ev[EV_SELECT], ctx->st));
-    }
-    RET(ensure(ctx, ctx->fin, (size_t)total * sizeof(pgx::FinishIn)));
-    RET(ensure(ctx, ctx->rows, (size_t)total * sizeof(pgx::ScreenRowDev)));
-    if (total > 0) {
-        const pgx::KeptPair *kp = precision == PGX_FP64 ? P<pgx::KeptPair>(ctx->kept) : pgx::mixed_kept(ctx->mixed);
-        pgx::k_finish_prep<<<(total + 127) / 128, 128, 0, ctx->st>>>(T, total, kp, P<pgx::FinishIn>(ctx->fin),
-                                                                     P<pgx::ScreenRowDev>(ctx->rows));
-        CKL();
-        if (precision == PGX_FP64) {
-            pgx::k_finish64<<<(unsigned)(((size_t)total * 32 + 255) / 256), 256, 0, ctx->st>>>(
-                total, P<pgx::FinishIn>(ctx->fin), P<pgx::ScreenRowDev>(ctx->rows));
-            CKL();
-        } else {
-            MRET(pgx::mixed_finish(ctx->st, total, P<pgx::FinishIn>(ctx->fin), P<pgx::ScreenRowDev>(ctx->rows),
-                                  ctx->mixed, &ctx->stats));
-        }
-        ctx->stats.kernels += 2;
-    }
-    CK(cudaEventRecord(ctx->ev[EV_FINISH], ctx->st));
-    CK(cudaStreamSynchronize(ctx->st));
-    PgxStats &S = ctx->stats;
-    S.ms_orbit = elapsed(ctx, EV_START, EV_ORBIT);
-    S.ms_cov = elapsed(ctx, EV_ORBIT, EV_COV);
-    S.ms_scan = elapsed(ctx, EV_COV, EV_SCAN);
-    S.ms_select = elapsed(ctx, EV_SCAN, EV_SELECT);
-    S.ms_finish = elapsed(ctx, EV_SELECT, EV_FINISH);
-    S.ms_total = elapsed(ctx, EV_START, EV_FINISH);
-    S.pairs = (long)nt * nc;
-    S.kept = total;
-    S.body_steps = (long)nt * 7 * (ns - 1) * PH_LIN_SUB;
-    ctx->n_rows = total;
-    if (n_rows) *n_rows = total;
-    return 0;
+    RET(tracks_slot(ctx, ctx->cur, tmax_myr, ctx->st, true));
+    return screen_slot(ctx, ctx->cur, cut, precision, n_rows, true);
 }
 
 int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n) {
@@ -599,6 +658,10 @@ int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *si
 }  // extern "C"
 
 namespace {
+// Blocks per SM of a chunk's orbits traced beside the previous chunk's screen: few enough to leave the screen its
+// registers (its FP32 and integer work and the orbits' FP64 work use different pipes), enough to finish first.
+constexpr int kSideOrbitBlocksPerSm = 2;
+
 // Rows or text out of the chunk pipeline (pgx_screen_chunks, pgx_screen_chunks_text).
 struct ChunkOut {
     int (*rows)(void *arg, int first, const PgxScreenRow *rows, long n) = nullptr;
@@ -606,10 +669,12 @@ struct ChunkOut {
     void *arg = nullptr;
 };
 
-// Three stages run at once: the host draws of chunk c + 1 (a helper thread), the GPU work of chunk c (a worker
-// thread: stage, exec, then the rows copied into device slot c % 2 -- or formatted there as text -- and from there
-// to page-locked host memory on a second stream), and the output of chunk c - 1 on the calling thread.  Slot s is
-// reused for chunk c + 2 only after the output of chunk c has returned.
+// Four stages run at once: the host draws of chunk c + 2 (a helper thread); the orbits of chunk c + 1 on the
+// high-priority side stream, whose FP64 work shares the SMs with the FP32 and integer work of the screen of chunk c
+// on the main stream (both issued by a worker thread, which then copies the rows into device slot c % 2 -- or
+// formats them there as text -- and from there to page-locked host memory on a copy stream); and the output of
+// chunk c - 1 on the calling thread.  Track slot c % 2 and output slot c % 2 are reused for chunk c + 2 only after
+// chunk c is screened and its output has returned.
 int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n_samp, int threads, double tmax,
                     double cut, int precision, const ChunkOut &out) {
     const bool text = out.text != nullptr;
@@ -661,16 +726,31 @@ int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n
         ctx->h_cap[s] = cap;
         return 0;
     };
+    // chunk c's draws into buf[c % 2], staged into track slot c % 2 and its orbits started on the side stream
+    auto start_tracks = [&](int c) {
+        const Draw &b = buf[c & 1];
+        int r = stage_slot(ctx, c & 1, b.n, b.ps0.data(), b.sig.data(), b.pre.data(), text ? b.ids.data() : nullptr,
+                           ctx->side);
+        const int blocks = c == 0 ? 0 : kSideOrbitBlocksPerSm * ctx->sms;     // chunk 0 has the GPU to itself
+        return r ? r : tracks_slot(ctx, c & 1, tmax, ctx->side, false, blocks);
+    };
     auto worker = [&]() {
         int wrc = cudaSetDevice(ctx->device) == cudaSuccess ? 0 : fail(ctx, PGX_E_CUDA, "screen chunks: device");
-        if (wrc == 0) draw(0, buf[0]);
+        std::thread ahead;
+        if (wrc == 0) {
+            draw(0, buf[0]);
+            wrc = start_tracks(0);
+            if (nch > 1) ahead = std::thread(draw, 1, std::ref(buf[1]));
+        }
         for (int c = 0; c < nch && wrc == 0; c++) {
-            Draw &cur = buf[c & 1];
-            std::thread ahead;
-            if (c + 1 < nch) ahead = std::thread(draw, c + 1, std::ref(buf[(c + 1) & 1]));
+            const int first = c * chunk;
+            if (c + 1 < nch) {                            // the next chunk's orbits, beside this chunk's screen
+                ahead.join();
+                wrc = start_tracks(c + 1);
+                if (wrc == 0 && c + 2 < nch) ahead = std::thread(draw, c + 2, std::ref(buf[c & 1]));
+            }
             long n = 0;
-            wrc = pgx_screen_stage(ctx, cur.n, cur.ps0.data(), cur.sig.data(), cur.pre.data());
-            if (wrc == 0) wrc = pgx_screen_exec(ctx, tmax, cut, precision, &n);
+            if (wrc == 0) wrc = screen_slot(ctx, c & 1, cut, precision, &n, false);
             const int slot = c & 1;
             if (wrc == 0) {
                 std::unique_lock<std::mutex> lk(mu);
@@ -680,13 +760,10 @@ int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n
             size_t bytes = (size_t)n * sizeof(PgxScreenRow);
             Buf &dev = ctx->rows_b[slot];
             if (wrc == 0 && text && n > 0) {
-                // the chunk's star ids, then the lines formatted into the device slot
-                wrc = ensure(ctx, ctx->lab_ids, (size_t)40 * cur.n);
-                if (wrc == 0 && cudaMemcpyAsync(ctx->lab_ids.p, cur.ids.data(), (size_t)40 * cur.n,
-                                                cudaMemcpyHostToDevice, ctx->st) != cudaSuccess)
-                    wrc = fail(ctx, PGX_E_CUDA, "screen chunks: star ids");
-                const pgx::TextLabels L = {P<char>(ctx->lab_ids), P<char>(ctx->lab_names), P<char>(ctx->lab_kinds),
-                                           P<double>(ctx->lab_age16), P<double>(ctx->lab_age84)};
+                // the lines formatted into the device slot (the star ids came with the chunk's inputs)
+                const pgx::TextLabels L = {P<char>(ctx->trk[c & 1].ids), P<char>(ctx->lab_names),
+                                           P<char>(ctx->lab_kinds), P<double>(ctx->lab_age16),
+                                           P<double>(ctx->lab_age84)};
                 for (int attempt = 0; wrc == 0 && attempt < 2; attempt++) {
                     std::string err;
                     size_t need = 0;
@@ -716,16 +793,17 @@ int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n
             }
             if (wrc == 0 && cudaEventRecord(ev_host[slot], cs) != cudaSuccess)
                 wrc = fail(ctx, PGX_E_CUDA, "screen chunks: event record");
-            if (ahead.joinable()) ahead.join();
             if (wrc == 0) {
                 std::lock_guard<std::mutex> lk(mu);
                 n_of[slot] = n;
                 bytes_of[slot] = n > 0 ? bytes : 0;
-                first_of[slot] = cur.first;
+                first_of[slot] = first;
                 produced = c + 1;
                 cv.notify_all();
             }
         }
+        if (ahead.joinable()) ahead.join();
+        cudaStreamSynchronize(ctx->side);                 // no orbits left running on a slot after an early stop
         std::lock_guard<std::mutex> lk(mu);
         worker_rc = wrc;
         worker_done = true;

@@ -28,38 +28,39 @@
 
 namespace pgx {
 
-// npts == nullptr: every object has nmax points
+// npts == nullptr: every object has nmax points.  Orbit t of the 7 N (object i = t % N, axis j = t / N) per
+// thread, grid-stride, so a small grid can trace a chunk beside other work (one orbit per thread with a full grid).
 __global__ void __launch_bounds__(128) k_stm_orbits(int N, const double *__restrict__ ps0, const int *__restrict__ npts,
                                                     int nmax, double *__restrict__ opos, double *__restrict__ ovel) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i >= N) return;
     const size_t NN = N;
-    Orbit o;
-    o.x = ps0[i]; o.y = ps0[NN + i]; o.z = ps0[2 * NN + i];
-    o.vx = ps0[3 * NN + i]; o.vy = ps0[4 * NN + i]; o.vz = ps0[5 * NN + i];
-    switch (j) {
-        case 1: o.x += kEps; break;
-        case 2: o.y += kEps; break;
-        case 3: o.z += kEps; break;
-        case 4: o.vx += kEps; break;
-        case 5: o.vy += kEps; break;
-        case 6: o.vz += kEps; break;
-        default: break;
-    }
-    o.init();
-    const int n = npts ? npts[i] : nmax;
-    constexpr double dt = -kStepMyr / kSub, h = 0.5 * dt;
-    for (int k = 0; k < n; k++) {
-        if (k > 0) {
-#pragma unroll 1
-            for (int s = 0; s < kSub; s++) o.kdk(dt, h);
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < 7 * NN; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % NN), j = (int)(t / NN);
+        Orbit o;
+        o.x = ps0[i]; o.y = ps0[NN + i]; o.z = ps0[2 * NN + i];
+        o.vx = ps0[3 * NN + i]; o.vy = ps0[4 * NN + i]; o.vz = ps0[5 * NN + i];
+        switch (j) {
+            case 1: o.x += kEps; break;
+            case 2: o.y += kEps; break;
+            case 3: o.z += kEps; break;
+            case 4: o.vx += kEps; break;
+            case 5: o.vy += kEps; break;
+            case 6: o.vz += kEps; break;
+            default: break;
         }
-        double *p = opos + (size_t)(k * 7 + j) * 3 * NN + i;
-        p[0] = o.x; p[NN] = o.y; p[2 * NN] = o.z;
-        if (j == 0) {
-            double *v = ovel + (size_t)k * 3 * NN + i;
-            v[0] = o.vx; v[NN] = o.vy; v[2 * NN] = o.vz;
+        o.init();
+        const int n = npts ? npts[i] : nmax;
+        constexpr double dt = -kStepMyr / kSub, h = 0.5 * dt;
+        for (int k = 0; k < n; k++) {
+            if (k > 0) {
+#pragma unroll 1
+                for (int s = 0; s < kSub; s++) o.kdk(dt, h);
+            }
+            double *p = opos + (size_t)(k * 7 + j) * 3 * NN + i;
+            p[0] = o.x; p[NN] = o.y; p[2 * NN] = o.z;
+            if (j == 0) {
+                double *v = ovel + (size_t)k * 3 * NN + i;
+                v[0] = o.vx; v[NN] = o.vy; v[2 * NN] = o.vz;
+            }
         }
     }
 }

@@ -442,6 +442,31 @@ class HostRows:
             pass
 
 
+class HostBuffer:
+    """Page-locked host memory (pgx_host_alloc) seen as a numpy array of `n` items of `dtype`; keep the object alive
+    while the array is in use."""
+
+    def __init__(self, n, dtype=np.float64):
+        dtype = np.dtype(dtype)
+        self._p = lib().pgx_host_alloc(max(int(n), 1) * dtype.itemsize)
+        if not self._p:
+            raise MemoryError("pgx_host_alloc(%d x %s)" % (n, dtype))
+        self.array = np.frombuffer((C.c_char * (max(int(n), 1) * dtype.itemsize)).from_address(self._p), dtype,
+                                   int(n))
+
+    def close(self):
+        if self._p:
+            self.array = None
+            lib().pgx_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """The request loop (pgx_server_*): slots device contexts with the cluster table resident, jobs admitted in
     arrival order as slots and the device-memory budget allow."""
@@ -521,13 +546,22 @@ def prefilter_pairs(targets, clusters, threads=0):
     raise RuntimeError("pgx_prefilter_pairs: pair count changed between calls")
 
 
-def draw_pair_batch(targets, ti, clusters, ci, n_clones, dt_myr=0.05, threads=0):
-    """pgx_draw_pair_batch: host clone draws with a clone count per pair -> clone_off, ps, steps, dt, r50, rtot."""
+def draw_pair_batch(targets, ti, clusters, ci, n_clones, dt_myr=0.05, threads=0, out_ps=None):
+    """pgx_draw_pair_batch: host clone draws with a clone count per pair -> clone_off, ps, steps, dt, r50, rtot.
+    out_ps: a float64 array of at least 12 * sum(n_clones) to draw the clones into (for instance page-locked memory
+    from HostBuffer, which the device reads at the link's full rate)."""
     targets, clusters = as_array(targets, PhTarget), as_array(clusters, PhCluster)
     ti, ci = np.ascontiguousarray(ti, np.int32), np.ascontiguousarray(ci, np.int32)
     nc = np.ascontiguousarray(np.broadcast_to(n_clones, ti.shape), np.int32)
     n = len(ti)
-    off, ps = np.zeros(n + 1, np.int32), np.zeros(12 * max(int(nc.sum()), 1))
+    need = 12 * max(int(nc.sum()), 1)
+    if out_ps is None:
+        ps = np.zeros(need)
+    else:
+        if out_ps.dtype != np.float64 or not out_ps.flags.c_contiguous or out_ps.size < need:
+            raise ValueError("out_ps: a contiguous float64 array of at least %d" % need)
+        ps = out_ps
+    off = np.zeros(n + 1, np.int32)
     steps, dt, r50, rt = np.zeros(n, np.int32), np.zeros(n), np.zeros(n), np.zeros(n)
     rc = lib().pgx_draw_pair_batch(n, targets, _ptr(ti, C.c_int), clusters, _ptr(ci, C.c_int), _ptr(nc, C.c_int),
                                    dt_myr, threads, _ptr(off, C.c_int), _ptr(ps), _ptr(steps, C.c_int), _ptr(dt),

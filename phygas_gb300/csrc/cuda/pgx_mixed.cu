@@ -14,7 +14,7 @@
 //                    (LB_k < cut, LB_k <= min UB) -- in four slots, or "more than four".
 //   k_mx_count / k_mx_emit   stable compaction, per star, of the pairs that may be kept
 //   k_mx_list_*      the listed candidates written out; k_mx_cand walks the overflowed pairs again for theirs,
-//                    keeping up to 32 per pair for k_mx_cand_copy (k_mx_cand_big walks a pair with more a third time)
+//                    keeping up to 64 per pair for k_mx_cand_copy (k_mx_cand_big walks a pair with more a third time)
 //   k_mx_eval64      one thread per candidate point: the FP64 point chi2 (full warps on the scarce FP64 pipe)
 //   k_mx_best        per possible pair: FP64 argmin over its candidates (smallest value, first point of equals)
 //   k_mx_kept_*      stable compaction of the pairs under the cut
@@ -426,7 +426,7 @@ __device__ __forceinline__ bool point_cand32(const ScreenTables &T, int s, int c
 }
 
 constexpr int kCandWarps = 4;
-constexpr int kCandCap = 32;            // candidates an overflowed pair keeps from its single walk
+constexpr int kCandCap = 64;            // candidates an overflowed pair keeps from its single walk
 
 // The walk: the candidates' point numbers into X[i][0, kCandCap), their count into cnt[p]; a pair with more is
 // listed in big[0, *nbig) (in any order) and walked again by k_mx_cand_big

@@ -251,6 +251,28 @@ SERVE_JOBS, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 20, 1.0, 3, 1004
 E2E_CHUNKS = 8
 
 
+def compare_rows(mixed, fp64, cut=0.001):
+    """The mixed-precision rows against the FP64 path's on the same chunk: pair sets (all kept pairs, and those with
+    p_r50 >= cut), and the largest and 99th-percentile differences of d_min (relative), t_min (relative), p_r50 and
+    p_rtot (absolute) over the pairs both keep."""
+    import numpy as np
+    key = lambda r: r["star"].astype(np.int64) * (1 << 32) + r["cluster"]
+    km, kf = key(mixed), key(fp64)
+    both, im, jf = np.intersect1d(km, kf, assume_unique=True, return_indices=True)
+    a, b = mixed[im], fp64[jf]
+    em, ef = set(km[mixed["p_r50"] >= cut].tolist()), set(kf[fp64["p_r50"] >= cut].tolist())
+
+    def stat(x):
+        x = np.abs(x)
+        return {"max": float(x.max()) if len(x) else 0.0, "p99": float(np.quantile(x, 0.99)) if len(x) else 0.0}
+    rel = lambda u, v: (u - v) / np.where(v != 0, np.abs(v), 1.0)
+    return {"rows_mixed": int(len(mixed)), "rows_fp64": int(len(fp64)), "rows_both": int(len(both)),
+            "emitted_mixed": len(em), "emitted_fp64": len(ef), "emitted_differ": len(em ^ ef),
+            "rows_bitwise_identical": bool(len(mixed) == len(fp64) and mixed.tobytes() == fp64.tobytes()),
+            "d_nom_rel": stat(rel(a["d_nom_pc"], b["d_nom_pc"])), "t_rel": stat(rel(a["t_myr"], b["t_myr"])),
+            "p_r50_abs": stat(a["p_r50"] - b["p_r50"]), "p_rtot_abs": stat(a["p_rtot"] - b["p_rtot"])}
+
+
 def cli_measure(cp, tp, reps=2):
     """The screen CLI end to end (process start, inputs read, cluster table, the pipelined chunks, the lines
     formatted on the GPU and written to /dev/null): wall time, best of `reps`."""
@@ -341,6 +363,7 @@ def main():
     ap.add_argument("--no-pair", action="store_true", help="skip the batched Monte Carlo measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-cli", action="store_true", help="skip the end-to-end run of the screen CLI")
+    ap.add_argument("--no-control", action="store_true", help="skip the velocity-shuffled control's accuracy check")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -399,7 +422,20 @@ def main():
         precision = pg.PGX_FP64
     with Clocks(local) as clk:
         per, stats, n_rows = run(precision, args.steps, args.warmup)
+    rows_mixed = ctx.fetch(n_rows)
     per64, stats64, n_rows64 = run(pg.PGX_FP64, max(2, min(args.steps, 3)), 1)
+    rows_fp64 = ctx.fetch(n_rows64)
+    accuracy = {"screen": compare_rows(rows_mixed, rows_fp64)}
+    del rows_mixed, rows_fp64
+    if rank == 0 and not args.no_control:
+        # the chance-alignment control: the same stars with velocities shuffled, mixed against FP64
+        ctl = pg.control_targets(stars)
+        ctx.stage(*pg.draw_targets(ctl, N_SAMP))
+        a = ctx.fetch(ctx.exec(tmax, CHI2_MAX, pg.PGX_MIXED))
+        b = ctx.fetch(ctx.exec(tmax, CHI2_MAX, pg.PGX_FP64))
+        accuracy["control"] = compare_rows(a, b)
+        del a, b
+        ctx.stage(ps0, sig, pre)
     ms = statistics.mean(per)
     ms64 = statistics.mean(per64)
     if ws > 1:
@@ -471,6 +507,7 @@ def main():
             "plain_fp64": {"value": ws * pairs / (ms64 * 1e-3), "unit": "pairs/s", "ms_per_step": ms64,
                            "speedup_of_value": ms64 / ms},
             "rows_per_step": n_rows, "rows_fp64": n_rows64,
+            "mixed_vs_fp64": accuracy,
             "work_per_step": {k: int(s[k]) for k in ("candidates", "ambiguous", "rechecked_points",
                                                      "rechecked_draws", "kept")},
             "stages_ms": {k: statistics.mean(x[k] for x in stats) for k in

@@ -546,6 +546,17 @@ def prefilter_pairs(targets, clusters, threads=0):
     raise RuntimeError("pgx_prefilter_pairs: pair count changed between calls")
 
 
+def control_targets(targets):
+    """The screen's chance-alignment control (pgx_control_targets): each star with the proper motions (rescaled by
+    the parallax ratio) and radial velocity of the star n/2 further on."""
+    targets = as_array(targets, PhTarget)
+    out = (PhTarget * len(targets))()
+    rc = lib().pgx_control_targets(targets, len(targets), out)
+    if rc:
+        raise ValueError("pgx_control_targets: %d" % rc)
+    return out
+
+
 def draw_pair_batch(targets, ti, clusters, ci, n_clones, dt_myr=0.05, threads=0, out_ps=None):
     """pgx_draw_pair_batch: host clone draws with a clone count per pair -> clone_off, ps, steps, dt, r50, rtot.
     out_ps: a float64 array of at least 12 * sum(n_clones) to draw the clones into (for instance page-locked memory

@@ -12,10 +12,14 @@ What it writes, all from the reference itself:
   ref_dump_*.txt.gz
       raw values (C99 hex floats) from oracle/_ref/ref_dump -- the reference core compiled from its own sources -- for
       small slices: draws, STM tracks, the chi2 scan and finish, pair draws/clones/reduce, tracks and the prefilter
+  cli_<case>.txt.gz
+      stdout of the reference's own phygas_screen CLI (oracle/_ref/phygas_screen, compiled from its sources) on a
+      seeded synthetic workload (phygas_gb300.synth "screen": CLI_STARS stars, CLI_CLUSTERS clusters, seed CLI_SEED):
+      default arguments, the chance-alignment control run, and other chi2_max / n_samp / r_kernel
   golden.json
       the published hashes, row counts and the commands above
 
-usage: python3 tests/golden/make_golden.py [--ref /root/reference]
+usage: python3 tests/golden/make_golden.py [--ref /root/reference] [--only-cli]
 """
 import argparse
 import gzip
@@ -47,6 +51,11 @@ DUMPS = [
 ]
 
 
+# the CLI cases: (name, arguments after clusters.txt stars.txt)
+CLI_STARS, CLI_CLUSTERS, CLI_SEED = 64, 1000, 1005
+CLI_CASES = [("plain", []), ("control", ["25", "64", "2", "control"]), ("args", ["20", "32", "0"])]
+
+
 def rows_hash(lines):
     return hashlib.sha1("".join(lines).encode()).hexdigest()[:12]
 
@@ -56,11 +65,36 @@ def write_gz(path, data):
         f.write(data if isinstance(data, bytes) else data.encode())
 
 
+def make_cli(info):
+    sys.path.insert(0, REPO)
+    from phygas_gb300 import synth
+    cli = os.path.join(REPO, "oracle", "_ref", "phygas_screen")
+    info.setdefault("cli", {})
+    with tempfile.TemporaryDirectory() as tmp:
+        cp, tp = synth.write_workload(tmp, "screen", CLI_STARS, CLI_SEED, CLI_CLUSTERS)
+        for name, args in CLI_CASES:
+            out = subprocess.check_output([cli, cp, tp] + args, stderr=subprocess.DEVNULL)
+            write_gz(os.path.join(HERE, "cli_%s.txt.gz" % name), out)
+            info["cli"][name] = {"args": args, "rows": out.count(b"\n"), "sha1_12": hashlib.sha1(out).hexdigest()[:12],
+                                 "workload": "synth screen %d stars %d clusters seed %d" % (CLI_STARS, CLI_CLUSTERS,
+                                                                                             CLI_SEED)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only-cli", action="store_true", help="only the CLI fixtures (cli_*.txt.gz)")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", "REF=" + a.ref])
+    if a.only_cli:
+        with open(os.path.join(HERE, "golden.json")) as f:
+            info = json.load(f)
+        make_cli(info)
+        with open(os.path.join(HERE, "golden.json"), "w") as f:
+            json.dump(info, f, indent=1, sort_keys=True)
+            f.write("\n")
+        print("CLI fixtures written to", HERE)
+        return
     app = os.path.join(REPO, "oracle", "_ref", "phygas_wu")
     dump = os.path.join(REPO, "oracle", "_ref", "ref_dump")
     info = {"published": {}, "commands": {}}
@@ -94,6 +128,7 @@ def main():
             out = subprocess.check_output(argv)
             write_gz(os.path.join(HERE, "ref_dump_%s.txt.gz" % name), out)
             info["commands"]["ref_dump_" + name] = " ".join(args)
+    make_cli(info)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(info, f, indent=1, sort_keys=True)
         f.write("\n")

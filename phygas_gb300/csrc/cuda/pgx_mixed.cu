@@ -765,32 +765,96 @@ __device__ __forceinline__ void draw32(const Fin32 &g, uint64_t w, float &x, flo
     ex = fmaf(g.eA, fmaxf(a0, fmaxf(a1, a2)), fmaf(g.eE, fmaxf(e0, fmaxf(e1, e2)), g.eM));
 }
 
-__global__ void __launch_bounds__(256) k_mx_finish32(int n, const FinishIn *__restrict__ fin,
-                                                     ScreenRowDev *__restrict__ rows, int *__restrict__ nrecheck) {
-    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (h >= n) return;
+// The 512 draws of a kept pair, in two phases.  A draw's first coordinate x = mx + l00 z0 depends on its first
+// Gaussian alone, and |x| >= max(r50, rtot) puts the draw outside both spheres whatever z1 and z2 are (r >= |x|, in
+// the FP64 path's arithmetic as well).  Phase 1 draws z0 for all 512 and settles the draws whose x, less its error
+// bound (4 eps |mx| + |l00| (4 eps |z0| + e0 (1 + 2 eps)), the x row of draw32's bound), clears the larger radius;
+// with sigma of hundreds of pc against radii of tens, most do.  The rest are queued per warp in shared memory with
+// z0 and its bound, and phase 2 completes them 32 at a time on full warps: z1, z2, the position and its bound as
+// draw32 computes them, and the FP64 recheck of a draw within its bound of a radius -- the counts are the FP64
+// path's, and the same as drawing every draw in full.
+constexpr int kFinWarps = 8, kFinQueue = 64;
+
+__global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const FinishIn *__restrict__ fin,
+                                                                ScreenRowDev *__restrict__ rows,
+                                                                int *__restrict__ nrecheck) {
+    __shared__ int s_i[kFinWarps][kFinQueue];
+    __shared__ float s_z[kFinWarps][kFinQueue], s_a[kFinWarps][kFinQueue], s_e[kFinWarps][kFinQueue];
+    const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    if (h >= n) return;                                           // the whole warp: uniform
     const Fin32 g = fin32(fin[h], lane);
+    const uint64_t seed = fin[h].seed;
+    // the x row of the bound, and the larger radius with a margin for its rounding to FP32
+    const float eA0 = fabsf(g.l00) * (4.f * kEps32 * 1.000001f) * 1.000001f;
+    const float eE0 = fabsf(g.l00) * (1.f + 6.f * kEps32) * 1.000001f;
+    const float eM0 = fabsf(g.mx) * (4.f * kEps32) * 1.000001f;
+    const float rout = sqrtf(fmaxf(g.r50s, g.rts)) * (1.f + 1e-6f);
     int in50 = 0, intot = 0, rechecks = 0;
+    // phase 2 for queue entries [0, cnt), one per lane
+    auto complete = [&](int cnt) {
+        __syncwarp();
+        if (lane < cnt) {
+            const int i = s_i[wq][lane];
+            const float z0 = s_z[wq][lane], a0 = s_a[wq][lane], e0 = s_e[wq][lane];
+            const uint64_t w = seed + (uint64_t)(6 * i) * kGolden;
+            float z1, z2, a1, a2, e1, e2;
+            gauss32(splitmix_mix(w + 3 * kGolden), splitmix_mix(w + 4 * kGolden), z1, a1, e1);
+            gauss32(splitmix_mix(w + 5 * kGolden), splitmix_mix(w + 6 * kGolden), z2, a2, e2);
+            const float x = fmaf(g.l00, z0, g.mx);
+            const float y = fmaf(g.l11, z1, fmaf(g.l10, z0, g.my));
+            const float z = fmaf(g.l22, z2, fmaf(g.l21, z1, fmaf(g.l20, z0, g.mz)));
+            const float ex = fmaf(g.eA, fmaxf(a0, fmaxf(a1, a2)), fmaf(g.eE, fmaxf(e0, fmaxf(e1, e2)), g.eM));
+            const float r2 = fmaf(x, x, fmaf(y, y, z * z));
+            const float x1 = fabsf(x) + fabsf(y) + fabsf(z);
+            const float er = 3.f * kEps32 * r2 + 2.f * x1 * ex + 3.f * ex * ex;
+            const float d50 = r2 - g.r50s, dt = r2 - g.rts;
+            if (fabsf(d50) > er + g.e50 && fabsf(dt) > er + g.etot) {
+                in50 += d50 < 0.f;
+                intot += dt < 0.f;
+            } else {
+                const int v = draw_inside64(fin[h], i);             // the FP64 path's own draw
+                in50 += v & 1;
+                intot += v >> 1;
+                rechecks++;
+            }
+        }
+        __syncwarp();
+    };
     // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden
-    uint64_t w = fin[h].seed + (uint64_t)(6 * lane) * kGolden;
+    uint64_t w = seed + (uint64_t)(6 * lane) * kGolden;
+    int qn = 0;
 #pragma unroll 1
     for (int q = 0; q < 16; q++, w += 192 * kGolden) {
-        float x, y, z, ex;
-        draw32(g, w, x, y, z, ex);
-        const float r2 = fmaf(x, x, fmaf(y, y, z * z));
-        const float x1 = fabsf(x) + fabsf(y) + fabsf(z);
-        const float er = 3.f * kEps32 * r2 + 2.f * x1 * ex + 3.f * ex * ex;
-        const float d50 = r2 - g.r50s, dt = r2 - g.rts;
-        if (fabsf(d50) > er + g.e50 && fabsf(dt) > er + g.etot) {
-            in50 += d50 < 0.f;
-            intot += dt < 0.f;
-        } else {
-            const int v = draw_inside64(fin[h], lane + 32 * q);      // the FP64 path's own draw
-            in50 += v & 1;
-            intot += v >> 1;
-            rechecks++;
+        float z0, a0, e0;
+        gauss32(splitmix_mix(w + kGolden), splitmix_mix(w + 2 * kGolden), z0, a0, e0);
+        const float x = fmaf(g.l00, z0, g.mx);
+        const float ex0 = fmaf(eA0, a0, fmaf(eE0, e0, eM0));
+        const bool open = !(fabsf(x) * (1.f - 4.f * kEps32) - ex0 >= rout);
+        const unsigned m = __ballot_sync(0xffffffffu, open);
+        if (open) {
+            const int at = qn + __popc(m & ((1u << lane) - 1u));
+            s_i[wq][at] = lane + 32 * q;
+            s_z[wq][at] = z0;
+            s_a[wq][at] = a0;
+            s_e[wq][at] = e0;
+        }
+        qn += __popc(m);
+        if (qn >= 32) {
+            complete(32);
+            const int rest = qn - 32;
+            int vi = 0;
+            float vz = 0.f, va = 0.f, ve = 0.f;
+            if (lane < rest) {
+                vi = s_i[wq][32 + lane]; vz = s_z[wq][32 + lane]; va = s_a[wq][32 + lane]; ve = s_e[wq][32 + lane];
+            }
+            __syncwarp();
+            if (lane < rest) {
+                s_i[wq][lane] = vi; s_z[wq][lane] = vz; s_a[wq][lane] = va; s_e[wq][lane] = ve;
+            }
+            qn = rest;
         }
     }
+    if (qn > 0) complete(qn);
     in50 = __reduce_add_sync(0xffffffffu, in50);
     intot = __reduce_add_sync(0xffffffffu, intot);
     rechecks = __reduce_add_sync(0xffffffffu, rechecks);
@@ -833,7 +897,7 @@ int mixed_finish(cudaStream_t st, int n, const FinishIn *fin, ScreenRowDev *rows
     if ((rc = grow(m.total, 64, m.err))) return rc;
     int *cnt = Pb<int>(m.total) + 8;
     if ((rc = check(cudaMemsetAsync(cnt, 0, 4, st), m.err, "memset"))) return rc;
-    k_mx_finish32<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(n, fin, rows, cnt);
+    k_mx_finish32<<<(unsigned)(((size_t)n + kFinWarps - 1) / kFinWarps), kFinWarps * 32, 0, st>>>(n, fin, rows, cnt);
     if (stats) stats->kernels += 0;     // counted with the finish prep by the caller
     if ((rc = check(cudaGetLastError(), m.err, "k_mx_finish32"))) return rc;
     int h = 0;

@@ -35,12 +35,18 @@ struct Buf {
     size_t cap = 0;
 };
 
-enum { EV_START, EV_ORBIT, EV_COV, EV_SCAN, EV_SELECT, EV_FINISH, EV_PAIR0, EV_PAIR1, EV_N };
+enum { EV_START, EV_ORBIT, EV_COV, EV_SCREEN, EV_SCAN, EV_SELECT, EV_FINISH, EV_PAIR0, EV_PAIR1, EV_N };
 
 }  // namespace
 
 // One staged chunk of stars: inputs (SoA), orbit scratch, the tracks the screen reads, the ids of the text lines,
 // and the event that marks its tracks done
+// Blocks per SM of a chunk's orbits traced beside another chunk's screen: few enough to leave the screen its
+// registers (its FP32 and integer work and the orbits' FP64 work use different pipes), enough to finish first.
+constexpr int kSideOrbitBlocksPerSm = 2;
+// pgx_screen_stage splits chunks of at least this many stars in two, so that exec can overlap them
+constexpr int kSplitStars = 8192;
+
 struct TrackSlot {
     int nt = 0, ns = 0;
     Buf ps0, sig21, prefix, opos, ovel, t64, t32, tlm, ids;
@@ -59,6 +65,7 @@ struct PgxContext {
     // previous chunk is screened (pgx_screen_chunks); the single-chunk entry points use slot `cur`
     TrackSlot trk[2];
     int cur = 0;
+    int split = 0;                             // > 0: pgx_screen_stage put stars [0, split) in slot 0, the rest in 1
     cudaStream_t side = nullptr;               // higher priority: the orbits' blocks start as soon as SMs free up
     // the screen's work buffers
     Buf chi2T, kbT, sbT, cnt, off, total, kept, fin, rows;
@@ -166,7 +173,7 @@ int run_lin(PgxContext *ctx, cudaStream_t st, int N, const double *d_ps0, const 
 
 pgx::ScreenTables tables(PgxContext *ctx, TrackSlot &k) {
     pgx::ScreenTables T;
-    T.nt = k.nt; T.ns = k.ns; T.nc = ctx->nc; T.ncp = ctx->ncp;
+    T.nt = k.nt; T.ns = k.ns; T.nc = ctx->nc; T.ncp = ctx->ncp; T.s_off = 0;
     T.t64 = P<double>(k.t64); T.t32 = P<float4>(k.t32); T.lm_t = P<float>(k.tlm);
     T.seed_prefix = P<uint64_t>(k.prefix);
     T.c64 = P<double>(ctx->c64); T.c32 = P<float4>(ctx->c32); T.lm_c = P<float>(ctx->clm); T.cn = P<int>(ctx->cn);
@@ -219,10 +226,27 @@ int tracks_slot(PgxContext *ctx, int s, double tmax_myr, cudaStream_t st, bool t
     return 0;
 }
 
+// ctx->rows with room for `rows` rows, the first `keep` of them kept
+int rows_room(PgxContext *ctx, long keep, long rows) {
+    const size_t need = (size_t)rows * sizeof(pgx::ScreenRowDev);
+    if (ctx->rows.cap >= need) return 0;
+    Buf old = ctx->rows;
+    ctx->rows = Buf();
+    RET(ensure(ctx, ctx->rows, need));
+    if (keep > 0)
+        CK(cudaMemcpyAsync(ctx->rows.p, old.p, (size_t)keep * sizeof(pgx::ScreenRowDev), cudaMemcpyDeviceToDevice,
+                           ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    if (old.p) CK(cudaFree(old.p));
+    return 0;
+}
+
 // The screen of slot s on the main stream, after its tracks (which may run on another stream): the scan, the
-// selection of the kept pairs and their 512 draws; the rows stay on the device (ctx->rows, *n_rows of them).
+// selection of the kept pairs and their 512 draws; the rows stay on the device (ctx->rows, *n_rows of them from row
+// row_off on, star indices star_off + the slot's).
 // tracks_timed: the tracks ran on the main stream right before, timed by EV_START / EV_ORBIT / EV_COV.
-int screen_slot(PgxContext *ctx, int s, double cut, int precision, long *n_rows, bool tracks_timed) {
+int screen_slot(PgxContext *ctx, int s, double cut, int precision, long *n_rows, bool tracks_timed, long row_off = 0,
+                int star_off = 0) {
     TrackSlot &k = ctx->trk[s];
     const int nt = k.nt, nc = ctx->nc, ns = k.ns;
     CK(cudaStreamWaitEvent(ctx->st, k.done, 0));
@@ -230,7 +254,9 @@ int screen_slot(PgxContext *ctx, int s, double cut, int precision, long *n_rows,
         ctx->stats = PgxStats();
         for (int e : {EV_START, EV_ORBIT, EV_COV}) CK(cudaEventRecord(ctx->ev[e], ctx->st));
     }
+    CK(cudaEventRecord(ctx->ev[EV_SCREEN], ctx->st));
     pgx::ScreenTables T = tables(ctx, k);
+    T.s_off = star_off;
     int total = 0;
     if (precision == PGX_FP64) {
         const size_t pairs = (size_t)nt * nc;
@@ -264,19 +290,19 @@ int screen_slot(PgxContext *ctx, int s, double cut, int precision, long *n_rows,
         CK(cudaEventRecord(ctx->ev[EV_SELECT], ctx->st));
     }
     RET(ensure(ctx, ctx->fin, (size_t)total * sizeof(pgx::FinishIn)));
-    RET(ensure(ctx, ctx->rows, (size_t)total * sizeof(pgx::ScreenRowDev)));
+    RET(rows_room(ctx, row_off, row_off + total));
+    pgx::ScreenRowDev *rows = P<pgx::ScreenRowDev>(ctx->rows) + row_off;
     if (total > 0) {
         const pgx::KeptPair *kp = precision == PGX_FP64 ? P<pgx::KeptPair>(ctx->kept) : pgx::mixed_kept(ctx->mixed);
         pgx::k_finish_prep<<<(total + 127) / 128, 128, 0, ctx->st>>>(T, total, kp, P<pgx::FinishIn>(ctx->fin),
-                                                                     P<pgx::ScreenRowDev>(ctx->rows));
+                                                                     rows);
         CKL();
         if (precision == PGX_FP64) {
             pgx::k_finish64<<<(unsigned)(((size_t)total * 32 + 255) / 256), 256, 0, ctx->st>>>(
-                total, P<pgx::FinishIn>(ctx->fin), P<pgx::ScreenRowDev>(ctx->rows));
+                total, P<pgx::FinishIn>(ctx->fin), rows);
             CKL();
         } else {
-            MRET(pgx::mixed_finish(ctx->st, total, P<pgx::FinishIn>(ctx->fin), P<pgx::ScreenRowDev>(ctx->rows),
-                                  ctx->mixed, &ctx->stats));
+            MRET(pgx::mixed_finish(ctx->st, total, P<pgx::FinishIn>(ctx->fin), rows, ctx->mixed, &ctx->stats));
         }
         ctx->stats.kernels += 2;
     }
@@ -285,14 +311,14 @@ int screen_slot(PgxContext *ctx, int s, double cut, int precision, long *n_rows,
     PgxStats &S = ctx->stats;
     S.ms_orbit = elapsed(ctx, EV_START, EV_ORBIT);
     S.ms_cov = elapsed(ctx, EV_ORBIT, EV_COV);
-    S.ms_scan = elapsed(ctx, EV_COV, EV_SCAN);
+    S.ms_scan = elapsed(ctx, EV_SCREEN, EV_SCAN);
     S.ms_select = elapsed(ctx, EV_SCAN, EV_SELECT);
     S.ms_finish = elapsed(ctx, EV_SELECT, EV_FINISH);
     S.ms_total = elapsed(ctx, EV_START, EV_FINISH);
     S.pairs = (long)nt * nc;
     S.kept = total;
     S.body_steps = (long)nt * 7 * (ns - 1) * PH_LIN_SUB;
-    ctx->n_rows = total;
+    ctx->n_rows = row_off + total;
     if (n_rows) *n_rows = total;
     return 0;
 }
@@ -595,7 +621,16 @@ int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *s
     if (!ctx) return PGX_E_ARG;
     if (nt <= 0 || !ps0 || !sig || !prefix) return fail(ctx, PGX_E_ARG, "pgx_screen_stage: bad args");
     CK(cudaSetDevice(ctx->device));
-    return stage_slot(ctx, ctx->cur, nt, ps0, sig, prefix, nullptr, ctx->st);
+    ctx->cur = 0;
+    ctx->split = 0;
+    ctx->trk[1].nt = 0;
+    if (nt < kSplitStars) return stage_slot(ctx, 0, nt, ps0, sig, prefix, nullptr, ctx->st);
+    // two halves in the two track slots, for exec to trace the second beside the first's screen
+    const int n1 = nt / 2;
+    RET(stage_slot(ctx, 0, n1, ps0, sig, prefix, nullptr, ctx->st));
+    RET(stage_slot(ctx, 1, nt - n1, ps0 + (size_t)6 * n1, sig + (size_t)36 * n1, prefix + n1, nullptr, ctx->st));
+    ctx->split = n1;
+    return 0;
 }
 
 int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision, long *n_rows) {
@@ -608,7 +643,32 @@ int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision,
     ctx->stats = PgxStats();
     CK(cudaEventRecord(ctx->ev[EV_START], ctx->st));
     RET(tracks_slot(ctx, ctx->cur, tmax_myr, ctx->st, true));
-    return screen_slot(ctx, ctx->cur, cut, precision, n_rows, true);
+    if (ctx->split == 0) return screen_slot(ctx, ctx->cur, cut, precision, n_rows, true);
+    // a staged chunk in two halves: with the mixed screen the second half's orbits run on the side stream beside
+    // the first half's screen (FP64 pipe beside FP32 and integer work); the plain FP64 path runs them in turn
+    const bool overlap = precision == PGX_MIXED;
+    if (overlap) RET(tracks_slot(ctx, 1, tmax_myr, ctx->side, false, kSideOrbitBlocksPerSm * ctx->sms));
+    long na = 0, nb = 0;
+    RET(screen_slot(ctx, 0, cut, precision, &na, true));
+    const PgxStats a = ctx->stats;
+    if (!overlap) RET(tracks_slot(ctx, 1, tmax_myr, ctx->st, false));
+    RET(screen_slot(ctx, 1, cut, precision, &nb, true, na, ctx->split));
+    // the stages of both halves; the orbit and covariance times are the first half's (the second half's ran beside
+    // its screen, or in turn on the plain path)
+    PgxStats &S = ctx->stats;
+    S.ms_scan += a.ms_scan;
+    S.ms_select += a.ms_select;
+    S.ms_finish += a.ms_finish;
+    S.pairs += a.pairs;
+    S.kept += a.kept;
+    S.body_steps += a.body_steps;
+    S.candidates += a.candidates;
+    S.ambiguous += a.ambiguous;
+    S.rechecked_points += a.rechecked_points;
+    S.rechecked_draws += a.rechecked_draws;
+    S.kernels += a.kernels;
+    if (n_rows) *n_rows = na + nb;
+    return 0;
 }
 
 int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n) {
@@ -658,10 +718,6 @@ int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *si
 }  // extern "C"
 
 namespace {
-// Blocks per SM of a chunk's orbits traced beside the previous chunk's screen: few enough to leave the screen its
-// registers (its FP32 and integer work and the orbits' FP64 work use different pipes), enough to finish first.
-constexpr int kSideOrbitBlocksPerSm = 2;
-
 // Rows or text out of the chunk pipeline (pgx_screen_chunks, pgx_screen_chunks_text).
 struct ChunkOut {
     int (*rows)(void *arg, int first, const PgxScreenRow *rows, long n) = nullptr;
@@ -834,6 +890,9 @@ int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n
         cv.notify_all();
     }
     if (gpu.joinable()) gpu.join();
+    // the slots hold pipeline chunks now, not a pgx_screen_stage chunk
+    ctx->split = 0;
+    ctx->trk[0].nt = ctx->trk[1].nt = 0;
     // codes set here, after the worker has ended, so that the message is this function's
     if (rc == PGX_E_ARG) rc = fail(ctx, PGX_E_ARG, "screen chunks: the output callback stopped the run");
     else if (rc == PGX_E_CUDA) rc = fail(ctx, PGX_E_CUDA, "screen chunks: copy to the host failed");
@@ -1136,7 +1195,7 @@ int pair_tables(PgxContext *ctx, const PhLin *tl, const PhLin *cl, const PhClust
     CK(cudaMemcpyAsync(base, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemcpyAsync(base + h.size() * 8, &aux, sizeof aux, cudaMemcpyHostToDevice, ctx->st));
     const char *a = base + h.size() * 8;
-    T.nt = 1; T.ns = tl->n; T.nc = 1; T.ncp = cl->n;
+    T.nt = 1; T.ns = tl->n; T.nc = 1; T.ncp = cl->n; T.s_off = 0;
     T.t64 = (const double *)base;
     T.c64 = (const double *)base + (size_t)nmax * 12;
     T.t32 = nullptr; T.c32 = nullptr; T.lm_t = nullptr; T.lm_c = nullptr;

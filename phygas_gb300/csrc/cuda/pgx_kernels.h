@@ -44,6 +44,7 @@ struct ScreenTables {
     const int *cn;
     const double *R2, *r50, *rtot;
     const char *cname;               // nc * 40 bytes
+    int s_off;                       // added to the star index of the rows written (a chunk screened in parts)
 };
 
 // one pair kept past the chi2 cut, in (star, cluster) order

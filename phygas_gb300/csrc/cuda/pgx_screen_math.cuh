@@ -85,7 +85,7 @@ __device__ __forceinline__ void finish_prep_pair(const ScreenTables &T, const Ke
     double C[6];
 #pragma unroll
     for (int i = 0; i < 6; i++) C[i] = ta[(6 + i) * NT] + ca[(6 + i) * NC];
-    r.star = p.s; r.cluster = p.c; r.kb = kb; r.pad = 0; r.sb = sb; r.chi2 = p.chi2;
+    r.star = p.s + T.s_off; r.cluster = p.c; r.kb = kb; r.pad = 0; r.sb = sb; r.chi2 = p.chi2;
     r.t_myr = ((double)kb + sb) * kStepMyr;
     r.d_nom_pc = sqrt(mx * mx + my * my + mz * mz) * 1000.0;
     r.vrel_kms = sqrt(vx * vx + vy * vy + vz * vz) * kKms;

@@ -202,3 +202,24 @@ def test_screen_chunks_text_is_printf_of_the_rows(ctx, golden):
         assert b"".join(got) == want, chunk
     with pytest.raises(pg.GpuError):
         ctx.screen_chunks_text(stars, clusters[:10], 64, tmax, lambda *a: None)     # not the resident table
+
+
+def test_split_chunk_equals_unsplit(ctx, golden):
+    """A staged chunk of at least 8,192 stars is screened in two halves (the second half's orbits beside the first
+    half's screen): its rows -- star indices across the halves, their order, every field -- equal the same chunk
+    screened whole through pgx_screen_chunks, in both precisions."""
+    from phygas_gb300 import synth
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "screen", 9001, 1006, 1000)
+        clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    ctx.set_clusters(clusters)
+    tmax = max(c.tmax_myr for c in clusters)
+    for prec in PRECISIONS:
+        split = ctx.screen(*pg.draw_targets(stars), tmax, 25.0, prec)
+        whole = []
+        ctx.screen_chunks(stars, len(stars), tmax, lambda first, rows: whole.append(np.array(rows, copy=True)),
+                          25.0, prec)
+        assert len(whole) == 1 and len(split) > 10000
+        assert split["star"].max() > len(stars) // 2                 # rows from both halves
+        assert split.tobytes() == whole[0].tobytes(), prec

@@ -490,7 +490,7 @@ def main():
 
     s = stats[-1]
     orbit_ms = statistics.mean(x["ms_orbit"] for x in stats)
-    achieved = FLOPS_PER_BODY_STEP * s["body_steps"] / (orbit_ms * 1e-3)
+    achieved = FLOPS_PER_BODY_STEP * s["orbit_body_steps"] / (orbit_ms * 1e-3)
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -523,7 +523,9 @@ def main():
                          "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
                          "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
                          "traffic": ORBIT_TRAFFIC_BYTES, "flops_per_body_step": FLOPS_PER_BODY_STEP,
-                         "body_steps_per_launch": s["body_steps"], "ms_per_launch": orbit_ms},
+                         "body_steps_per_launch": s["orbit_body_steps"], "ms_per_launch": orbit_ms,
+                         "launch": "the orbits of the first half of the chunk (the second half's run beside the "
+                                   "first half's screen)"},
             "fp32_peak_tflops": fp32_peak / 1e12,
             "cluster_table_s": table_s,
             "gpu_launches": int(sum(x["kernels"] for x in stats)),

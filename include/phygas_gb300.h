@@ -168,6 +168,8 @@ typedef struct {
     long ambiguous;                  /* mixed screen: pairs that may be kept (candidates) whose candidate points
                                         were found by a second walk; rechecked_points = points evaluated in FP64 */
     int kernels;                     /* kernel launches of the call */
+    long orbit_body_steps;           /* body steps of the orbit launch that ms_orbit times (a chunk screened in two
+                                        halves times the first half's; the second's runs beside the first's screen) */
 } PgxStats;
 int pgx_stats(const PgxContext *ctx, PgxStats *out);
 

@@ -50,7 +50,8 @@ class PgxStats(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("ms_total", "ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish",
                                           "ms_pair")] + [
         (k, C.c_long) for k in ("pairs", "kept", "candidates", "rechecked_points", "rechecked_draws", "clones",
-                                "clone_steps", "body_steps", "ambiguous")] + [("kernels", C.c_int)]
+                                "clone_steps", "body_steps", "ambiguous")] + [("kernels", C.c_int),
+                                                                               ("orbit_body_steps", C.c_long)]
 
 
 ROW_DTYPE = np.dtype([("star", "i4"), ("cluster", "i4"), ("kb", "i4"), ("pad", "i4"), ("sb", "f8"), ("chi2", "f8"),

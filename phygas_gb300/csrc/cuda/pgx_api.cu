@@ -318,6 +318,7 @@ int screen_slot(PgxContext *ctx, int s, double cut, int precision, long *n_rows,
     S.pairs = (long)nt * nc;
     S.kept = total;
     S.body_steps = (long)nt * 7 * (ns - 1) * PH_LIN_SUB;
+    S.orbit_body_steps = S.body_steps;
     ctx->n_rows = row_off + total;
     if (n_rows) *n_rows = total;
     return 0;
@@ -662,6 +663,7 @@ int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision,
     S.pairs += a.pairs;
     S.kept += a.kept;
     S.body_steps += a.body_steps;
+    S.orbit_body_steps = a.body_steps;
     S.candidates += a.candidates;
     S.ambiguous += a.ambiguous;
     S.rechecked_points += a.rechecked_points;

@@ -38,6 +38,8 @@ CHI2_MAX, N_SAMP, R_KERNEL = 25.0, 64, 2.0
 # executed FP64 instructions of k_stm_orbits per body step: 36.0 DFMA + 3.0 DADD + 29.0 DMUL (ncu sass op counters of
 # the 2,000-star screen of `python -m phygas_gb300.run_pairs`, FMA = 2 flops)
 FLOPS_PER_BODY_STEP = 104.0
+# the same count as FP64 instructions (each takes one FP64-pipe slot, whatever its flops)
+FP64_INSTR_PER_BODY_STEP = 36.0 + 3.0 + 29.0
 # the same for one clone-step of the pair Monte Carlo (two body steps and the segment test), from k_pair_mc_t on the
 # batch of `python -m phygas_gb300.run_pairs` (4,052 pairs, 1.49e9 clone-steps): 79.0 DFMA + 12.2 DADD + 65.5 DMUL
 FLOPS_PER_CLONE_STEP = 235.7
@@ -423,8 +425,14 @@ def main():
     with Clocks(local) as clk:
         per, stats, n_rows = run(precision, args.steps, args.warmup)
     rows_mixed = ctx.fetch(n_rows)
+    # the plain FP64 comparator: the chunk whole, every stage in turn (no halves, no overlap); its orbit launch is
+    # also the roofline's (the whole chunk on the whole GPU)
+    ctx.set_split(0)
+    ctx.stage(ps0, sig, pre)
     per64, stats64, n_rows64 = run(pg.PGX_FP64, max(2, min(args.steps, 3)), 1)
     rows_fp64 = ctx.fetch(n_rows64)
+    ctx.set_split(8192)
+    ctx.stage(ps0, sig, pre)
     accuracy = {"screen": compare_rows(rows_mixed, rows_fp64)}
     del rows_mixed, rows_fp64
     if rank == 0 and not args.no_control:
@@ -488,9 +496,9 @@ def main():
         except Exception as e:          # reported beside the headline, not part of it
             log("serving measurement failed: %s" % e)
 
-    s = stats[-1]
-    orbit_ms = statistics.mean(x["ms_orbit"] for x in stats)
-    achieved = FLOPS_PER_BODY_STEP * s["orbit_body_steps"] / (orbit_ms * 1e-3)
+    s, s64 = stats[-1], stats64[-1]
+    orbit_ms = statistics.mean(x["ms_orbit"] for x in stats64)
+    achieved = FLOPS_PER_BODY_STEP * s64["orbit_body_steps"] / (orbit_ms * 1e-3)
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -523,9 +531,14 @@ def main():
                          "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
                          "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
                          "traffic": ORBIT_TRAFFIC_BYTES, "flops_per_body_step": FLOPS_PER_BODY_STEP,
-                         "body_steps_per_launch": s["orbit_body_steps"], "ms_per_launch": orbit_ms,
-                         "launch": "the orbits of the first half of the chunk (the second half's run beside the "
-                                   "first half's screen)"},
+                         "body_steps_per_launch": s64["orbit_body_steps"], "ms_per_launch": orbit_ms,
+                         "launch": "the orbits of the whole chunk (the plain FP64 run's launch; the same kernel "
+                                   "as the mixed path's)",
+                         "fp64_instr_frac": FP64_INSTR_PER_BODY_STEP * s64["orbit_body_steps"] / (orbit_ms * 1e-3)
+                                            / (fp64_peak / 2),
+                         "fp64_instr_note": "FP64 instructions issued / the FMA instruction rate: DADD and DMUL take "
+                                            "a full slot for one flop, so the flop fraction understates how busy the "
+                                            "pipe is"},
             "fp32_peak_tflops": fp32_peak / 1e12,
             "cluster_table_s": table_s,
             "gpu_launches": int(sum(x["kernels"] for x in stats)),

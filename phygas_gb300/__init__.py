@@ -102,6 +102,7 @@ SIGNATURES = [
     ("pgx_screen_into", C.c_int, [C.c_void_p, C.c_int, _D, _D, _U64, C.c_double, C.c_double, C.c_int, C.c_void_p,
                                   C.c_long, _P(C.c_long)]),
     ("pgx_host_alloc", C.c_void_p, [C.c_size_t]),
+    ("pgx_screen_split", C.c_int, [C.c_void_p, C.c_int]),
     ("pgx_screen_chunks", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                     C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     ("pgx_host_free", None, [C.c_void_p]),
@@ -360,6 +361,11 @@ class Context:
         if err:
             raise err[0]
         self._check(rc, "pgx_screen_chunks_text")
+
+    def set_split(self, min_stars):
+        """pgx_screen_split: stage chunks of at least min_stars stars as two halves, screened with the second
+        half's orbits beside the first half's screen (0 = never)."""
+        self._check(lib().pgx_screen_split(self.h, int(min_stars)), "pgx_screen_split")
 
     def stage(self, ps0, sig, prefix):
         self._keep = (np.ascontiguousarray(ps0, np.float64), np.ascontiguousarray(sig, np.float64),

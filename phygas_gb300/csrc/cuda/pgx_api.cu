@@ -51,6 +51,8 @@ struct TrackSlot {
     int nt = 0, ns = 0;
     Buf ps0, sig21, prefix, opos, ovel, t64, t32, tlm, ids;
     cudaEvent_t done = nullptr;
+    char *h_stage = nullptr;                   // page-locked staging of the inputs (SoA), reused
+    size_t h_stage_cap = 0;
 };
 
 struct PgxContext {
@@ -66,6 +68,7 @@ struct PgxContext {
     TrackSlot trk[2];
     int cur = 0;
     int split = 0;                             // > 0: pgx_screen_stage put stars [0, split) in slot 0, the rest in 1
+    int split_min = kSplitStars;               // chunks of at least this many stars are split (0: never)
     cudaStream_t side = nullptr;               // higher priority: the orbits' blocks start as soon as SMs free up
     // the screen's work buffers
     Buf chi2T, kbT, sbT, cnt, off, total, kept, fin, rows;
@@ -138,10 +141,8 @@ template <class T> T *P(Buf &b) { return reinterpret_cast<T *>(b.p); }
 int npts_of(double tmax) { return (int)std::ceil(tmax / PH_PRE_STEP_MYR) + 1; }
 
 // ps0 [n][6] -> [6][n]; sig [n][36] -> the 21 upper-triangle entries [21][n]
-void to_soa(int n, const double *ps0, const double *sig, std::vector<double> &p6, std::vector<double> &s21,
-            const int *order = nullptr) {
-    p6.resize((size_t)6 * n);
-    s21.resize((size_t)21 * n);
+// per-object ps0[6] and Sigma0[6][6] -> SoA p6[6][n] and the upper triangle s21[21][n] (slot order: order[slot])
+void to_soa_into(int n, const double *ps0, const double *sig, double *p6, double *s21, const int *order = nullptr) {
     for (int slot = 0; slot < n; slot++) {
         const int i = order ? order[slot] : slot;
         for (int c = 0; c < 6; c++) p6[(size_t)c * n + slot] = ps0[(size_t)6 * i + c];
@@ -149,6 +150,13 @@ void to_soa(int n, const double *ps0, const double *sig, std::vector<double> &p6
         for (int a = 0; a < 6; a++)
             for (int b = a; b < 6; b++) s21[(size_t)q++ * n + slot] = sig[(size_t)36 * i + 6 * a + b];
     }
+}
+
+void to_soa(int n, const double *ps0, const double *sig, std::vector<double> &p6, std::vector<double> &s21,
+            const int *order = nullptr) {
+    p6.resize((size_t)6 * n);
+    s21.resize((size_t)21 * n);
+    to_soa_into(n, ps0, sig, p6.data(), s21.data(), order);
 }
 
 // nominal + neighbour orbits of N objects (ps0 / sig21 device SoA, npts per slot or uniform) into t64 / t32
@@ -188,22 +196,35 @@ float elapsed(PgxContext *ctx, int a, int b) {
     return ms;
 }
 
-// Host inputs of nt stars (and, for text lines, their 40-byte ids) into track slot s, copied on stream st.
+// Host inputs of nt stars (and, for text lines, their 40-byte ids) into track slot s, copied on stream st from the
+// slot's page-locked staging area.
 int stage_slot(PgxContext *ctx, int s, int nt, const double *ps0, const double *sig, const uint64_t *prefix,
                const char *ids, cudaStream_t st) {
     if (nt > (1 << 20)) return fail(ctx, PGX_E_LIMIT, "pgx_screen_stage: %d stars in one chunk (limit 2^20)", nt);
     TrackSlot &k = ctx->trk[s];
-    std::vector<double> p6, s21;
-    to_soa(nt, ps0, sig, p6, s21);
-    RET(ensure(ctx, k.ps0, p6.size() * 8));
-    RET(ensure(ctx, k.sig21, s21.size() * 8));
-    RET(ensure(ctx, k.prefix, (size_t)nt * 8));
-    CK(cudaMemcpyAsync(k.ps0.p, p6.data(), p6.size() * 8, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(k.sig21.p, s21.data(), s21.size() * 8, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(k.prefix.p, prefix, (size_t)nt * 8, cudaMemcpyHostToDevice, st));
+    const size_t b6 = (size_t)6 * nt * 8, b21 = (size_t)21 * nt * 8, bp = (size_t)nt * 8;
+    const size_t bi = ids ? (size_t)40 * nt : 0;
+    if (k.h_stage_cap < b6 + b21 + bp + bi) {
+        pgx_host_free(k.h_stage);
+        k.h_stage_cap = 0;
+        const size_t cap = b6 + b21 + bp + (size_t)40 * nt;
+        k.h_stage = (char *)pgx_host_alloc(cap);
+        if (!k.h_stage) return fail(ctx, PGX_E_NOMEM, "pgx_screen_stage: %zu bytes of page-locked memory", cap);
+        k.h_stage_cap = cap;
+    }
+    double *p6 = reinterpret_cast<double *>(k.h_stage), *s21 = p6 + (size_t)6 * nt;
+    to_soa_into(nt, ps0, sig, p6, s21);
+    memcpy(k.h_stage + b6 + b21, prefix, bp);
+    if (ids) memcpy(k.h_stage + b6 + b21 + bp, ids, bi);
+    RET(ensure(ctx, k.ps0, b6));
+    RET(ensure(ctx, k.sig21, b21));
+    RET(ensure(ctx, k.prefix, bp));
+    CK(cudaMemcpyAsync(k.ps0.p, p6, b6, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(k.sig21.p, s21, b21, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(k.prefix.p, k.h_stage + b6 + b21, bp, cudaMemcpyHostToDevice, st));
     if (ids) {
-        RET(ensure(ctx, k.ids, (size_t)40 * nt));
-        CK(cudaMemcpyAsync(k.ids.p, ids, (size_t)40 * nt, cudaMemcpyHostToDevice, st));
+        RET(ensure(ctx, k.ids, bi));
+        CK(cudaMemcpyAsync(k.ids.p, k.h_stage + b6 + b21 + bp, bi, cudaMemcpyHostToDevice, st));
     }
     CK(cudaStreamSynchronize(st));
     k.nt = nt;
@@ -381,6 +402,7 @@ void pgx_close(PgxContext *ctx) {
         for (Buf *b : {&k.ps0, &k.sig21, &k.prefix, &k.opos, &k.ovel, &k.t64, &k.t32, &k.tlm, &k.ids})
             if (b->p) cudaFree(b->p);
         if (k.done) cudaEventDestroy(k.done);
+        if (k.h_stage) cudaFreeHost(k.h_stage);
     }
     for (auto *h : ctx->h_buf)
         if (h) cudaFreeHost(h);
@@ -625,12 +647,19 @@ int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *s
     ctx->cur = 0;
     ctx->split = 0;
     ctx->trk[1].nt = 0;
-    if (nt < kSplitStars) return stage_slot(ctx, 0, nt, ps0, sig, prefix, nullptr, ctx->st);
+    if (ctx->split_min <= 0 || nt < ctx->split_min) return stage_slot(ctx, 0, nt, ps0, sig, prefix, nullptr, ctx->st);
     // two halves in the two track slots, for exec to trace the second beside the first's screen
     const int n1 = nt / 2;
     RET(stage_slot(ctx, 0, n1, ps0, sig, prefix, nullptr, ctx->st));
     RET(stage_slot(ctx, 1, nt - n1, ps0 + (size_t)6 * n1, sig + (size_t)36 * n1, prefix + n1, nullptr, ctx->st));
     ctx->split = n1;
+    return 0;
+}
+
+int pgx_screen_split(PgxContext *ctx, int min_stars) {
+    if (!ctx) return PGX_E_ARG;
+    if (min_stars < 0) return fail(ctx, PGX_E_ARG, "pgx_screen_split: %d", min_stars);
+    ctx->split_min = min_stars;
     return 0;
 }
 

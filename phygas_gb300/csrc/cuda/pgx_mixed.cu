@@ -6,10 +6,11 @@
 // FP32 value with a rigorous error bound.  Only what the bound cannot decide is recomputed with the FP64 path's own
 // functions (pgx_screen_math.cuh), so the rows are the FP64 path's rows bit for bit:
 //
-//   k_mx_scan32      FP32 filter, one thread per pair (warp = 32 stars x one cluster).  Per point: the reference's
-//                    trace bound (chi2 >= dist^2 / trace M), then bounds LB <= chi2_64 <= UB on the FP64 path's
-//                    value (a Rayleigh lower bound that needs no inversion, and an LDL^T solve where it is well
-//                    conditioned).
+//   k_mx_scan32      FP32 filter, one thread per pair (warp = 32 stars x one cluster).  Per point: a cheap skip
+//                    test (triangle inequality in the M^-1 norm, one FP32 LDL^T) that settles most points; the rest
+//                    are queued per warp for the bounds LB <= chi2_64 <= UB on the FP64 path's value (the
+//                    reference's trace bound, a Rayleigh lower bound that needs no inversion, and an LDL^T solve
+//                    where it is well conditioned), 32 at a time on full warps.
 //                    Per pair: its candidate points -- those that can be the FP64 minimum of a kept pair
 //                    (LB_k < cut, LB_k <= min UB) -- in four slots, or "more than four".
 //   k_mx_count / k_mx_emit   stable compaction, per star, of the pairs that may be kept
@@ -18,8 +19,9 @@
 //   k_mx_eval64      one thread per candidate point: the FP64 point chi2 (full warps on the scarce FP64 pipe)
 //   k_mx_best        per possible pair: FP64 argmin over its candidates (smallest value, first point of equals)
 //   k_mx_kept_*      stable compaction of the pairs under the cut
-//   k_mx_finish32    one warp per kept pair: the 512 draws in FP32 with a per-draw error bound; a draw whose
-//                    distance is within the bound of r50 or rtot is redone in FP64
+//   k_mx_finish32    one warp per kept pair: the 512 draws in FP32 with a per-draw error bound, in two phases (the
+//                    first Gaussian settles the draws far outside both radii; the rest are completed from a
+//                    per-warp queue); a draw whose distance is within the bound of r50 or rtot is redone in FP64
 #include <algorithm>
 #include <vector>
 #include "pgx_bits.cuh"

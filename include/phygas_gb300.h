@@ -150,6 +150,9 @@ int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const doub
                   const double *dt, const double *r50_pc, const double *rtot_pc, double *ms, int *best);
 /* number of launch shapes; the first n as (warps per block, clones per lane, minimum resident blocks per SM) */
 int pgx_pair_shapes(int n, int *warps, int *clones_per_lane, int *min_blocks);
+/* The persistent clone kernels of this context on at most blocks_per_sm blocks per SM (0 = as many as fit, the
+ * default): leaves registers for other contexts' kernels to run beside them -- the request loop's slots. */
+int pgx_pair_blocks(PgxContext *ctx, int blocks_per_sm);
 
 /* pgx_pair for callers that cannot allocate GPU memory (no counterpart in the reference): code running inside
  * another framework's device memory pool, loops that must not stall on the allocator, hosts that can only hand

@@ -103,6 +103,7 @@ SIGNATURES = [
                                   C.c_long, _P(C.c_long)]),
     ("pgx_host_alloc", C.c_void_p, [C.c_size_t]),
     ("pgx_screen_split", C.c_int, [C.c_void_p, C.c_int]),
+    ("pgx_pair_blocks", C.c_int, [C.c_void_p, C.c_int]),
     ("pgx_screen_chunks", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                     C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     ("pgx_host_free", None, [C.c_void_p]),
@@ -361,6 +362,10 @@ class Context:
         if err:
             raise err[0]
         self._check(rc, "pgx_screen_chunks_text")
+
+    def pair_blocks(self, blocks_per_sm):
+        """pgx_pair_blocks: the persistent clone kernels on at most blocks_per_sm blocks per SM (0 = all that fit)."""
+        self._check(lib().pgx_pair_blocks(self.h, int(blocks_per_sm)), "pgx_pair_blocks")
 
     def set_split(self, min_stars):
         """pgx_screen_split: stage chunks of at least min_stars stars as two halves, screened with the second

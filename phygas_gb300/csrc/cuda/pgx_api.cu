@@ -84,6 +84,7 @@ struct PgxContext {
     // pair Monte Carlo
     Buf p_off, p_ps, p_steps, p_dt, p_r50, p_rt, p_items, p_q, p_done, p_cres, p_res, p_params;
     int mc_variant = 0;                        // launch shape of the clone kernel (pgx_tune_pair picks it)
+    int mc_blocks_per_sm = 0;                  // > 0: the persistent clone kernels on at most this many blocks per SM
     cudaGraphExec_t mc_exec[16] = {};          // prep + trace + reduce, captured once per shape, replayed
     // one-object helpers of the drop-in API
     Buf x_ps0, x_sig21, x_npts, x_opos, x_ovel, x_t64, x_t32, x_lm;
@@ -1004,6 +1005,7 @@ int mc_graph(PgxContext *ctx, int v, cudaGraphExec_t &exec) {
     RET(ensure(ctx, ctx->p_params, sizeof(pgx::McPairs)));
     int grid = 0;
     CK(pgx::mc_variant_grid(v, ctx->sms, grid));
+    if (ctx->mc_blocks_per_sm > 0) grid = std::min(grid, ctx->mc_blocks_per_sm * ctx->sms);
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
     const cudaError_t le = pgx::launch_mc(v, grid, ctx->sms * 4, ctx->sms * 8, ctx->st,
@@ -1101,6 +1103,7 @@ int pair_run(PgxContext *ctx, int variant, int n_pairs, const int *clone_off, co
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pgx::k_pair_mc, pgx::kMcThreads, 0));
             const int warps_needed = (int)items.size();
             int grid = std::max(1, ctx->sms * std::max(1, per_sm));
+            if (ctx->mc_blocks_per_sm > 0) grid = std::min(grid, ctx->mc_blocks_per_sm * ctx->sms);
             grid = std::min(grid, (warps_needed + pgx::kMcThreads / 32 - 1) / (pgx::kMcThreads / 32));
             pgx::k_pair_mc<<<grid, pgx::kMcThreads, 0, ctx->st>>>(Pp);
             CKL();
@@ -1155,6 +1158,19 @@ int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const doub
     }
     ctx->mc_variant = b;
     if (best) *best = b;
+    return 0;
+}
+
+int pgx_pair_blocks(PgxContext *ctx, int blocks_per_sm) {
+    if (!ctx) return PGX_E_ARG;
+    if (blocks_per_sm < 0) return fail(ctx, PGX_E_ARG, "pgx_pair_blocks: %d", blocks_per_sm);
+    CK(cudaSetDevice(ctx->device));
+    ctx->mc_blocks_per_sm = blocks_per_sm;
+    for (auto &g : ctx->mc_exec)                  // captured with the old grid
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
     return 0;
 }
 

@@ -24,6 +24,9 @@
 #include "phygas_gb300.h"
 #include "../host/ph_host.h"
 
+// persistent clone-kernel blocks per SM of a slot when several slots share the GPU
+constexpr int kServeMcBlocksPerSm = 2;
+
 namespace {
 
 uint64_t fnv(uint64_t h, const void *p, size_t n) {
@@ -217,6 +220,9 @@ int pgx_server_open(int device, int slots, double hbm_budget_gb, const PhCluster
         s->ctx.push_back(ctx);
         rc = pgx_screen_clusters(ctx, nc, ps0.data(), sig.data(), tm.data(), r50.data(), rt.data(), names.data(),
                                  r_kernel);
+        // a pair job's persistent clone kernel would hold nearly every register of the GPU until it ends, and the
+        // other slots' screens would wait for it: with more than one slot it keeps to kServeMcBlocksPerSm blocks
+        if (rc == 0 && slots > 1) rc = pgx_pair_blocks(ctx, kServeMcBlocksPerSm);
         if (rc) {
             for (PgxContext *x : s->ctx) pgx_close(x);
             return rc;

@@ -150,6 +150,12 @@ int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const doub
                   const double *dt, const double *r50_pc, const double *rtot_pc, double *ms, int *best);
 /* number of launch shapes; the first n as (warps per block, clones per lane, minimum resident blocks per SM) */
 int pgx_pair_shapes(int n, int *warps, int *clones_per_lane, int *min_blocks);
+/* ph_pair over a list of (target, cluster) pairs -- pair q = (t[ti[q]], c[ci[q]]) with n_clones[q] clones, seeds
+ * ph_seed(id, name), dt_myr as pgx_draw_pair_batch -- with the host draws pipelined: the clones of batch b + 1
+ * (batch_pairs pairs; <= 0: 1,024) are drawn on `threads` host threads (<= 0: all cores) into page-locked memory
+ * while the GPU traces batch b.  res[q] as pgx_pair gives it; pgx_stats sums the batches. */
+int pgx_pair_targets(PgxContext *ctx, int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
+                     const int *n_clones, double dt_myr, int threads, int batch_pairs, PhResult *res);
 /* The persistent clone kernels of this context on at most blocks_per_sm blocks per SM (0 = as many as fit, the
  * default): leaves registers for other contexts' kernels to run beside them -- the request loop's slots. */
 int pgx_pair_blocks(PgxContext *ctx, int blocks_per_sm);

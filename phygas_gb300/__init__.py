@@ -104,6 +104,8 @@ SIGNATURES = [
     ("pgx_host_alloc", C.c_void_p, [C.c_size_t]),
     ("pgx_screen_split", C.c_int, [C.c_void_p, C.c_int]),
     ("pgx_pair_blocks", C.c_int, [C.c_void_p, C.c_int]),
+    ("pgx_pair_targets", C.c_int, [C.c_void_p, C.c_int, _P(PhTarget), _P(C.c_int), _P(PhCluster), _P(C.c_int),
+                                   _P(C.c_int), C.c_double, C.c_int, C.c_int, C.c_void_p]),
     ("pgx_screen_chunks", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                     C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     ("pgx_host_free", None, [C.c_void_p]),
@@ -362,6 +364,18 @@ class Context:
         if err:
             raise err[0]
         self._check(rc, "pgx_screen_chunks_text")
+
+    def pair_targets(self, targets, ti, clusters, ci, n_clones, dt_myr=0.05, threads=0, batch_pairs=0):
+        """pgx_pair_targets: ph_pair over the pairs (targets[ti[q]], clusters[ci[q]]) with n_clones[q] clones, the
+        host draws of each batch of pairs overlapping the GPU's tracing of the one before -> PhResult records."""
+        targets, clusters = as_array(targets, PhTarget), as_array(clusters, PhCluster)
+        ti, ci = np.ascontiguousarray(ti, np.int32), np.ascontiguousarray(ci, np.int32)
+        nc = np.ascontiguousarray(np.broadcast_to(n_clones, ti.shape), np.int32)
+        res = np.zeros(len(ti), RESULT_DTYPE)
+        self._check(lib().pgx_pair_targets(self.h, len(ti), targets, _ptr(ti, C.c_int), clusters, _ptr(ci, C.c_int),
+                                           _ptr(nc, C.c_int), dt_myr, threads, batch_pairs, res.ctypes.data),
+                    "pgx_pair_targets")
+        return res
 
     def pair_blocks(self, blocks_per_sm):
         """pgx_pair_blocks: the persistent clone kernels on at most blocks_per_sm blocks per SM (0 = all that fit)."""

@@ -85,6 +85,8 @@ struct PgxContext {
     Buf p_off, p_ps, p_steps, p_dt, p_r50, p_rt, p_items, p_q, p_done, p_cres, p_res, p_params;
     int mc_variant = 0;                        // launch shape of the clone kernel (pgx_tune_pair picks it)
     int mc_blocks_per_sm = 0;                  // > 0: the persistent clone kernels on at most this many blocks per SM
+    double *h_clones[2] = {};                  // pgx_pair_targets: two batches of clones, page-locked, reused
+    size_t h_clones_cap[2] = {};
     cudaGraphExec_t mc_exec[16] = {};          // prep + trace + reduce, captured once per shape, replayed
     // one-object helpers of the drop-in API
     Buf x_ps0, x_sig21, x_npts, x_opos, x_ovel, x_t64, x_t32, x_lm;
@@ -406,6 +408,8 @@ void pgx_close(PgxContext *ctx) {
         if (k.h_stage) cudaFreeHost(k.h_stage);
     }
     for (auto *h : ctx->h_buf)
+        if (h) cudaFreeHost(h);
+    for (auto *h : ctx->h_clones)
         if (h) cudaFreeHost(h);
     pgx::text_free(ctx->text_bufs);
     pgx::mixed_free(ctx->mixed);
@@ -1135,6 +1139,75 @@ int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *p
              const double *r50_pc, const double *rtot_pc, PhResult *res, double *clone_out) {
     if (!ctx) return PGX_E_ARG;
     return pair_run(ctx, ctx->mc_variant, n_pairs, clone_off, ps, steps, dt, r50_pc, rtot_pc, res, clone_out);
+}
+
+int pgx_pair_targets(PgxContext *ctx, int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
+                     const int *n_clones, double dt_myr, int threads, int batch_pairs, PhResult *res) {
+    if (!ctx) return PGX_E_ARG;
+    if (n_pairs < 0 || (n_pairs > 0 && (!t || !ti || !c || !ci || !n_clones || !res)) || !(dt_myr > 0))
+        return fail(ctx, PGX_E_ARG, "pgx_pair_targets: bad args");
+    if (n_pairs == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    const int bp = batch_pairs > 0 ? batch_pairs : 1024, nb = (n_pairs + bp - 1) / bp;
+    const int th = threads > 0 ? threads : pgh_default_threads();
+    // batch k's clones are drawn into buffer k % 2 (by a helper thread for k > 0) while the GPU traces batch k - 1
+    struct Batch {
+        std::vector<int> off, steps;
+        std::vector<double> dt, r50, rt;
+        int p0 = 0, n = 0, rc = 0;
+    } b[2];
+    auto draw = [&](int k, int i) {
+        Batch &x = b[i];
+        x.p0 = k * bp;
+        x.n = std::min(bp, n_pairs - x.p0);
+        long clones = 0;
+        for (int q = x.p0; q < x.p0 + x.n; q++) clones += std::max(n_clones[q], 0);
+        const size_t need = (size_t)12 * std::max(clones, 1L) * sizeof(double);
+        if (ctx->h_clones_cap[i] < need) {
+            pgx_host_free(ctx->h_clones[i]);
+            ctx->h_clones_cap[i] = 0;
+            ctx->h_clones[i] = (double *)pgx_host_alloc(need + need / 4);
+            if (!ctx->h_clones[i]) {
+                x.rc = -1;
+                return;
+            }
+            ctx->h_clones_cap[i] = need + need / 4;
+        }
+        x.off.resize(x.n + 1);
+        x.steps.resize(x.n);
+        x.dt.resize(x.n);
+        x.r50.resize(x.n);
+        x.rt.resize(x.n);
+        x.rc = pgh_draw_pair_batch(x.n, t, ti + x.p0, c, ci + x.p0, n_clones + x.p0, dt_myr, th, x.off.data(),
+                                   ctx->h_clones[i], x.steps.data(), x.dt.data(), x.r50.data(), x.rt.data());
+    };
+    draw(0, 0);
+    PgxStats sum = PgxStats();
+    int rc = 0;
+    for (int k = 0; k < nb && rc == 0; k++) {
+        const int i = k & 1;
+        std::thread ahead;
+        if (k + 1 < nb) ahead = std::thread(draw, k + 1, i ^ 1);
+        const Batch &x = b[i];
+        if (x.rc) {
+            rc = fail(ctx, x.rc == -1 ? PGX_E_NOMEM : PGX_E_LIMIT, "pgx_pair_targets: clone draws of pairs %d..%d",
+                      x.p0, x.p0 + x.n);
+        } else {
+            rc = pair_run(ctx, ctx->mc_variant, x.n, x.off.data(), ctx->h_clones[i], x.steps.data(), x.dt.data(),
+                          x.r50.data(), x.rt.data(), res + x.p0, nullptr);
+            const PgxStats &st = ctx->stats;
+            sum.ms_pair += st.ms_pair;
+            sum.clones += st.clones;
+            sum.clone_steps += st.clone_steps;
+            sum.body_steps += st.body_steps;
+            sum.pairs += st.pairs;
+            sum.kernels += st.kernels;
+        }
+        if (ahead.joinable()) ahead.join();
+    }
+    sum.ms_total = sum.ms_pair;
+    ctx->stats = sum;
+    return rc;
 }
 
 int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,

@@ -126,21 +126,19 @@ int run_pairs(PgxServer &s, PgxContext *ctx, Job &job) {
     const long np = pgh_prefilter_pairs(job.targets.data(), j.n_targets, s.clusters.data(), nc, s.host_threads,
                                         ti.data(), ci.data(), (long)ti.size());
     if (np < 0) return PGX_E_NOMEM;
-    std::vector<int> ncl(np, j.n_clones), off(np + 1), steps(np);
-    std::vector<double> ps((size_t)12 * np * std::max(j.n_clones, 1) + 1), dt(np), r50(np), rt(np);
+    std::vector<int> ncl(np, j.n_clones);
+    double work = 0;
     if (np > 0) {
-        const int d = pgh_draw_pair_batch((int)np, job.targets.data(), ti.data(), s.clusters.data(), ci.data(),
-                                          ncl.data(), j.dt_myr, s.host_threads, off.data(), ps.data(), steps.data(),
-                                          dt.data(), r50.data(), rt.data());
-        if (d) return d == -1 ? PGX_E_NOMEM : PGX_E_LIMIT;
+        // the clone draws of each batch of pairs overlap the GPU's tracing of the one before (page-locked buffers)
         job.res.resize(np);
-        const int rc = pgx_pair(ctx, (int)np, off.data(), ps.data(), steps.data(), dt.data(), r50.data(), rt.data(),
-                                job.res.data(), nullptr);
+        const int rc = pgx_pair_targets(ctx, (int)np, job.targets.data(), ti.data(), s.clusters.data(), ci.data(),
+                                        ncl.data(), j.dt_myr, s.host_threads, 0, job.res.data());
         if (rc) return rc;
+        PgxStats st;
+        pgx_stats(ctx, &st);
+        work = (double)st.clone_steps;
     }
     job.cluster.assign(ci.begin(), ci.begin() + np);
-    double work = 0;
-    for (long q = 0; q < np; q++) work += (double)(off[q + 1] - off[q]) * steps[q];
     job.out.n_out = np;
     job.out.work = work;
     uint64_t h = fnv(1469598103934665603ULL, job.cluster.data(), job.cluster.size() * sizeof(int));

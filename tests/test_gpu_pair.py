@@ -162,3 +162,26 @@ def test_every_launch_shape_gives_the_same_bits(ctx):
         got = clones[:, off[q]:off[q + 1]].T
         assert np.all(np.abs(got - ref) <= ot.REL_TOL * np.abs(ref) + 1e-12), q
     print("launch shapes:", table, "chosen", table[best][:3])
+
+
+def test_pipelined_pair_targets_and_capped_grid_give_the_same_bits(ctx):
+    """pgx_pair_targets (host draws of each batch of pairs overlapping the GPU's tracing of the one before, in batches
+    of 7 pairs here) gives the bits of pgx_draw_pair_batch + pgx_pair on the whole list, also with the persistent
+    clone kernel capped at one block per SM (pgx_pair_blocks, the request loop's setting)."""
+    rng = np.random.default_rng(5)
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "pair64", 3, 1001)
+        targets, clusters = pg.read_targets(tp), pg.read_clusters(cp)
+    ti = rng.integers(0, 3, 40).astype(np.int32)
+    ci = rng.integers(0, len(clusters), 40).astype(np.int32)
+    ncl = rng.choice([0, 1, 33, 200, 1000, 1500], 40).astype(np.int32)
+    want = ctx.pair(*pg.draw_pair_batch(targets, ti, clusters, ci, ncl, 0.05))
+    got = ctx.pair_targets(targets, ti, clusters, ci, ncl, 0.05, batch_pairs=7)
+    assert got.tobytes() == want.tobytes()
+    st = ctx.stats()
+    assert st["pairs"] == 40 and st["clones"] == int(ncl.sum())
+    ctx.pair_blocks(1)
+    try:
+        assert ctx.pair_targets(targets, ti, clusters, ci, ncl, 0.05).tobytes() == want.tobytes()
+    finally:
+        ctx.pair_blocks(0)

@@ -360,7 +360,8 @@ def config(args):
                         % (N_STARS, N_CLUSTERS, SEED, CHI2_MAX, N_SAMP, R_KERNEL),
             "stars": N_STARS, "clusters": N_CLUSTERS, "pairs_per_step": N_STARS * N_CLUSTERS,
             "l2": "flushed between steps (256 MiB write)", "cluster_table": "resident, built once outside timing",
-            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+            "parallelism": ("%d ranks, a star chunk each (no data exchange)" % args.gpus) if args.gpus > 1
+                           else "single GPU"}
 
 
 def main():

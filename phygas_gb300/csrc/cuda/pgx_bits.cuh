@@ -73,6 +73,34 @@ PGX_HD uint32_t f64_hi(double x) {
 #endif
 }
 
+PGX_HD uint32_t f64_lo(double x) {
+#ifdef __CUDA_ARCH__
+    return (uint32_t)__double2loint(x);
+#else
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    return (uint32_t)b;
+#endif
+}
+
+// x in FP32 with its significand truncated (toward zero), by integer operations: |f| <= |x| < |f| (1 + 2^-23) for
+// 2^-126 <= |x| < 2^128; +-0 below that range and +-FLT_MAX above it (NaN included)
+PGX_HD float f32_trunc(double x) {
+    const uint32_t hi = f64_hi(x), lo = f64_lo(x);
+    const uint32_t e = (hi >> 20) & 0x7ffu, sign = hi & 0x80000000u;
+    uint32_t b;
+    if (e < 897u) b = sign;
+    else if (e > 1150u) b = sign | 0x7f7fffffu;
+    else b = sign | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+#endif
+}
+
 PGX_HD bool seed_ok(uint32_t hi) { return hi - kSeedLo < kSeedSpan; }
 
 // the float with the argument's exponent and top 20 significand bits (seed_ok(hi) holds)

@@ -130,55 +130,91 @@ __global__ void __launch_bounds__(256) k_stm_cov(int N, int nmax, const int *__r
 // ---------------------------------------------------------------------------------------------------------------
 // clone Monte Carlo
 
+// |v| in FP32 (components already in FP32), bounded from below (lo) or above (hi): the approximate square root is
+// within a few ulp, and the 1e-6 margins cover it; outside 1e-18 <= |v| <= 1e18 the bounds are 0 and +inf
+__device__ __forceinline__ float norm32_rsqrt(float q) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(q));
+    return r;
+}
+__device__ __forceinline__ float norm32_lo(float x, float y, float z) {
+    const float q = fmaf(x, x, fmaf(y, y, z * z));
+    return q >= 1e-36f && q <= 1e36f ? q * norm32_rsqrt(q) * (1.f - 1e-6f) : 0.f;
+}
+__device__ __forceinline__ float norm32_hi(float x, float y, float z) {
+    const float q = fmaf(x, x, fmaf(y, y, z * z));
+    return q >= 1e-36f && q <= 1e36f ? q * norm32_rsqrt(q) * (1.f + 1e-6f) : __int_as_float(0x7f800000);
+}
+
 // One clone traced back: the target's and the cluster's orbit, the closest approach so far (reference
 // ph_pair_clone and seg_min, src/phygas.c:147-156, 200-216).  Results in kpc, Myr, kpc/Myr.
+//
+// Each step's segment r0 -> r1 first gets an FP32 lower bound on its distance from the origin: every point of it is
+// within |r1 - r0| / 2 of r0 or of r1, so none is nearer than min(|r0|, |r1|) - |r1 - r0| / 2.  The separations in
+// FP32 are truncated (never above |r|) and the FP32 norms carry 1e-6 margins; when the bound exceeds the closest
+// approach so far (an upper bound of it in FP32, with an absolute margin for the FP64 path's own rounding), the
+// segment cannot improve it and the FP64 segment test is skipped.  Otherwise the reference's test runs as before,
+// so the results are the same bits -- and the FP64 pipe does that work only near the closest approach.
 struct Clone {
     Orbit a, b;
-    double r0x, r0y, r0z, r0s, best, best2, tbest, vbest;
+    double r0x, r0y, r0z, best, tbest, vbest;
+    float f0x, f0y, f0z, n0, best_up;          // r0 truncated to FP32, |r0| from below, best from above
+    __device__ __forceinline__ void set_best_up() { best_up = fmaf(f32_trunc(best), 1.f + 2.4e-7f, 1e-37f); }
     __device__ __forceinline__ void start(const double *__restrict__ ps) {
         a.x = ps[0]; a.y = ps[1]; a.z = ps[2]; a.vx = ps[3]; a.vy = ps[4]; a.vz = ps[5];
         b.x = ps[6]; b.y = ps[7]; b.z = ps[8]; b.vx = ps[9]; b.vy = ps[10]; b.vz = ps[11];
         a.init();
         b.init();
         r0x = a.x - b.x; r0y = a.y - b.y; r0z = a.z - b.z;
-        r0s = fma(r0x, r0x, fma(r0y, r0y, r0z * r0z));
-        best = sqrt(r0s); best2 = r0s; tbest = 0.0;
+        best = sqrt(fma(r0x, r0x, fma(r0y, r0y, r0z * r0z)));
+        tbest = 0.0;
         const double ux = a.vx - b.vx, uy = a.vy - b.vy, uz = a.vz - b.vz;
         vbest = sqrt(fma(ux, ux, fma(uy, uy, uz * uz)));
+        f0x = f32_trunc(r0x); f0y = f32_trunc(r0y); f0z = f32_trunc(r0z);
+        n0 = norm32_lo(f0x, f0y, f0z);
+        set_best_up();
     }
     // step i (1-based) of length dt (negative), h = dt / 2
     __device__ __forceinline__ void step(int i, double dt, double h) {
         a.kdk(dt, h);
         b.kdk(dt, h);
         const double r1x = a.x - b.x, r1y = a.y - b.y, r1z = a.z - b.z;
-        const double dx = r1x - r0x, dy = r1y - r0y, dz = r1z - r0z;
-        const double dd = fma(dx, dx, fma(dy, dy, dz * dz));
-        const double an = fma(r0x, dx, fma(r0y, dy, r0z * dz));
-        const double r1s = fma(r1x, r1x, fma(r1y, r1y, r1z * r1z));
-        // squared distance of the segment r0 -> r1 from the origin, times dd (no division): the cheap pre-test
-        double near2dd;
-        if (!(dd > 0) || an >= 0) near2dd = r0s * dd;
-        else if (-an >= dd) near2dd = r1s * dd;
-        else near2dd = fma(r0s, dd, -an * an);
-        if (near2dd < best2 * dd * (1.0 + 1e-12) || (!(dd > 0) && r0s < best2 * (1.0 + 1e-12))) {
-            // the reference's segment minimum (seg_min) and its strict comparison
-            double s = 0.0;
-            if (dd > 0) {
-                s = -an / dd;
-                s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
-            }
-            const double mx = fma(dx, s, r0x), my = fma(dy, s, r0y), mz = fma(dz, s, r0z);
-            const double dm = sqrt(fma(mx, mx, fma(my, my, mz * mz)));
-            if (dm < best) {
-                best = dm;
-                best2 = dm * dm;
-                tbest = ((double)(i - 1) + s) * -dt;
-                const double wx = a.vx - b.vx, wy = a.vy - b.vy, wz = a.vz - b.vz;
-                vbest = sqrt(fma(wx, wx, fma(wy, wy, wz * wz)));
+        const float f1x = f32_trunc(r1x), f1y = f32_trunc(r1y), f1z = f32_trunc(r1z);
+        const float n1 = norm32_lo(f1x, f1y, f1z);
+        const float dn = fmaf(2.2e-7f, n0 + n1, norm32_hi(f1x - f0x, f1y - f0y, f1z - f0z));
+        const float lb = (fminf(n0, n1) - 0.5f * dn) * (1.f - 1e-6f) - 1e-12f * (n0 + n1);
+        if (!(lb > best_up)) {
+            // the reference's segment test (seg_min and its strict comparison), with its own cheap pre-test
+            const double dx = r1x - r0x, dy = r1y - r0y, dz = r1z - r0z;
+            const double dd = fma(dx, dx, fma(dy, dy, dz * dz));
+            const double an = fma(r0x, dx, fma(r0y, dy, r0z * dz));
+            const double r0s = fma(r0x, r0x, fma(r0y, r0y, r0z * r0z));
+            const double r1s = fma(r1x, r1x, fma(r1y, r1y, r1z * r1z));
+            const double best2 = best * best;
+            double near2dd;
+            if (!(dd > 0) || an >= 0) near2dd = r0s * dd;
+            else if (-an >= dd) near2dd = r1s * dd;
+            else near2dd = fma(r0s, dd, -an * an);
+            if (near2dd < best2 * dd * (1.0 + 1e-12) || (!(dd > 0) && r0s < best2 * (1.0 + 1e-12))) {
+                double s = 0.0;
+                if (dd > 0) {
+                    s = -an / dd;
+                    s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+                }
+                const double mx = fma(dx, s, r0x), my = fma(dy, s, r0y), mz = fma(dz, s, r0z);
+                const double dm = sqrt(fma(mx, mx, fma(my, my, mz * mz)));
+                if (dm < best) {
+                    best = dm;
+                    tbest = ((double)(i - 1) + s) * -dt;
+                    const double wx = a.vx - b.vx, wy = a.vy - b.vy, wz = a.vz - b.vz;
+                    vbest = sqrt(fma(wx, wx, fma(wy, wy, wz * wz)));
+                    set_best_up();
+                }
             }
         }
         r0x = r1x; r0y = r1y; r0z = r1z;
-        r0s = r1s;
+        f0x = f1x; f0y = f1y; f0z = f1z;
+        n0 = n1;
     }
 };
 

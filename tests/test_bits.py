@@ -196,3 +196,73 @@ def test_fixed_point_text_matches_printf():
         r = subprocess.run([exe], stdout=subprocess.PIPE, text=True)
     assert r.returncode == 0, r.stdout
     assert "bad 0" in r.stdout
+
+
+TRUNC = r"""
+#include <cmath>
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+#include <cfloat>
+#include "pgx_bits.cuh"
+static uint64_t sm = 777;
+static uint64_t next() {
+    uint64_t z = (sm += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+static long bad = 0, tested = 0;
+static void check(double x) {
+    const float f = pgx::f32_trunc(x);
+    const double a = std::fabs(x), g = std::fabs((double)f);
+    bool ok;
+    if (std::isnan(x)) ok = g == (double)FLT_MAX;
+    else if (a < 0x1p-126) ok = f == 0.f && std::signbit(f) == std::signbit(x);
+    else if (a >= 0x1p128) ok = g == (double)FLT_MAX && std::signbit(f) == std::signbit(x);
+    else ok = g <= a && a < g * (1.0 + 0x1p-23) && std::signbit(f) == std::signbit(x) && std::isnormal(f);
+    if (std::isfinite(x) && a >= 0x1p-126 && a < 0x1p128) {     // the truncation itself: the nearest float toward zero
+        const float n = (float)x;
+        const float t = std::fabs((double)n) > a ? std::nextafter(n, 0.f) : n;
+        ok = ok && t == f;
+    }
+    tested++;
+    if (!ok && bad++ < 5) std::printf("x=%a got %a\n", x, (double)f);
+}
+int main() {
+    const double sp[] = {0.0, -0.0, 0x1p-1074, 0x1p-127, 0x1.fffffffffffffp-127, 0x1p-126, 0x1.ffffffp-126,
+                         1.0, -1.0, 0x1.fffffep127, 0x1.ffffffp127, 0x1.fffffffffffffp127, 0x1p128, -0x1p128,
+                         INFINITY, -INFINITY, NAN, -NAN, DBL_MAX};
+    for (double x : sp) check(x);
+    for (int e = -130; e <= 130; e++)
+        for (int d = -3; d <= 3; d++) {
+            const double p = std::ldexp(1.0, e);
+            double x = p;
+            for (int k = 0; k < (d < 0 ? -d : d); k++) x = std::nextafter(x, d < 0 ? 0.0 : INFINITY);
+            check(x);
+            check(-x);
+        }
+    for (long i = 0; i < 4000000; i++) {
+        const uint64_t r = next();
+        double x;
+        std::memcpy(&x, &r, 8);
+        check(x);                                       // any bit pattern
+        check(std::ldexp((double)(r >> 11), -53 + (int)(r % 40) - 20) * ((r >> 7) & 1 ? -1 : 1));   // kpc-sized
+    }
+    std::printf("tested %ld bad %ld\n", tested, bad);
+    return bad != 0;
+}
+"""
+
+
+def test_f32_truncation_bounds():
+    """The clone kernel's FP32 pre-test (pgx_orbit.cu) rests on f32_trunc (pgx_bits.cuh): the float nearest x toward
+    zero, so |f| <= |x| < |f| (1 + 2^-23) in the normal range, +-0 below it and +-FLT_MAX above it and for NaN."""
+    inc = os.path.join(ot.REPO, "phygas_gb300", "csrc", "cuda")
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = os.path.join(d, "trunc.cpp"), os.path.join(d, "trunc")
+        open(src, "w").write(TRUNC)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", inc, src, "-o", exe], check=True)
+        r = subprocess.run([exe], stdout=subprocess.PIPE, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "bad 0" in r.stdout

@@ -40,9 +40,11 @@ CHI2_MAX, N_SAMP, R_KERNEL = 25.0, 64, 2.0
 FLOPS_PER_BODY_STEP = 104.0
 # the same count as FP64 instructions (each takes one FP64-pipe slot, whatever its flops)
 FP64_INSTR_PER_BODY_STEP = 36.0 + 3.0 + 29.0
-# the same for one clone-step of the pair Monte Carlo (two body steps and the segment test), from k_pair_mc_t on the
-# batch of `python -m phygas_gb300.run_pairs` (4,052 pairs, 1.49e9 clone-steps): 79.0 DFMA + 12.2 DADD + 65.5 DMUL
-FLOPS_PER_CLONE_STEP = 235.7
+# the same for one clone-step of the pair Monte Carlo (two body steps, and the FP64 segment test where the FP32 bound
+# does not rule it out), from k_pair_mc_t on the batch of `python -m phygas_gb300.run_pairs` (4,052 pairs, 1.49e9
+# clone-steps): 73.3 DFMA + 9.3 DADD + 58.9 DMUL executed
+FLOPS_PER_CLONE_STEP = 214.9
+FP64_INSTR_PER_CLONE_STEP = 73.3 + 9.3 + 58.9
 # DRAM traffic of one k_stm_orbits launch on this chunk (dram__bytes_read.sum + dram__bytes_write.sum from one ncu
 # capture of `python -m phygas_gb300.run_screen --stars 20000`): 4.9 MB read + 711.8 MB of orbit output written
 ORBIT_TRAFFIC_BYTES = 716.7e6
@@ -232,7 +234,9 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
                         "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
                         "frac": FLOPS_PER_CLONE_STEP * cs / (statistics.mean(ms) * 1e-3) / fp64_peak,
                         "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
-                        "flops_per_clone_step": FLOPS_PER_CLONE_STEP},
+                        "flops_per_clone_step": FLOPS_PER_CLONE_STEP,
+                        "fp64_instr_frac": FP64_INSTR_PER_CLONE_STEP * cs / (statistics.mean(ms) * 1e-3)
+                                           / (fp64_peak / 2)},
            "autotune": {"chosen": {"warps_per_block": table[best][0], "clones_per_lane": table[best][1],
                                    "min_blocks_per_sm": table[best][2]},
                         "ms_on_sample": [{"warps_per_block": w, "clones_per_lane": c, "min_blocks_per_sm": b, "ms": t}

@@ -75,7 +75,7 @@ __device__ __forceinline__ double rcp_h3(double d) {
 //   aR * x / R     = -GM x / D^3                 (disk, the R of the radial force cancels)
 //   az(disk)       = -GM z (a + s) / (s D^3), s = sqrt(z^2 + b^2): (a + s) / s = 1 + a / s
 //   x^g / (1 + x^(g-1)) = x p / (1 + p), p = x^(g-1) = x * x^(g-2)   (halo)
-// Mathematically identical; the last bits differ from glibc's as any libm's do.  62 FP64 operations.
+// Mathematically identical; the last bits differ from glibc's as any libm's do.  59 FP64 operations.
 __device__ __forceinline__ void mw_accel(double x, double y, double z, double &ax, double &ay, double &az) {
     const double R2 = fma(x, x, y * y);
     const double r2 = fma(z, z, R2);
@@ -85,15 +85,17 @@ __device__ __forceinline__ void mw_accel(double x, double y, double z, double &a
     const double s = fma(zb2, iz, kDiskA);                      // a + sqrt(z^2 + b^2)
     const double iD = rsqrt_h3(fma(s, s, R2));
     const double fd = -kDiskGM * (iD * iD * iD);
+    // r2 > kTinyR2 and min(r, cut) as integer compares of the bit patterns (for doubles >= 0 they order as the values
+    // do; a compare or min of doubles would take an FP64-pipe slot): the same selections for every r2 >= 0
     double r, ir;
-    if (r2 > 1e-24) {
+    if (__double_as_longlong(r2) > kTinyR2Bits) {
         ir = rsqrt_h3(r2);
         r = r2 * ir;
     } else {
         r = 1e-12;
         ir = 1e12;
     }
-    const double xh = fmin(r, kHaloCut) * kHaloInvA;
+    const double xh = (__double_as_longlong(r) < kHaloCutBits ? r : kHaloCut) * kHaloInvA;
     const double p = xh * halo_pow_a(xh);              // xh^(gamma - 1)
     const double q = p * rcp_h3(1.0 + p);
     const double fh = -kHaloGM * xh * q * ((ir * ir) * ir);

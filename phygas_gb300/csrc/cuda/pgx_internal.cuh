@@ -16,6 +16,9 @@ constexpr double kDiskB2 = 0.25 * 0.25;
 constexpr double kHaloGM = kG * (4615.0 * 2.325e7);
 constexpr double kHaloInvA = 1.0 / 12.0;
 constexpr double kHaloCut = 100.0;
+constexpr long long kHaloCutBits = 0x4059000000000000LL;       // the bit pattern of kHaloCut (checked in orbit_setup)
+constexpr double kTinyR2 = 1e-24;                               // below it the force's r is taken as 1e-12
+constexpr long long kTinyR2Bits = 0x3af357c299a88ea7LL;        // the bit pattern of kTinyR2 (checked in orbit_setup)
 constexpr double kHaloG1 = 2.02 - 1.0;                          // gamma - 1, as the reference forms it
 constexpr double kStepMyr = 0.5;                                // PH_PRE_STEP_MYR
 constexpr int kSub = 10;                                        // PH_LIN_SUB

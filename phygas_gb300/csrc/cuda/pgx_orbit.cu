@@ -766,6 +766,10 @@ int orbit_setup(int dev) {
     if (dev < 0 || dev >= 64) return 1;
     std::lock_guard<std::mutex> lk(mu);
     if (ready[dev]) return 0;
+    long long b1, b2;                       // the force compares these bit patterns as integers
+    std::memcpy(&b1, &kHaloCut, 8);
+    std::memcpy(&b2, &kTinyR2, 8);
+    if (b1 != kHaloCutBits || b2 != kTinyR2Bits) return 3;
     k_halo_tables<<<1, kHaloTableThreads>>>();
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();

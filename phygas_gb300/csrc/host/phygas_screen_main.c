@@ -7,7 +7,7 @@
  * Progress on stderr.  The draws run on all host cores; the orbits, the scan, the 512-draw probabilities and the
  * formatting of the lines on the GPU (libphygas_gb300).  PHYGAS_PRECISION=fp64 selects the plain FP64 screen
  * instead of the default mixed-precision one (their rows are identical); PHYGAS_CHUNK sets the stars per GPU chunk
- * (default 20000).
+ * (default 2500: small chunks let the draws, the orbits, the screen and the lines of neighbouring chunks overlap).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -83,7 +83,7 @@ int main(int argc, char **argv) {
         tg = v;
         fprintf(stderr, "control run: velocities taken from the star %d lines away\n", nt / 2);
     }
-    const int chunk = env_int("PHYGAS_CHUNK", 20000);
+    const int chunk = env_int("PHYGAS_CHUNK", 2500);
     Printer P = {0, now_s()};
     /* the draws of the next chunk run while the GPU screens this one and the previous chunk's lines are written */
     if (pgx_screen_chunks_text(ctx, tg, nt, cl, nc, chunk, n_samp, 0, tmax, chi2_max, precision, print_text, &P)) {

@@ -194,9 +194,19 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
     with open(pp, "w") as f:
         f.write("\n".join(synth.pulsars(C3_PULSARS, C3_SEED)) + "\n")
     pulsars = pg.read_targets(pp)
+    # the prefilter on the GPU (first call: the cluster tracks too; second: the targets only, the cluster side kept),
+    # and the host code it replaces, which must keep the same pairs
+    pref_s = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        pti, pci = ctx.prefilter(pulsars, clusters)
+        pref_s.append(time.perf_counter() - t0)
+    pref_st = ctx.stats()
     t0 = time.perf_counter()
-    pti, pci = pg.prefilter_pairs(pulsars, clusters)
-    t_pref = time.perf_counter() - t0
+    hti, hci = pg.prefilter_pairs(pulsars, clusters)
+    t_pref_host = time.perf_counter() - t0
+    if not (np.array_equal(hti, pti) and np.array_equal(hci, pci)):
+        raise RuntimeError("pgx_prefilter kept other pairs than the host code")
     targets = list(stars) + list(pulsars)
     ti = np.concatenate([rows["star"][take], pti + len(stars)]).astype(np.int32)
     ci = np.concatenate([rows["cluster"][take], pci]).astype(np.int32)
@@ -244,7 +254,11 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
            "e2e": {"value": cs / min(e2e_walls), "unit": "clone-steps/s", "s_per_step": min(e2e_walls),
                    "how": "pgx_pair_targets: host clone draws of each batch of 1,024 pairs overlap the GPU's tracing "
                           "of the one before (page-locked buffers)",
-                   "host_draw_s_unpipelined": t_draw, "prefilter_s": t_pref,
+                   "host_draw_s_unpipelined": t_draw,
+                   "prefilter_s": {"gpu_first_call": pref_s[0], "gpu_clusters_kept": pref_s[1],
+                                   "gpu_device_ms": pref_st["ms_prefilter"],
+                                   "host_decided_pairs": pref_st["prefilter_rechecked"],
+                                   "host_code": t_pref_host},
                    "h2d_bytes_per_step": int(12 * 8 * st["clones"] + 28 * len(ti)),
                    "d2h_bytes_per_step": int(96 * len(ti))},
            "cpu_baseline": None}

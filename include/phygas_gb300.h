@@ -128,6 +128,21 @@ int pgx_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, i
 int pgx_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c, const int *ci,
                         const int *n_clones, double dt_myr, int threads, int *clone_off, double *ps, int *steps,
                         double *dt, double *r50_pc, double *rtot_pc);
+/* The prefilter on the GPU (reference ph_track_target / ph_track_cluster / ph_prefilter over every pair,
+ * src/phygas.c:98-168, as src/phygas_cli.c:31-46 runs them): the same pairs in the same order as pgx_prefilter_pairs
+ * (at most cap written to ti/ci, *n = how many pass).  The host draws the tracks' starts and spreads on `threads`
+ * threads (0 = all cores); the GPU traces the coarse tracks and tests the pairs; the cluster tracks stay in the
+ * context for the next call with the same clusters.  A pair the GPU cannot decide with the margin to spare is decided
+ * by the host code.  pgx_stats: ms_prefilter (device time), prefilter_pairs, prefilter_rechecked, body_steps. */
+int pgx_prefilter(PgxContext *ctx, const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti,
+                  int *ci, long cap, long *n);
+/* The distance (kpc, >= 0) the GPU's prefilter decisions keep from the threshold, a bound on how far a GPU-traced
+ * track point may lie from the host-traced one (default 1e-7). */
+int pgx_prefilter_margin(PgxContext *ctx, double margin_kpc);
+/* Coarse tracks of n objects (reference track, src/phygas.c:98-111): from nominal starts ps (6 doubles each; kpc,
+ * kpc/Myr), npts[i] points 0.5 Myr apart (10 KDK steps of -0.05 Myr): pos = 3 npts[i] doubles per object, back to
+ * back. */
+int pgx_tracks(PgxContext *ctx, int n, const double *ps, const int *npts, double *pos);
 
 /* ---- pair Monte Carlo ------------------------------------------------------------------------------------------ */
 /* Trace every clone of n_pairs pairs back and reduce each pair (reference ph_pair_clone + ph_pair_reduce,
@@ -183,6 +198,8 @@ typedef struct {
     int kernels;                     /* kernel launches of the call */
     long orbit_body_steps;           /* body steps of the orbit launch that ms_orbit times (a chunk screened in two
                                         halves times the first half's; the second's runs beside the first's screen) */
+    double ms_prefilter;             /* pgx_prefilter: device time of the tracks and the pair tests */
+    long prefilter_pairs, prefilter_rechecked;   /* pairs tested; pairs within the margin, decided on the host */
 } PgxStats;
 int pgx_stats(const PgxContext *ctx, PgxStats *out);
 

@@ -51,7 +51,10 @@ class PgxStats(C.Structure):
                                           "ms_pair")] + [
         (k, C.c_long) for k in ("pairs", "kept", "candidates", "rechecked_points", "rechecked_draws", "clones",
                                 "clone_steps", "body_steps", "ambiguous")] + [("kernels", C.c_int),
-                                                                               ("orbit_body_steps", C.c_long)]
+                                                                               ("orbit_body_steps", C.c_long),
+                                                                               ("ms_prefilter", C.c_double),
+                                                                               ("prefilter_pairs", C.c_long),
+                                                                               ("prefilter_rechecked", C.c_long)]
 
 
 ROW_DTYPE = np.dtype([("star", "i4"), ("cluster", "i4"), ("kb", "i4"), ("pad", "i4"), ("sb", "f8"), ("chi2", "f8"),
@@ -116,6 +119,10 @@ SIGNATURES = [
     ("pgx_seed_prefix", C.c_uint64, [C.c_char_p]),
     ("pgx_prefilter_pairs", C.c_int, [_P(PhTarget), C.c_int, _P(PhCluster), C.c_int, C.c_int, _I, _I, C.c_long,
                                       _P(C.c_long)]),
+    ("pgx_prefilter", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, _P(PhCluster), C.c_int, C.c_int, _I, _I,
+                                C.c_long, _P(C.c_long)]),
+    ("pgx_prefilter_margin", C.c_int, [C.c_void_p, C.c_double]),
+    ("pgx_tracks", C.c_int, [C.c_void_p, C.c_int, _D, _I, _D]),
     ("pgx_draw_pair_batch", C.c_int, [C.c_int, _P(PhTarget), _I, _P(PhCluster), _I, _I, C.c_double, C.c_int, _I, _D,
                                       _I, _D, _D, _D]),
     ("pgx_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, C.c_void_p, _D]),
@@ -376,6 +383,29 @@ class Context:
                                            _ptr(nc, C.c_int), dt_myr, threads, batch_pairs, res.ctypes.data),
                     "pgx_pair_targets")
         return res
+
+    def prefilter(self, targets, clusters, threads=0):
+        """pgx_prefilter: (target index, cluster index) arrays of the pairs that pass ph_prefilter, tested on the GPU
+        (the same pairs as prefilter_pairs)."""
+        targets, clusters = as_array(targets, PhTarget), as_array(clusters, PhCluster)
+        n = C.c_long()
+        cap = len(targets) * len(clusters)
+        ti, ci = np.zeros(max(cap, 1), np.int32), np.zeros(max(cap, 1), np.int32)
+        self._check(lib().pgx_prefilter(self.h, targets, len(targets), clusters, len(clusters), int(threads),
+                                        _ptr(ti, C.c_int), _ptr(ci, C.c_int), cap, C.byref(n)), "pgx_prefilter")
+        return ti[:n.value], ci[:n.value]
+
+    def prefilter_margin(self, margin_kpc):
+        """pgx_prefilter_margin: the distance (kpc) the GPU's prefilter decisions keep from the threshold."""
+        self._check(lib().pgx_prefilter_margin(self.h, float(margin_kpc)), "pgx_prefilter_margin")
+
+    def tracks(self, ps, npts):
+        """pgx_tracks: coarse tracks from nominal starts ps[n, 6]; returns the positions [sum(npts), 3]."""
+        ps = np.ascontiguousarray(ps, np.float64).reshape(-1, 6)
+        npts = np.ascontiguousarray(npts, np.int32)
+        pos = np.zeros((int(npts.sum()), 3))
+        self._check(lib().pgx_tracks(self.h, len(npts), _ptr(ps), _ptr(npts, C.c_int), _ptr(pos)), "pgx_tracks")
+        return pos
 
     def pair_blocks(self, blocks_per_sm):
         """pgx_pair_blocks: the persistent clone kernels on at most blocks_per_sm blocks per SM (0 = all that fit)."""

@@ -6,6 +6,7 @@
 //   -> k_finish_prep -> k_finish64            (the FP64 path; the mixed path replaces scan..finish, pgx_mixed.cu)
 // Pair Monte Carlo: one persistent k_pair_mc launch over a longest-first queue (+ k_pair_reduce_big).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -21,6 +22,7 @@
 #include "phygas_gb300.h"
 #include "pgx_kernels.h"
 #include "pgx_mixed.h"
+#include "pgx_prefilter.h"
 #include "pgx_text.h"
 #include "../host/ph_host.h"
 
@@ -79,6 +81,7 @@ struct PgxContext {
     size_t h_cap[2] = {};
     Buf lab_names, lab_kinds, lab_age16, lab_age84;
     pgx::TextBufs text_bufs;
+    pgx::PrefilterState pre;         // the prefilter's device tracks (the cluster side kept between calls)
     pgx::MixedBufs mixed;
     long n_rows = 0;
     // pair Monte Carlo
@@ -412,6 +415,7 @@ void pgx_close(PgxContext *ctx) {
     for (auto *h : ctx->h_clones)
         if (h) cudaFreeHost(h);
     pgx::text_free(ctx->text_bufs);
+    pgx::prefilter_free(ctx->pre);
     pgx::mixed_free(ctx->mixed);
     for (auto &g : ctx->mc_exec)
         if (g) cudaGraphExecDestroy(g);
@@ -467,6 +471,47 @@ int pgx_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhC
                                       threads > 0 ? threads : pgh_default_threads(), clone_off, ps, steps, dt,
                                       r50_pc, rtot_pc);
     return r == 0 ? 0 : (r == -1 ? PGX_E_NOMEM : PGX_E_LIMIT);
+}
+
+int pgx_prefilter(PgxContext *ctx, const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti,
+                  int *ci, long cap, long *n) {
+    if (!ctx) return PGX_E_ARG;
+    if (nt < 0 || nc < 0 || cap < 0 || !n || (nt > 0 && !t) || (nc > 0 && !c) || (cap > 0 && (!ti || !ci)))
+        return fail(ctx, PGX_E_ARG, "pgx_prefilter: bad args");
+    CK(cudaSetDevice(ctx->device));
+    pgx::PrefilterCounts cnt;
+    std::string err;
+    ctx->stats = PgxStats();
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = pgx::prefilter_pairs(ctx->st, ctx->pre, t, nt, c, nc, threads > 0 ? threads : pgh_default_threads(),
+                                        ti, ci, cap, n, cnt, err);
+    if (rc) return fail(ctx, rc, "pgx_prefilter: %s", err.c_str());
+    ctx->stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    ctx->stats.ms_prefilter = cnt.ms_device;
+    ctx->stats.prefilter_pairs = cnt.pairs;
+    ctx->stats.prefilter_rechecked = cnt.rechecked;
+    ctx->stats.body_steps = cnt.body_steps;
+    ctx->stats.kernels = cnt.kernels;
+    return 0;
+}
+
+int pgx_prefilter_margin(PgxContext *ctx, double margin_kpc) {
+    if (!ctx) return PGX_E_ARG;
+    if (!(margin_kpc >= 0.0 && margin_kpc <= 1e6)) return fail(ctx, PGX_E_ARG, "pgx_prefilter_margin: %g", margin_kpc);
+    ctx->pre.margin = margin_kpc;
+    return 0;
+}
+
+int pgx_tracks(PgxContext *ctx, int n, const double *ps, const int *npts, double *pos) {
+    if (!ctx) return PGX_E_ARG;
+    if (n < 0 || (n > 0 && (!ps || !npts || !pos))) return fail(ctx, PGX_E_ARG, "pgx_tracks: bad args");
+    for (int i = 0; i < n; i++)
+        if (npts[i] < 1 || npts[i] > 200001) return fail(ctx, PGX_E_ARG, "pgx_tracks: npts[%d] = %d", i, npts[i]);
+    CK(cudaSetDevice(ctx->device));
+    std::string err;
+    const int rc = pgx::coarse_tracks(ctx->st, ctx->pre, n, ps, npts, pos, err);
+    if (rc) return fail(ctx, rc, "pgx_tracks: %s", err.c_str());
+    return 0;
 }
 
 int pgx_stats(const PgxContext *ctx, PgxStats *out) {

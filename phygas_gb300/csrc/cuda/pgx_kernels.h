@@ -70,6 +70,8 @@ int orbit_setup(int dev);
 __global__ void k_stm_orbits(int N, const double *ps0, const int *npts, int nmax, double *opos, double *ovel);
 __global__ void k_stm_cov(int N, int nmax, const int *npts, const double *opos, const double *ovel,
                           const double *sig21, double *t64, float4 *t32, float *lm);
+// the prefilter's coarse tracks: nominal orbits from ps (6 doubles per object), pos[k][3][N] for k < npts[i]
+cudaError_t launch_coarse_tracks(cudaStream_t st, int N, const double *ps, const int *npts, double *pos);
 __global__ void k_pair_mc(McPairs P);
 // launch-shape variants of the persistent clone kernel (parameters in device memory): count, shape (warps per block,
 // clones per lane), full persistent grid, and the prep + trace + reduce kernels as one sequence on a stream (pairs of

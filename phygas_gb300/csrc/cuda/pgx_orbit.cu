@@ -65,6 +65,38 @@ __global__ void __launch_bounds__(128) k_stm_orbits(int N, const double *__restr
     }
 }
 
+// Coarse tracks of the prefilter (reference track, src/phygas.c:98-111): the nominal orbit of each object from ps
+// (6 doubles per object), one thread per object; pos[k][3][N] = the position after 10 k KDK steps of -0.05 Myr, for
+// k < npts[i].  The same orbit, steps and force as k_stm_orbits' nominal orbit.
+__global__ void __launch_bounds__(32) k_coarse_tracks(int N, const double *__restrict__ ps,
+                                                      const int *__restrict__ npts, double *__restrict__ pos) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const size_t NN = N;
+    const double *q = ps + 6 * (size_t)i;
+    Orbit o;
+    o.x = q[0]; o.y = q[1]; o.z = q[2]; o.vx = q[3]; o.vy = q[4]; o.vz = q[5];
+    o.init();
+    const int n = npts[i];
+    constexpr double dt = -kStepMyr / kSub, h = 0.5 * dt;
+    for (int k = 0; k < n; k++) {
+        if (k > 0) {
+#pragma unroll 1
+            for (int s = 0; s < kSub; s++) o.kdk(dt, h);
+        }
+        double *p = pos + (size_t)k * 3 * NN + i;
+        p[0] = o.x; p[NN] = o.y; p[2 * NN] = o.z;
+    }
+}
+
+cudaError_t launch_coarse_tracks(cudaStream_t st, int N, const double *ps, const int *npts, double *pos) {
+    if (N <= 0) return cudaSuccess;
+    // a warp per block: the few hundred to few thousand orbits spread over every SM, each warp with an SM's FP64
+    // pipe to itself
+    k_coarse_tracks<<<(N + 31) / 32, 32, 0, st>>>(N, ps, npts, pos);
+    return cudaGetLastError();
+}
+
 // sig21: the 21 distinct entries of the symmetric 6x6 Sigma0, [21][N], upper triangle row by row
 __global__ void __launch_bounds__(256) k_stm_cov(int N, int nmax, const int *__restrict__ npts,
                                                  const double *__restrict__ opos, const double *__restrict__ ovel,

@@ -1,0 +1,308 @@
+// pgx_prefilter.cu -- the pair prefilter on the GPU (reference ph_track_target / ph_track_cluster / ph_prefilter,
+// src/phygas.c:98-168, as the pair CLI uses them, src/phygas_cli.c:31-46).
+//
+// The host draws each object's nominal start and its 32-draw spread (the host code the reference's tracks use, so
+// those values are the reference's bits); the GPU traces the coarse tracks (k_coarse_tracks: 10 KDK steps of
+// -0.05 Myr per 0.5 Myr point) and tests every (target, cluster) pair's segments (k_prefilter).  The cluster side is
+// kept on the device while the same clusters come back, so a stream of pulsar jobs traces the 4,087 cluster tracks
+// once.
+//
+// The GPU's tracks differ from the host's in the last bits (the force's own reciprocal square roots and power), so
+// a pair whose distance comes within a margin of the threshold is not decided on the GPU: every segment k gives
+//   d_k    the segment's distance from the origin (1-Lipschitz in the endpoints: a host value is within 2m of it,
+//          m = the margin on each object's position),
+//   thr_k  r0 + 3 (sp + sv (k + s) 0.5) over the range of s the host's endpoints allow (first-order bound on s,
+//          four times over, clamped to [0, 1]),
+// and the pair is kept when some segment has d_k + 2m < thr_k at its lowest, dropped when every segment has
+// d_k - 2m > thr_k at its highest, and otherwise traced and tested on the host with the reference's code.  So the
+// kept pairs are the host's pgh_prefilter_pairs' for any tracks within the margin; tests/test_gpu_prefilter.py
+// checks both that and the margin.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "pgx_kernels.h"
+#include "pgx_prefilter.h"
+#include "../host/ph_host.h"
+
+namespace pgx {
+namespace {
+
+template <class T> T *Pb(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
+
+constexpr int kPrefThreads = 128;
+
+// keep[j][i]: 0 dropped, 1 kept, 2 within the margin (decided on the host).  One thread per (target j, cluster i);
+// cluster tracks pos[k][3][nc] (a warp reads consecutive clusters), target tracks pos[k][3][nt] (one target per
+// block row: broadcast).
+__global__ void __launch_bounds__(kPrefThreads) k_prefilter(int nt, int nc, int j0, int t_n,
+                                                            const double *__restrict__ tpos,
+                                                            const double *__restrict__ tsig,
+                                                            const int *__restrict__ cn,
+                                                            const double *__restrict__ cpos,
+                                                            const double *__restrict__ csig,
+                                                            const double *__restrict__ cr0, double margin,
+                                                            unsigned char *__restrict__ keep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = j0 + blockIdx.y;
+    if (i >= nc || j >= nt) return;
+    const size_t NT = nt, NC = nc;
+    const int n = min(t_n, cn[i]);
+    const double sp = hypot(tsig[2 * j], csig[2 * i]), sv = hypot(tsig[2 * j + 1], csig[2 * i + 1]);
+    const double r0c = cr0[i];
+    const double *ta = tpos + j, *ca = cpos + i;
+    double x0 = ta[0] - ca[0], y0 = ta[NT] - ca[NC], z0 = ta[2 * NT] - ca[2 * NC];
+    double a0 = sqrt(x0 * x0 + y0 * y0 + z0 * z0);
+    int res = 0;
+    for (int k = 0; k + 1 < n; k++) {
+        const double *tb = tpos + (size_t)(k + 1) * 3 * NT + j, *cb = cpos + (size_t)(k + 1) * 3 * NC + i;
+        const double x1 = tb[0] - cb[0], y1 = tb[NT] - cb[NC], z1 = tb[2 * NT] - cb[2 * NC];
+        const double a1 = sqrt(x1 * x1 + y1 * y1 + z1 * z1);
+        // the reference's nearest point of the segment (nearest_on_segment / seg_min)
+        const double dx = x1 - x0, dy = y1 - y0, dz = z1 - z0;
+        const double dd = dx * dx + dy * dy + dz * dz;
+        double s = 0.0;
+        if (dd > 0) {
+            s = -(x0 * dx + y0 * dy + z0 * dz) / dd;
+            s = s < 0.0 ? 0.0 : (s > 1.0 ? 1.0 : s);
+        }
+        const double mx = x0 + dx * s, my = y0 + dy * s, mz = z0 + dz * s;
+        const double d = sqrt(mx * mx + my * my + mz * mz);
+        // the margins: positions (2m on a separation) plus rounding; the range of s the host can find
+        const double M = 2.0 * margin + 1e-12 * (a0 + a1);
+        const double ds = dd > 0 ? fmin(1.0, 4.0 * M * (sqrt(dd) + 6.0 * a0) / dd) : 1.0;
+        const double slo = fmax(0.0, s - ds), shi = fmin(1.0, s + ds);
+        const double thr_lo = r0c + 3.0 * (sp + sv * (((double)k + slo) * PH_PRE_STEP_MYR));
+        const double thr_hi = r0c + 3.0 * (sp + sv * (((double)k + shi) * PH_PRE_STEP_MYR));
+        const double T = 1e-12 * fabs(thr_hi);
+        if (d + M < thr_lo - T) {
+            res = 1;
+            break;
+        }
+        if (!(d - M > thr_hi + T)) res = 2;
+        x0 = x1; y0 = y1; z0 = z1; a0 = a1;
+    }
+    keep[(size_t)j * NC + i] = (unsigned char)res;
+}
+
+uint64_t fnv_bytes(uint64_t h, const void *p, size_t n) {
+    const unsigned char *b = static_cast<const unsigned char *>(p);
+    for (size_t k = 0; k < n; k++) h = (h ^ b[k]) * 1099511628211ULL;
+    return h;
+}
+
+int points_of(double tmax_myr, int *n, std::string &err) {
+    // the reference's ceil(tmax / 0.5) + 1, for tmax in [0, 1e5] Myr
+    if (!(tmax_myr >= 0.0 && tmax_myr <= 1e5)) {
+        err = "prefilter: tmax_myr out of [0, 1e5]";
+        return PGX_E_ARG;
+    }
+    *n = (int)ceil(tmax_myr / PH_PRE_STEP_MYR) + 1;
+    return 0;
+}
+
+int ck(cudaError_t e, std::string &err, const char *what) {
+    if (e == cudaSuccess) return 0;
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? PGX_E_NOMEM : PGX_E_CUDA;
+}
+
+struct TrackJob {
+    const PhTarget *t;
+    const PhCluster *c;
+    const int *idx;
+    PhTrack *out;
+    double tmax;
+};
+
+void host_tracks_range(void *p, int a, int b) {
+    TrackJob *J = static_cast<TrackJob *>(p);
+    for (int q = a; q < b; q++) {
+        const int i = J->idx[q];
+        if (J->t) ph_track_target(&J->t[i], J->tmax, 32, ph_seed("track", J->t[i].id), &J->out[q]);
+        else ph_track_cluster(&J->c[i], 32, ph_seed("track", J->c[i].name), &J->out[q]);
+    }
+}
+
+void free_host_tracks(PrefilterState &P) {
+    for (PhTrack &t : P.host_ctr) ph_track_free(&t);
+    P.host_ctr.clear();
+}
+
+}  // namespace
+
+void prefilter_free(PrefilterState &P) {
+    DevBuf *all[] = {&P.c_ps, &P.c_sig, &P.c_n, &P.c_r0, &P.c_pos, &P.t_ps, &P.t_sig, &P.t_n, &P.t_pos, &P.keep};
+    for (DevBuf *b : all)
+        if (b->p) { cudaFree(b->p); b->p = nullptr; b->cap = 0; }
+    free_host_tracks(P);
+    P.digest = 0;
+    P.nc = 0;
+}
+
+int coarse_tracks(cudaStream_t st, PrefilterState &P, int n, const double *ps, const int *npts, double *pos,
+                  std::string &err) {
+    if (n <= 0) return 0;
+    int nmax = 0;
+    for (int i = 0; i < n; i++) nmax = std::max(nmax, npts[i]);
+    int rc;
+    if ((rc = grow(P.t_ps, (size_t)n * 6 * 8, err)) || (rc = grow(P.t_n, (size_t)n * 4, err)) ||
+        (rc = grow(P.t_pos, (size_t)nmax * 3 * n * 8, err)))
+        return rc;
+    if ((rc = ck(cudaMemcpyAsync(P.t_ps.p, ps, (size_t)n * 6 * 8, cudaMemcpyHostToDevice, st), err, "tracks: copy")) ||
+        (rc = ck(cudaMemcpyAsync(P.t_n.p, npts, (size_t)n * 4, cudaMemcpyHostToDevice, st), err, "tracks: copy")) ||
+        (rc = ck(launch_coarse_tracks(st, n, Pb<double>(P.t_ps), Pb<int>(P.t_n), Pb<double>(P.t_pos)), err,
+                 "k_coarse_tracks")))
+        return rc;
+    std::vector<double> h((size_t)nmax * 3 * n);
+    if ((rc = ck(cudaMemcpyAsync(h.data(), P.t_pos.p, h.size() * 8, cudaMemcpyDeviceToHost, st), err, "tracks: copy")) ||
+        (rc = ck(cudaStreamSynchronize(st), err, "tracks")))
+        return rc;
+    size_t o = 0;
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < npts[i]; k++, o++)
+            for (int c = 0; c < 3; c++) pos[3 * o + c] = h[((size_t)k * 3 + c) * n + i];
+    return 0;
+}
+
+int prefilter_pairs(cudaStream_t st, PrefilterState &P, const PhTarget *t, int nt, const PhCluster *c, int nc,
+                    int threads, int *ti, int *ci, long cap, long *n, PrefilterCounts &cnt, std::string &err) {
+    cnt = PrefilterCounts();
+    *n = 0;
+    if (nt <= 0 || nc <= 0) return 0;
+    int rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if ((rc = ck(cudaEventCreate(&e0), err, "prefilter: event")) || (rc = ck(cudaEventCreate(&e1), err, "event"))) {
+        if (e0) cudaEventDestroy(e0);
+        return rc;
+    }
+    struct Events {
+        cudaEvent_t a, b;
+        ~Events() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } events{e0, e1};
+    double tmax = 0;
+    for (int i = 0; i < nc; i++) tmax = std::max(tmax, c[i].tmax_myr);
+    int t_n;
+    if ((rc = points_of(tmax, &t_n, err))) return rc;
+    std::vector<int> cn(nc);
+    for (int i = 0; i < nc; i++)
+        if ((rc = points_of(c[i].tmax_myr, &cn[i], err))) return rc;
+
+    // the cluster side, unless these clusters are the ones held; the host draws first, then the device work in one
+    // stretch of the stream (timed by the events)
+    const uint64_t digest = fnv_bytes(fnv_bytes(14695981039346656037ULL, &nc, sizeof nc), c, sizeof(PhCluster) * nc);
+    const bool fresh = !(P.nc == nc && P.digest == digest && P.c_pos.p);
+    std::vector<double> cps, csig, r0;
+    int c_nmax = 0;
+    if (fresh) {
+        P.nc = 0;
+        free_host_tracks(P);
+        cps.resize((size_t)nc * 6);
+        csig.resize((size_t)nc * 2);
+        r0.resize(nc);
+        pgh_track_starts(nullptr, c, nc, threads, cps.data(), csig.data());
+        for (int i = 0; i < nc; i++) {
+            r0[i] = (3.0 * c[i].rtot_pc + 10.0) / 1000.0;
+            c_nmax = std::max(c_nmax, cn[i]);
+            cnt.body_steps += (long)(cn[i] - 1) * 10;
+        }
+    }
+    std::vector<double> tps((size_t)nt * 6), tsig((size_t)nt * 2);
+    std::vector<int> tn(nt, t_n);
+    pgh_track_starts(t, nullptr, nt, threads, tps.data(), tsig.data());
+    cnt.body_steps += (long)nt * (t_n - 1) * 10;
+
+    if ((rc = ck(cudaEventRecord(e0, st), err, "prefilter: event"))) return rc;
+    if (fresh) {
+        if ((rc = grow(P.c_ps, cps.size() * 8, err)) || (rc = grow(P.c_sig, csig.size() * 8, err)) ||
+            (rc = grow(P.c_n, (size_t)nc * 4, err)) || (rc = grow(P.c_r0, (size_t)nc * 8, err)) ||
+            (rc = grow(P.c_pos, (size_t)c_nmax * 3 * nc * 8, err)))
+            return rc;
+        if ((rc = ck(cudaMemcpyAsync(P.c_ps.p, cps.data(), cps.size() * 8, cudaMemcpyHostToDevice, st), err,
+                     "copy")) ||
+            (rc = ck(cudaMemcpyAsync(P.c_sig.p, csig.data(), csig.size() * 8, cudaMemcpyHostToDevice, st), err,
+                     "copy")) ||
+            (rc = ck(cudaMemcpyAsync(P.c_n.p, cn.data(), (size_t)nc * 4, cudaMemcpyHostToDevice, st), err, "copy")) ||
+            (rc = ck(cudaMemcpyAsync(P.c_r0.p, r0.data(), (size_t)nc * 8, cudaMemcpyHostToDevice, st), err,
+                     "copy")) ||
+            (rc = ck(launch_coarse_tracks(st, nc, Pb<double>(P.c_ps), Pb<int>(P.c_n), Pb<double>(P.c_pos)), err,
+                     "k_coarse_tracks")))
+            return rc;
+        cnt.kernels++;
+    }
+    if ((rc = grow(P.t_ps, tps.size() * 8, err)) || (rc = grow(P.t_sig, tsig.size() * 8, err)) ||
+        (rc = grow(P.t_n, (size_t)nt * 4, err)) || (rc = grow(P.t_pos, (size_t)t_n * 3 * nt * 8, err)) ||
+        (rc = grow(P.keep, (size_t)nt * nc, err)))
+        return rc;
+    if ((rc = ck(cudaMemcpyAsync(P.t_ps.p, tps.data(), tps.size() * 8, cudaMemcpyHostToDevice, st), err, "copy")) ||
+        (rc = ck(cudaMemcpyAsync(P.t_sig.p, tsig.data(), tsig.size() * 8, cudaMemcpyHostToDevice, st), err,
+                 "copy")) ||
+        (rc = ck(cudaMemcpyAsync(P.t_n.p, tn.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, st), err, "copy")) ||
+        (rc = ck(launch_coarse_tracks(st, nt, Pb<double>(P.t_ps), Pb<int>(P.t_n), Pb<double>(P.t_pos)), err,
+                 "k_coarse_tracks")))
+        return rc;
+    cnt.kernels++;
+    for (int j0 = 0; j0 < nt; j0 += 65535) {
+        const dim3 grid((nc + kPrefThreads - 1) / kPrefThreads, std::min(nt - j0, 65535));
+        k_prefilter<<<grid, kPrefThreads, 0, st>>>(nt, nc, j0, t_n, Pb<double>(P.t_pos), Pb<double>(P.t_sig),
+                                                   Pb<int>(P.c_n), Pb<double>(P.c_pos), Pb<double>(P.c_sig),
+                                                   Pb<double>(P.c_r0), P.margin, Pb<unsigned char>(P.keep));
+        if ((rc = ck(cudaGetLastError(), err, "k_prefilter"))) return rc;
+        cnt.kernels++;
+    }
+    if ((rc = ck(cudaEventRecord(e1, st), err, "prefilter: event"))) return rc;
+    P.h_keep.resize((size_t)nt * nc);
+    // the copies above read pageable vectors of this frame; the synchronize below ends them before it returns
+    if ((rc = ck(cudaMemcpyAsync(P.h_keep.data(), P.keep.p, P.h_keep.size(), cudaMemcpyDeviceToHost, st), err,
+                 "copy")) ||
+        (rc = ck(cudaStreamSynchronize(st), err, "k_prefilter")))
+        return rc;
+    cudaEventElapsedTime(&cnt.ms_device, e0, e1);
+    if (fresh) {
+        P.host_ctr.assign(nc, PhTrack{0, nullptr, 0.0, 0.0});
+        P.digest = digest;
+        P.nc = nc;
+    }
+    cnt.pairs = (long)nt * nc;
+
+    // the pairs within the margin: traced and tested by the host code
+    std::vector<int> tj, ci_need;
+    std::vector<char> t_mark(nt, 0), c_mark(nc, 0);
+    for (int j = 0; j < nt; j++)
+        for (int i = 0; i < nc; i++)
+            if (P.h_keep[(size_t)j * nc + i] == 2) {
+                cnt.rechecked++;
+                if (!t_mark[j]) { t_mark[j] = 1; tj.push_back(j); }
+                if (!c_mark[i] && P.host_ctr[i].n == 0) { c_mark[i] = 1; ci_need.push_back(i); }
+            }
+    if (cnt.rechecked) {
+        if (!ci_need.empty()) {
+            std::vector<PhTrack> tr(ci_need.size());
+            TrackJob J{nullptr, c, ci_need.data(), tr.data(), 0.0};
+            pgh_parallel_for((int)ci_need.size(), threads, 1, host_tracks_range, &J);
+            for (size_t q = 0; q < ci_need.size(); q++) P.host_ctr[ci_need[q]] = tr[q];
+        }
+        std::vector<PhTrack> ttr(tj.size());
+        TrackJob J{t, nullptr, tj.data(), ttr.data(), tmax};
+        pgh_parallel_for((int)tj.size(), threads, 1, host_tracks_range, &J);
+        for (size_t q = 0; q < tj.size(); q++) {
+            const int j = tj[q];
+            for (int i = 0; i < nc; i++) {
+                unsigned char &k = P.h_keep[(size_t)j * nc + i];
+                if (k == 2) k = (unsigned char)ph_prefilter(&ttr[q], &P.host_ctr[i], &c[i]);
+            }
+            ph_track_free(&ttr[q]);
+        }
+    }
+    long m = 0;
+    for (int j = 0; j < nt; j++)
+        for (int i = 0; i < nc; i++) {
+            if (!P.h_keep[(size_t)j * nc + i]) continue;
+            if (m < cap) { ti[m] = j; ci[m] = i; }
+            m++;
+        }
+    *n = m;
+    return 0;
+}
+
+}  // namespace pgx

@@ -5,10 +5,10 @@
 // (orbits, covariances, the FP32 copies) and its work buffers resident between jobs.  Jobs -- screen chunks, control
 // chunks, single-target pair jobs -- queue in arrival order.  A job starts when a slot is idle and the estimated
 // device memory of the running jobs plus its own fits the budget (the first job of an empty GPU always starts).  Slot
-// workers run their job's host part (draws, prefilter) on their share of the host cores while other slots' kernels
-// run, so jobs that arrive while others are on the GPU are admitted as slots and memory free up, and their work
-// overlaps on the device.  A job's results depend only on its own inputs: every slot runs the same kernels on its own
-// buffers, so a job gives the same bits alone and in a mix.
+// workers run their job's host part (draws, the prefilter's track starts) on their share of the host cores while
+// other slots' kernels run, so jobs that arrive while others are on the GPU are admitted as slots and memory free up,
+// and their work overlaps on the device.  A job's results depend only on its own inputs: every slot runs the same
+// kernels on its own buffers, so a job gives the same bits alone and in a mix.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -77,7 +77,8 @@ namespace {
 
 // device memory a job needs while it runs, bytes: per screened star its 7 orbits (38.6 KB at 201 points), tracks
 // (FP64 19.3 KB, FP32 9.6 KB), the per-pair filter state (17 B x clusters) and room for its kept pairs; per traced
-// clone its start state, results and queue share (about 130 B)
+// clone its start state, results and queue share (about 130 B); the 64 MiB allowance covers the prefilter's coarse
+// tracks (24 B per point: 19.7 MB for 4,087 clusters of up to 201 points, kept by the slot)
 size_t footprint(const PgxServer &s, const PgxJob &j) {
     const size_t nc = s.clusters.size();
     if (j.kind == PGX_JOB_PAIRS) return (size_t)j.n_targets * nc * (size_t)std::max(j.n_clones, 1) * 130 + (64u << 20);
@@ -123,9 +124,11 @@ int run_pairs(PgxServer &s, PgxContext *ctx, Job &job) {
     const PgxJob &j = job.spec;
     const int nc = (int)s.clusters.size();
     std::vector<int> ti((size_t)j.n_targets * nc), ci((size_t)j.n_targets * nc);
-    const long np = pgh_prefilter_pairs(job.targets.data(), j.n_targets, s.clusters.data(), nc, s.host_threads,
-                                        ti.data(), ci.data(), (long)ti.size());
-    if (np < 0) return PGX_E_NOMEM;
+    // the prefilter on the GPU: the slot's context keeps the cluster tracks, so each job traces only its targets
+    long np = 0;
+    const int prc = pgx_prefilter(ctx, job.targets.data(), j.n_targets, s.clusters.data(), nc, s.host_threads,
+                                  ti.data(), ci.data(), (long)ti.size(), &np);
+    if (prc) return prc;
     std::vector<int> ncl(np, j.n_clones);
     double work = 0;
     if (np > 0) {

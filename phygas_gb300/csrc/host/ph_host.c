@@ -304,28 +304,65 @@ static void spread_of(PhaseSpace nom, const PhaseSpace *d, int n, PhTrack *out) 
     out->sig_vel = n ? sqrt(sv / n) : 0;
 }
 
-void ph_track_target(const PhTarget *t, double tmax, int n_spread, uint64_t seed, PhTrack *out) {
-    PhaseSpace nom, d[64];
+/* the nominal point and the draws of a track's spread (at most 64); returns how many draws succeeded */
+static int track_draws_target(const PhTarget *t, int n_spread, uint64_t seed, PhaseSpace *nom, PhaseSpace d[64]) {
     McRng g;
     int k = 0;
-    ph_sample_target(t, NULL, &nom);
+    ph_sample_target(t, NULL, nom);
     g.state = seed;
     if (n_spread > 64) n_spread = 64;
     for (int i = 0; i < n_spread; i++) if (ph_sample_target(t, &g, &d[k]) == 0) k++;
+    return k;
+}
+
+static int track_draws_cluster(const PhCluster *c, int n_spread, uint64_t seed, PhaseSpace *nom, PhaseSpace d[64]) {
+    McRng g;
+    int k = 0;
+    ph_sample_cluster(c, NULL, nom);
+    g.state = seed;
+    if (n_spread > 64) n_spread = 64;
+    for (int i = 0; i < n_spread; i++) if (ph_sample_cluster(c, &g, &d[k]) == 0) k++;
+    return k;
+}
+
+void ph_track_target(const PhTarget *t, double tmax, int n_spread, uint64_t seed, PhTrack *out) {
+    PhaseSpace nom, d[64];
+    const int k = track_draws_target(t, n_spread, seed, &nom, d);
     coarse(nom, tmax, out);
     spread_of(nom, d, k, out);
 }
 
 void ph_track_cluster(const PhCluster *c, int n_spread, uint64_t seed, PhTrack *out) {
     PhaseSpace nom, d[64];
-    McRng g;
-    int k = 0;
-    ph_sample_cluster(c, NULL, &nom);
-    g.state = seed;
-    if (n_spread > 64) n_spread = 64;
-    for (int i = 0; i < n_spread; i++) if (ph_sample_cluster(c, &g, &d[k]) == 0) k++;
+    const int k = track_draws_cluster(c, n_spread, seed, &nom, d);
     coarse(nom, c->tmax_myr, out);
     spread_of(nom, d, k, out);
+}
+
+typedef struct {
+    const PhTarget *t;
+    const PhCluster *c;
+    double *ps, *sig;
+} StartArg;
+
+static void starts_range(void *p, int i0, int i1) {
+    StartArg *A = p;
+    for (int i = i0; i < i1; i++) {
+        PhaseSpace nom, d[64];
+        PhTrack s;
+        const int k = A->t ? track_draws_target(&A->t[i], 32, ph_seed("track", A->t[i].id), &nom, d)
+                           : track_draws_cluster(&A->c[i], 32, ph_seed("track", A->c[i].name), &nom, d);
+        spread_of(nom, d, k, &s);
+        double *o = A->ps + 6 * (size_t)i;
+        o[0] = nom.pos.x; o[1] = nom.pos.y; o[2] = nom.pos.z; o[3] = nom.vel.x; o[4] = nom.vel.y; o[5] = nom.vel.z;
+        A->sig[2 * (size_t)i] = s.sig_pos;
+        A->sig[2 * (size_t)i + 1] = s.sig_vel;
+    }
+}
+
+void pgh_track_starts(const PhTarget *t, const PhCluster *c, int n, int threads, double *ps, double *sig) {
+    StartArg A = {t, t ? NULL : c, ps, sig};
+    pgh_parallel_for(n, threads, 16, starts_range, &A);
 }
 
 void ph_track_free(PhTrack *t) { free(t->pos); t->pos = NULL; t->n = 0; }

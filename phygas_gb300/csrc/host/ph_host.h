@@ -28,6 +28,10 @@ void pgh_draw_pairs(int n_pairs, const PhTarget *const *t, const PhCluster *cons
  * cluster) order; writes at most cap pairs and returns how many pass (-1: out of memory) */
 long pgh_prefilter_pairs(const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti, int *ci,
                          long cap);
+/* the start of each coarse track as ph_track_target / ph_track_cluster build it (32 spread draws, seeds
+ * ph_seed("track", id/name)), without the track: of n targets (t != NULL) or n clusters, on `threads` host threads;
+ * ps = the nominal phase-space point (6 doubles per object), sig = (sig_pos, sig_vel) per object */
+void pgh_track_starts(const PhTarget *t, const PhCluster *c, int n, int threads, double *ps, double *sig);
 /* ph_pair_draw for pair q = (t[ti[q]], c[ci[q]]) with n_clones[q] clones, seeds ph_seed(id, name); the clones of all
  * pairs written back to back into ps (room for 12 * sum(n_clones) doubles) with clone_off[n_pairs + 1]; steps, dt,
  * r50_pc, rtot_pc per pair.  Returns 0, or -1 (out of memory), -2 (more than 2^31 - 1 clones) */

@@ -4,9 +4,10 @@
  *
  * Same arguments; one stdout row per (target, cluster) pair that passes the prefilter, in (target, cluster) order:
  *   target cluster kind n d05 d50 d95 t05 t50 t95 v05 v50 v95 f_r50 f_rtot age16 age84
- * The tracks, the prefilter and the clone draws (bit-identical to the reference's) run on all host cores; the clones
- * of many pairs and targets are traced and reduced together on the GPU (PHYGAS_BATCH_CLONES per launch, default
- * 2^20), and rows are printed by whole targets.
+ * The prefilter runs on the GPU (pgx_prefilter: the same pairs as the reference's tracks and ph_prefilter keep), the
+ * clone draws (bit-identical to the reference's) on all host cores; the clones of many pairs and targets are traced
+ * and reduced together on the GPU (PHYGAS_BATCH_CLONES per launch, default 2^20), and rows are printed by whole
+ * targets.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -27,12 +28,6 @@ static int wanted(const char *id, const char *only) {
     for (const char *p = only; (p = strstr(p, id)) != NULL; p += n)
         if ((p == only || p[-1] == ',') && (p[n] == ',' || p[n] == '\0')) return 1;
     return 0;
-}
-
-typedef struct { const PhCluster *cl; PhTrack *tr; } TrackArg;
-static void tracks_range(void *p, int i0, int i1) {
-    TrackArg *A = p;
-    for (int i = i0; i < i1; i++) ph_track_cluster(&A->cl[i], 32, ph_seed("track", A->cl[i].name), &A->tr[i]);
 }
 
 typedef struct {        /* pairs waiting for the GPU */
@@ -113,30 +108,32 @@ int main(int argc, char **argv) {
     int rc = pgx_open(-1, &ctx);
     if (rc) { fprintf(stderr, "phygas_cli: no usable GPU (pgx_open: %d)\n", rc); return 1; }
     const int threads = pgh_default_threads();
-    PhTrack *ctr = malloc(sizeof(PhTrack) * nc);
-    TrackArg ta = {cl, ctr};
-    pgh_parallel_for(nc, threads, 16, tracks_range, &ta);
     fprintf(stderr, "%d clusters (traced back up to %.0f Myr), %d targets, %d clones, dt %.3f Myr\n", nc, tmax, nt,
             n_clones, dt);
     long pairs = 0, done = 0;
     double t0 = now_s();
+    /* the wanted targets, prefiltered against every cluster on the GPU in one call */
+    int nw = 0, *widx = malloc(sizeof(int) * nt);
+    PhTarget *wt = malloc(sizeof(PhTarget) * nt);
+    for (int j = 0; j < nt; j++)
+        if (wanted(tg[j].id, only)) { widx[nw] = j; wt[nw++] = tg[j]; }
+    long cap = (long)nw * nc, np = 0;
+    int *pti = malloc(sizeof(int) * (cap > 0 ? cap : 1)), *pci = malloc(sizeof(int) * (cap > 0 ? cap : 1));
+    if (pgx_prefilter(ctx, wt, nw, cl, nc, threads, pti, pci, cap, &np)) {
+        fprintf(stderr, "phygas_cli: prefilter: %s\n", pgx_last_error(ctx));
+        return 1;
+    }
     Pending P = {0, 0, NULL, NULL};
-    for (int j = 0; j < nt; j++) {
-        if (!wanted(tg[j].id, only)) continue;
-        PhTrack tt;
-        ph_track_target(&tg[j], tmax, 32, ph_seed("track", tg[j].id), &tt);
+    for (long q = 0; q < np;) {
+        const int w = pti[q];
         int kept = 0;
-        for (int i = 0; i < nc; i++) {
-            if (!ph_prefilter(&tt, &ctr[i], &cl[i])) continue;
-            kept++;
-            push(&P, j, i);
-        }
-        ph_track_free(&tt);
+        for (; q < np && pti[q] == w; q++, kept++) push(&P, widx[w], pci[q]);
         pairs += kept;
         done++;
         if ((long)P.n * n_clones >= batch && flush(ctx, &P, tg, cl, n_clones, dt, threads)) return 1;
-        fprintf(stderr, "%s: %d of %d clusters reachable (%.1f s so far)\n", tg[j].id, kept, nc, now_s() - t0);
+        fprintf(stderr, "%s: %d of %d clusters reachable (%.1f s so far)\n", tg[widx[w]].id, kept, nc, now_s() - t0);
     }
+    done = nw;
     if (flush(ctx, &P, tg, cl, n_clones, dt, threads)) return 1;
     fprintf(stderr, "# done %ld targets, %ld pairs, %.1f s\n", done, pairs, now_s() - t0);
     pgx_close(ctx);

@@ -420,7 +420,9 @@ def main():
     t0 = time.time()
     ctx.set_clusters(clusters, N_SAMP, R_KERNEL)
     table_s = time.time() - t0
+    t0 = time.perf_counter()
     ps0, sig, pre = pg.draw_targets(stars, N_SAMP)
+    draw_s = time.perf_counter() - t0
     ctx.stage(ps0, sig, pre)
 
     def barrier():
@@ -553,7 +555,8 @@ def main():
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s,
                     "how": "pgx_screen_chunks over %d chunks of the %d stars: host draws of chunk i+2, the orbits of "
                            "chunk i+1 (side stream) and the screen of chunk i overlap; rows copied to page-locked host "
-                           "memory" % (E2E_CHUNKS, N_STARS)},
+                           "memory" % (E2E_CHUNKS, N_STARS),
+                    "host_draw_s_unpipelined": draw_s},
             "roofline": {"bound": "fp64", "kernel": "k_stm_orbits", "achieved": achieved / 1e12,
                          "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
                          "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",

@@ -75,10 +75,11 @@ int pgx_screen(PgxContext *ctx, int nt, const double *ps0, const double *sig, co
 int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *sig, const uint64_t *seed_prefix);
 int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double chi2_max, int precision, long *n_rows);
 int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n);
-/* Chunks of at least min_stars stars (default 8192; 0 = never) are staged as two halves, and exec traces the second
- * half's orbits beside the first half's screen (the mixed path; the FP64 path screens the halves in turn).  The rows
- * are the same either way. */
+/* Chunks of at least min_stars stars (default 8192; 0 = never) are staged in parts (pgx_screen_parts; default 0: parts
+ * of about 4,000 stars, 2 to 8 of them), and exec traces each part's orbits beside the previous part's screen (the
+ * mixed path; the FP64 path screens the parts in turn).  The rows are the same either way. */
 int pgx_screen_split(PgxContext *ctx, int min_stars);
+int pgx_screen_parts(PgxContext *ctx, int parts);
 /* pgx_screen writing into the caller's rows[cap] (no allocation); *n_rows = the kept pairs, PGX_E_LIMIT (rows kept on
  * the device for pgx_screen_fetch) when more than cap.  With rows from pgx_host_alloc the copy runs at the link's
  * full rate: page-locked host memory, allocated once and freed with pgx_host_free. */

@@ -106,6 +106,7 @@ SIGNATURES = [
                                   C.c_long, _P(C.c_long)]),
     ("pgx_host_alloc", C.c_void_p, [C.c_size_t]),
     ("pgx_screen_split", C.c_int, [C.c_void_p, C.c_int]),
+    ("pgx_screen_parts", C.c_int, [C.c_void_p, C.c_int]),
     ("pgx_pair_blocks", C.c_int, [C.c_void_p, C.c_int]),
     ("pgx_pair_targets", C.c_int, [C.c_void_p, C.c_int, _P(PhTarget), _P(C.c_int), _P(PhCluster), _P(C.c_int),
                                    _P(C.c_int), C.c_double, C.c_int, C.c_int, C.c_void_p]),
@@ -411,10 +412,12 @@ class Context:
         """pgx_pair_blocks: the persistent clone kernels on at most blocks_per_sm blocks per SM (0 = all that fit)."""
         self._check(lib().pgx_pair_blocks(self.h, int(blocks_per_sm)), "pgx_pair_blocks")
 
-    def set_split(self, min_stars):
-        """pgx_screen_split: stage chunks of at least min_stars stars as two halves, screened with the second
-        half's orbits beside the first half's screen (0 = never)."""
+    def set_split(self, min_stars, parts=None):
+        """pgx_screen_split / pgx_screen_parts: stage chunks of at least min_stars stars (0 = never) in `parts`
+        parts, each part's orbits traced beside the previous part's screen."""
         self._check(lib().pgx_screen_split(self.h, int(min_stars)), "pgx_screen_split")
+        if parts is not None:
+            self._check(lib().pgx_screen_parts(self.h, int(parts)), "pgx_screen_parts")
 
     def stage(self, ps0, sig, prefix):
         self._keep = (np.ascontiguousarray(ps0, np.float64), np.ascontiguousarray(sig, np.float64),

@@ -46,12 +46,19 @@ enum { EV_START, EV_ORBIT, EV_COV, EV_SCREEN, EV_SCAN, EV_SELECT, EV_FINISH, EV_
 // Blocks per SM of a chunk's orbits traced beside another chunk's screen: few enough to leave the screen its
 // registers (its FP32 and integer work and the orbits' FP64 work use different pipes), enough to finish first.
 constexpr int kSideOrbitBlocksPerSm = 2;
-// pgx_screen_stage splits chunks of at least this many stars in two, so that exec can overlap them
+// pgx_screen_stage splits chunks of at least this many stars in parts, so that exec can overlap one part's orbits
+// with the previous part's screen: by default parts of about kPartStars stars, 2 to kMaxAutoParts of them (measured
+// on 20,000 x 4,087: 123 ms whole, 113 ms in 2 parts, 108-110 ms in 3 to 8; more parts hide more orbit time but
+// their screens share the FP64 pipe with the next part's orbits)
 constexpr int kSplitStars = 8192;
+constexpr int kPartStars = 4000, kMaxAutoParts = 8;
 
 struct TrackSlot {
     int nt = 0, ns = 0;
     Buf ps0, sig21, prefix, opos, ovel, t64, t32, tlm, ids;
+    // the inputs the slot's tracks and screen read: its own buffers, or a part of a split chunk
+    const double *in_ps0 = nullptr, *in_sig21 = nullptr;
+    const uint64_t *in_prefix = nullptr;
     cudaEvent_t done = nullptr;
     char *h_stage = nullptr;                   // page-locked staging of the inputs (SoA), reused
     size_t h_stage_cap = 0;
@@ -69,8 +76,16 @@ struct PgxContext {
     // previous chunk is screened (pgx_screen_chunks); the single-chunk entry points use slot `cur`
     TrackSlot trk[2];
     int cur = 0;
-    int split = 0;                             // > 0: pgx_screen_stage put stars [0, split) in slot 0, the rest in 1
     int split_min = kSplitStars;               // chunks of at least this many stars are split (0: never)
+    int parts = 0;                             // in this many parts (0: about kPartStars stars each)
+    // a split chunk: pgx_screen_stage put part p's inputs (ps0[6][n], sig21[21][n], prefix[n]) at part_at[p] in
+    // part_in; exec binds the parts to the two track slots in turn
+    int nparts = 0;
+    std::vector<int> part_n, part_off;
+    std::vector<size_t> part_at;
+    Buf part_in;
+    char *h_part = nullptr;                    // page-locked staging of part_in
+    size_t h_part_cap = 0;
     cudaStream_t side = nullptr;               // higher priority: the orbits' blocks start as soon as SMs free up
     // the screen's work buffers
     Buf chi2T, kbT, sbT, cnt, off, total, kept, fin, rows;
@@ -189,7 +204,7 @@ pgx::ScreenTables tables(PgxContext *ctx, TrackSlot &k) {
     pgx::ScreenTables T;
     T.nt = k.nt; T.ns = k.ns; T.nc = ctx->nc; T.ncp = ctx->ncp; T.s_off = 0;
     T.t64 = P<double>(k.t64); T.t32 = P<float4>(k.t32); T.lm_t = P<float>(k.tlm);
-    T.seed_prefix = P<uint64_t>(k.prefix);
+    T.seed_prefix = k.in_prefix;
     T.c64 = P<double>(ctx->c64); T.c32 = P<float4>(ctx->c32); T.lm_c = P<float>(ctx->clm); T.cn = P<int>(ctx->cn);
     T.R2 = P<double>(ctx->cR2); T.r50 = P<double>(ctx->cr50); T.rtot = P<double>(ctx->crt);
     T.cname = P<char>(ctx->cname);
@@ -228,6 +243,9 @@ int stage_slot(PgxContext *ctx, int s, int nt, const double *ps0, const double *
     CK(cudaMemcpyAsync(k.ps0.p, p6, b6, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(k.sig21.p, s21, b21, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(k.prefix.p, k.h_stage + b6 + b21, bp, cudaMemcpyHostToDevice, st));
+    k.in_ps0 = P<double>(k.ps0);
+    k.in_sig21 = P<double>(k.sig21);
+    k.in_prefix = P<uint64_t>(k.prefix);
     if (ids) {
         RET(ensure(ctx, k.ids, bi));
         CK(cudaMemcpyAsync(k.ids.p, k.h_stage + b6 + b21 + bp, bi, cudaMemcpyHostToDevice, st));
@@ -246,11 +264,22 @@ int tracks_slot(PgxContext *ctx, int s, double tmax_myr, cudaStream_t st, bool t
     RET(ensure(ctx, k.t64, (size_t)ns * 12 * nt * 8));
     RET(ensure(ctx, k.t32, (size_t)ns * 3 * nt * 16));
     RET(ensure(ctx, k.tlm, (size_t)ns * nt * 4));
-    RET(run_lin(ctx, st, nt, P<double>(k.ps0), P<double>(k.sig21), nullptr, ns, k.opos, k.ovel, P<double>(k.t64),
+    RET(run_lin(ctx, st, nt, k.in_ps0, k.in_sig21, nullptr, ns, k.opos, k.ovel, P<double>(k.t64),
                 P<float4>(k.t32), P<float>(k.tlm), timed, orbit_blocks));
     CK(cudaEventRecord(k.done, st));
     k.ns = ns;
     return 0;
+}
+
+// part p of a split chunk into track slot s (its inputs in ctx->part_in)
+void bind_part(PgxContext *ctx, int s, int p) {
+    TrackSlot &k = ctx->trk[s];
+    const int n = ctx->part_n[p];
+    k.nt = n;
+    k.ns = 0;
+    k.in_ps0 = reinterpret_cast<const double *>(static_cast<const char *>(ctx->part_in.p) + ctx->part_at[p]);
+    k.in_sig21 = k.in_ps0 + (size_t)6 * n;
+    k.in_prefix = reinterpret_cast<const uint64_t *>(k.in_sig21 + (size_t)21 * n);
 }
 
 // ctx->rows with room for `rows` rows, the first `keep` of them kept
@@ -401,9 +430,10 @@ void pgx_close(PgxContext *ctx) {
                    &ctx->p_q, &ctx->p_done, &ctx->p_cres, &ctx->p_res, &ctx->p_params, &ctx->x_ps0, &ctx->x_sig21,
                    &ctx->x_npts,
                    &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32, &ctx->rows_b[0], &ctx->rows_b[1],
-                   &ctx->lab_names, &ctx->lab_kinds, &ctx->lab_age16, &ctx->lab_age84};
+                   &ctx->lab_names, &ctx->lab_kinds, &ctx->lab_age16, &ctx->lab_age84, &ctx->part_in};
     for (Buf *b : bufs)
         if (b->p) cudaFree(b->p);
+    if (ctx->h_part) cudaFreeHost(ctx->h_part);
     for (auto &k : ctx->trk) {
         for (Buf *b : {&k.ps0, &k.sig21, &k.prefix, &k.opos, &k.ovel, &k.t64, &k.t32, &k.tlm, &k.ids})
             if (b->p) cudaFree(b->p);
@@ -695,14 +725,42 @@ int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *s
     if (nt <= 0 || !ps0 || !sig || !prefix) return fail(ctx, PGX_E_ARG, "pgx_screen_stage: bad args");
     CK(cudaSetDevice(ctx->device));
     ctx->cur = 0;
-    ctx->split = 0;
+    ctx->nparts = 0;
     ctx->trk[1].nt = 0;
     if (ctx->split_min <= 0 || nt < ctx->split_min) return stage_slot(ctx, 0, nt, ps0, sig, prefix, nullptr, ctx->st);
-    // two halves in the two track slots, for exec to trace the second beside the first's screen
-    const int n1 = nt / 2;
-    RET(stage_slot(ctx, 0, n1, ps0, sig, prefix, nullptr, ctx->st));
-    RET(stage_slot(ctx, 1, nt - n1, ps0 + (size_t)6 * n1, sig + (size_t)36 * n1, prefix + n1, nullptr, ctx->st));
-    ctx->split = n1;
+    if (nt > (1 << 20)) return fail(ctx, PGX_E_LIMIT, "pgx_screen_stage: %d stars in one chunk (limit 2^20)", nt);
+    // the parts' inputs, SoA per part, back to back: one page-locked staging buffer and one copy
+    const int K = std::min(nt, ctx->parts > 0 ? ctx->parts
+                                              : std::max(2, std::min(kMaxAutoParts, (nt + kPartStars / 2) / kPartStars)));
+    ctx->part_n.assign(K, 0);
+    ctx->part_off.assign(K, 0);
+    ctx->part_at.assign(K, 0);
+    size_t bytes = 0;
+    for (int p = 0, off = 0; p < K; p++) {
+        ctx->part_n[p] = nt / K + (p < nt % K ? 1 : 0);
+        ctx->part_off[p] = off;
+        ctx->part_at[p] = bytes;
+        off += ctx->part_n[p];
+        bytes += (size_t)ctx->part_n[p] * (6 + 21 + 1) * 8;
+    }
+    if (ctx->h_part_cap < bytes) {
+        pgx_host_free(ctx->h_part);
+        ctx->h_part_cap = 0;
+        ctx->h_part = (char *)pgx_host_alloc(bytes);
+        if (!ctx->h_part) return fail(ctx, PGX_E_NOMEM, "pgx_screen_stage: %zu bytes of page-locked memory", bytes);
+        ctx->h_part_cap = bytes;
+    }
+    for (int p = 0; p < K; p++) {
+        const int n = ctx->part_n[p], o = ctx->part_off[p];
+        double *p6 = reinterpret_cast<double *>(ctx->h_part + ctx->part_at[p]), *s21 = p6 + (size_t)6 * n;
+        to_soa_into(n, ps0 + (size_t)6 * o, sig + (size_t)36 * o, p6, s21);
+        memcpy(s21 + (size_t)21 * n, prefix + o, (size_t)n * 8);
+    }
+    RET(ensure(ctx, ctx->part_in, bytes));
+    CK(cudaMemcpyAsync(ctx->part_in.p, ctx->h_part, bytes, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->nparts = K;
+    bind_part(ctx, 0, 0);
     return 0;
 }
 
@@ -710,6 +768,13 @@ int pgx_screen_split(PgxContext *ctx, int min_stars) {
     if (!ctx) return PGX_E_ARG;
     if (min_stars < 0) return fail(ctx, PGX_E_ARG, "pgx_screen_split: %d", min_stars);
     ctx->split_min = min_stars;
+    return 0;
+}
+
+int pgx_screen_parts(PgxContext *ctx, int parts) {
+    if (!ctx) return PGX_E_ARG;
+    if (parts != 0 && (parts < 2 || parts > 64)) return fail(ctx, PGX_E_ARG, "pgx_screen_parts: %d (0, or 2 to 64)", parts);
+    ctx->parts = parts;
     return 0;
 }
 
@@ -722,33 +787,51 @@ int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision,
     CK(cudaSetDevice(ctx->device));
     ctx->stats = PgxStats();
     CK(cudaEventRecord(ctx->ev[EV_START], ctx->st));
-    RET(tracks_slot(ctx, ctx->cur, tmax_myr, ctx->st, true));
-    if (ctx->split == 0) return screen_slot(ctx, ctx->cur, cut, precision, n_rows, true);
-    // a staged chunk in two halves: with the mixed screen the second half's orbits run on the side stream beside
-    // the first half's screen (FP64 pipe beside FP32 and integer work); the plain FP64 path runs them in turn
+    if (ctx->nparts == 0) {
+        RET(tracks_slot(ctx, ctx->cur, tmax_myr, ctx->st, true));
+        return screen_slot(ctx, ctx->cur, cut, precision, n_rows, true);
+    }
+    // a chunk staged in parts: part p is screened from slot p & 1 while, with the mixed screen, part p + 1's orbits
+    // run on the side stream in the other slot (FP64 pipe beside FP32 and integer work); the plain FP64 path runs
+    // them in turn.  A slot is bound to its next part only after its previous part's screen has returned (the
+    // screen ends with a synchronize).  The first part's orbits are the only ones not hidden.
+    const int K = ctx->nparts;
     const bool overlap = precision == PGX_MIXED;
-    if (overlap) RET(tracks_slot(ctx, 1, tmax_myr, ctx->side, false, kSideOrbitBlocksPerSm * ctx->sms));
-    long na = 0, nb = 0;
-    RET(screen_slot(ctx, 0, cut, precision, &na, true));
-    const PgxStats a = ctx->stats;
-    if (!overlap) RET(tracks_slot(ctx, 1, tmax_myr, ctx->st, false));
-    RET(screen_slot(ctx, 1, cut, precision, &nb, true, na, ctx->split));
-    // the stages of both halves; the orbit and covariance times are the first half's (the second half's ran beside
-    // its screen, or in turn on the plain path)
-    PgxStats &S = ctx->stats;
-    S.ms_scan += a.ms_scan;
-    S.ms_select += a.ms_select;
-    S.ms_finish += a.ms_finish;
-    S.pairs += a.pairs;
-    S.kept += a.kept;
-    S.body_steps += a.body_steps;
-    S.orbit_body_steps = a.body_steps;
-    S.candidates += a.candidates;
-    S.ambiguous += a.ambiguous;
-    S.rechecked_points += a.rechecked_points;
-    S.rechecked_draws += a.rechecked_draws;
-    S.kernels += a.kernels;
-    if (n_rows) *n_rows = na + nb;
+    bind_part(ctx, 0, 0);
+    RET(tracks_slot(ctx, 0, tmax_myr, ctx->st, true));
+    long rows = 0;
+    for (int p = 0; p < K; p++) {
+        const int s = p & 1;
+        if (p + 1 < K) {
+            bind_part(ctx, s ^ 1, p + 1);
+            if (overlap) RET(tracks_slot(ctx, s ^ 1, tmax_myr, ctx->side, false, kSideOrbitBlocksPerSm * ctx->sms));
+        }
+        // the first part's screen keeps the exec's stats (its orbit and covariance times); later parts' are added
+        const PgxStats acc = ctx->stats;
+        if (p > 0) ctx->stats = PgxStats();
+        long np = 0;
+        RET(screen_slot(ctx, s, cut, precision, &np, true, rows, ctx->part_off[p]));
+        if (p > 0) {
+            PgxStats &S = ctx->stats;
+            S.ms_orbit = acc.ms_orbit;
+            S.ms_cov = acc.ms_cov;
+            S.ms_scan += acc.ms_scan;
+            S.ms_select += acc.ms_select;
+            S.ms_finish += acc.ms_finish;
+            S.pairs += acc.pairs;
+            S.kept += acc.kept;
+            S.body_steps += acc.body_steps;
+            S.orbit_body_steps = acc.orbit_body_steps;
+            S.candidates += acc.candidates;
+            S.ambiguous += acc.ambiguous;
+            S.rechecked_points += acc.rechecked_points;
+            S.rechecked_draws += acc.rechecked_draws;
+            S.kernels += acc.kernels;
+        }
+        rows += np;
+        if (!overlap && p + 1 < K) RET(tracks_slot(ctx, s ^ 1, tmax_myr, ctx->st, false));
+    }
+    if (n_rows) *n_rows = rows;
     return 0;
 }
 
@@ -972,7 +1055,7 @@ int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n
     }
     if (gpu.joinable()) gpu.join();
     // the slots hold pipeline chunks now, not a pgx_screen_stage chunk
-    ctx->split = 0;
+    ctx->nparts = 0;
     ctx->trk[0].nt = ctx->trk[1].nt = 0;
     // codes set here, after the worker has ended, so that the message is this function's
     if (rc == PGX_E_ARG) rc = fail(ctx, PGX_E_ARG, "screen chunks: the output callback stopped the run");

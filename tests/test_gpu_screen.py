@@ -205,9 +205,10 @@ def test_screen_chunks_text_is_printf_of_the_rows(ctx, golden):
 
 
 def test_split_chunk_equals_unsplit(ctx, golden):
-    """A staged chunk of at least 8,192 stars is screened in two halves (the second half's orbits beside the first
-    half's screen): its rows -- star indices across the halves, their order, every field -- equal the same chunk
-    screened whole through pgx_screen_chunks, in both precisions."""
+    """A staged chunk of at least 8,192 stars is screened in parts (each part's orbits beside the previous part's
+    screen, the two track slots in turn): its rows -- star indices across the parts, their order, every field --
+    equal the same chunk screened whole through pgx_screen_chunks, in both precisions, for 2, 3 (uneven), 4 and 7
+    parts."""
     from phygas_gb300 import synth
     import tempfile
     with tempfile.TemporaryDirectory() as d:
@@ -215,11 +216,19 @@ def test_split_chunk_equals_unsplit(ctx, golden):
         clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
     ctx.set_clusters(clusters)
     tmax = max(c.tmax_myr for c in clusters)
-    for prec in PRECISIONS:
-        split = ctx.screen(*pg.draw_targets(stars), tmax, 25.0, prec)
-        whole = []
-        ctx.screen_chunks(stars, len(stars), tmax, lambda first, rows: whole.append(np.array(rows, copy=True)),
-                          25.0, prec)
-        assert len(whole) == 1 and len(split) > 10000
-        assert split["star"].max() > len(stars) // 2                 # rows from both halves
-        assert split.tobytes() == whole[0].tobytes(), prec
+    draws = pg.draw_targets(stars)
+    try:
+        for prec in PRECISIONS:
+            whole = []
+            ctx.screen_chunks(stars, len(stars), tmax, lambda first, rows: whole.append(np.array(rows, copy=True)),
+                              25.0, prec)
+            assert len(whole) == 1 and len(whole[0]) > 10000
+            for parts in (2, 3, 4, 7):
+                ctx.set_split(8192, parts)
+                split = ctx.screen(*draws, tmax, 25.0, prec)
+                st = ctx.stats()
+                assert split["star"].max() > len(stars) * (parts - 1) // parts      # rows from the last part
+                assert split.tobytes() == whole[0].tobytes(), (prec, parts)
+                assert st["kept"] == len(split) and st["pairs"] == len(stars) * len(clusters), (prec, parts)
+    finally:
+        ctx.set_split(8192, 0)

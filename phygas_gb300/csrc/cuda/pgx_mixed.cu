@@ -13,7 +13,8 @@
 //                    where it is well conditioned), 32 at a time on full warps.
 //                    Per pair: its candidate points -- those that can be the FP64 minimum of a kept pair
 //                    (LB_k < cut, LB_k <= min UB) -- in four slots, or "more than four".
-//   k_mx_count / k_mx_emit   stable compaction, per star, of the pairs that may be kept
+//   k_mx_count / k_mx_emit   stable compaction of the pairs that may be kept, a thread per (star, range of 1/16 of
+//                            the clusters)
 //   k_mx_list_*      the listed candidates written out; k_mx_cand walks the overflowed pairs again for theirs,
 //                    keeping up to 64 per pair for k_mx_cand_copy (k_mx_cand_big walks a pair with more a third time)
 //   k_mx_eval64      one thread per candidate point: the FP64 point chi2 (full warps on the scarce FP64 pipe)
@@ -348,21 +349,36 @@ struct PossPair {
     unsigned long long klist;     // the candidate slots, as k_mx_scan32 left them
 };
 
+// A star's clusters are split into kEmitGroups contiguous ranges, one thread per (star, range) (grid y = range), so
+// that a part of a few thousand stars still fills the GPU.  Counts and offsets are indexed s * kEmitGroups + g: the
+// scan over them is in (star, cluster) order.
+constexpr int kEmitGroups = 16;
+
+__device__ __forceinline__ void emit_range(int nc, int g, int &c0, int &c1) {
+    const int len = (nc + kEmitGroups - 1) / kEmitGroups;
+    c0 = min(nc, g * len);
+    c1 = min(nc, c0 + len);
+}
+
 __global__ void k_mx_count(int nt, int nc, const unsigned char *__restrict__ flag, int *__restrict__ npair) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x, g = blockIdx.y;
     if (s >= nt) return;
+    int c0, c1;
+    emit_range(nc, g, c0, c1);
     int a = 0;
-    for (int c = 0; c < nc; c++) a += flag[(size_t)c * nt + s] != 0;
-    npair[s] = a;
+    for (int c = c0; c < c1; c++) a += flag[(size_t)c * nt + s] != 0;
+    npair[(size_t)s * kEmitGroups + g] = a;
 }
 
 __global__ void k_mx_emit(int nt, int nc, const unsigned char *__restrict__ flag, const float *__restrict__ ubmin,
                           const unsigned long long *__restrict__ klist, const int *__restrict__ opair,
                           PossPair *__restrict__ P) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x, g = blockIdx.y;
     if (s >= nt) return;
-    int p = opair[s];
-    for (int c = 0; c < nc; c++) {
+    int c0, c1;
+    emit_range(nc, g, c0, c1);
+    int p = opair[(size_t)s * kEmitGroups + g];
+    for (int c = c0; c < c1; c++) {
         const size_t o = (size_t)c * nt + s;
         const int f = flag[o];
         if (!f) continue;
@@ -573,9 +589,10 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
     const int nt = T.nt, nc = T.nc;
     const size_t pairs = (size_t)nt * nc;
     int rc, launches = 0;
-    const int nbs = nt / kScanBlock + 2;
+    const size_t ng = (size_t)nt * kEmitGroups;         // (star, cluster range) counts
+    const int nbs = (int)(ng / kScanBlock) + 2;
     if ((rc = grow(m.flag, pairs, err)) || (rc = grow(m.ub, pairs * 4, err)) || (rc = grow(m.kmin, pairs * 8, err)) ||
-        (rc = grow(m.cnt, (size_t)nt * 4, err)) || (rc = grow(m.off, (size_t)nt * 4, err)) ||
+        (rc = grow(m.cnt, ng * 4, err)) || (rc = grow(m.off, ng * 4, err)) ||
         (rc = grow(m.total, 64, err)) || (rc = grow(m.aux, (size_t)nbs * 4 + 64, err)))
         return rc;
     int *cnt = Pb<int>(m.cnt), *off = Pb<int>(m.off), *tot = Pb<int>(m.total), *part = Pb<int>(m.aux);
@@ -589,8 +606,9 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
                                    Pb<unsigned long long>(m.kmin));
     if ((rc = check(cudaGetLastError(), err, "k_mx_scan32"))) return rc;
     if ((rc = check(cudaEventRecord(ev_scan, st), err, "event"))) return rc;
-    k_mx_count<<<(nt + 127) / 128, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), cnt);
-    if ((rc = exclusive_scan(st, nt, cnt, off, part, tot, err))) return rc;
+    const dim3 ge((nt + 127) / 128, kEmitGroups);
+    k_mx_count<<<ge, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), cnt);
+    if ((rc = exclusive_scan(st, (int)ng, cnt, off, part, tot, err))) return rc;
     launches += 2 + 3;
     int np = 0;
     if ((rc = check(cudaMemcpyAsync(&np, tot, 4, cudaMemcpyDeviceToHost, st), err, "counts")) ||
@@ -607,8 +625,8 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
     int *A = Pb<int>(m.cand_off), *pc = A + np, *po = pc + np, *ppart = po + np;
     PairBest *B = Pb<PairBest>(m.entq);
     int *kf = reinterpret_cast<int *>(B + np), *ko = kf + np;
-    k_mx_emit<<<(nt + 127) / 128, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
-                                                Pb<unsigned long long>(m.kmin), off, P);
+    k_mx_emit<<<ge, 128, 0, st>>>(nt, nc, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
+                                  Pb<unsigned long long>(m.kmin), off, P);
     launches += 1;
     int na = 0, ne = 0, nk = 0;
     if (np > 0) {

@@ -76,8 +76,8 @@ int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *s
 int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double chi2_max, int precision, long *n_rows);
 int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n);
 /* Chunks of at least min_stars stars (default 8192; 0 = never) are staged in parts (pgx_screen_parts; default 0: parts
- * of about 4,000 stars, 2 to 8 of them), and exec traces each part's orbits beside the previous part's screen (the
- * mixed path; the FP64 path screens the parts in turn).  The rows are the same either way. */
+ * of about 1e7 star-cluster pairs, at least 2), and exec traces each part's orbits beside the previous part's screen
+ * (the mixed path; the FP64 path screens the parts in turn).  The rows are the same either way. */
 int pgx_screen_split(PgxContext *ctx, int min_stars);
 int pgx_screen_parts(PgxContext *ctx, int parts);
 /* pgx_screen writing into the caller's rows[cap] (no allocation); *n_rows = the kept pairs, PGX_E_LIMIT (rows kept on

@@ -47,11 +47,12 @@ enum { EV_START, EV_ORBIT, EV_COV, EV_SCREEN, EV_SCAN, EV_SELECT, EV_FINISH, EV_
 // registers (its FP32 and integer work and the orbits' FP64 work use different pipes), enough to finish first.
 constexpr int kSideOrbitBlocksPerSm = 2;
 // pgx_screen_stage splits chunks of at least this many stars in parts, so that exec can overlap one part's orbits
-// with the previous part's screen: by default parts of about kPartStars stars, 2 to kMaxAutoParts of them (measured
-// on 20,000 x 4,087: 123 ms whole, 113 ms in 2 parts, 108-110 ms in 3 to 8; more parts hide more orbit time but
-// their screens share the FP64 pipe with the next part's orbits)
+// with the previous part's screen: by default parts of about kPartPairs star-cluster pairs (2,447 stars at 4,087
+// clusters).  A part's screen must outlast the next part's orbits, whose 2,000 KDK steps set a latency floor of a few
+// ms: measured on 20,000 x 4,087, 122 ms whole, 103 ms in 5 parts, 100 ms in 8, 104 ms in 12, 116 ms in 16; and 3
+// parts best for 8,192 stars, 5 for 12,000.
 constexpr int kSplitStars = 8192;
-constexpr int kPartStars = 4000, kMaxAutoParts = 8;
+constexpr double kPartPairs = 1.0e7;
 
 struct TrackSlot {
     int nt = 0, ns = 0;
@@ -77,7 +78,7 @@ struct PgxContext {
     TrackSlot trk[2];
     int cur = 0;
     int split_min = kSplitStars;               // chunks of at least this many stars are split (0: never)
-    int parts = 0;                             // in this many parts (0: about kPartStars stars each)
+    int parts = 0;                             // in this many parts (0: about kPartPairs pairs each)
     // a split chunk: pgx_screen_stage put part p's inputs (ps0[6][n], sig21[21][n], prefix[n]) at part_at[p] in
     // part_in; exec binds the parts to the two track slots in turn
     int nparts = 0;
@@ -730,8 +731,9 @@ int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *s
     if (ctx->split_min <= 0 || nt < ctx->split_min) return stage_slot(ctx, 0, nt, ps0, sig, prefix, nullptr, ctx->st);
     if (nt > (1 << 20)) return fail(ctx, PGX_E_LIMIT, "pgx_screen_stage: %d stars in one chunk (limit 2^20)", nt);
     // the parts' inputs, SoA per part, back to back: one page-locked staging buffer and one copy
+    const double part_stars = std::max(1.0, kPartPairs / std::max(ctx->nc, 1));
     const int K = std::min(nt, ctx->parts > 0 ? ctx->parts
-                                              : std::max(2, std::min(kMaxAutoParts, (nt + kPartStars / 2) / kPartStars)));
+                                              : std::max(2, std::min(64, (int)std::lround(nt / part_stars))));
     ctx->part_n.assign(K, 0);
     ctx->part_off.assign(K, 0);
     ctx->part_at.assign(K, 0);

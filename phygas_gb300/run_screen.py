@@ -32,7 +32,7 @@ def main(argv=None):
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--parts", type=int, default=None,
                     help="parts of a chunk of at least 8,192 stars (pgx_screen_parts; 1 = screened whole; "
-                         "default: about 4,000 stars a part)")
+                         "default: about 1e7 star-cluster pairs a part)")
     a = ap.parse_args(argv)
     with tempfile.TemporaryDirectory() as d:
         cp, tp = synth.write_workload(d, "screen", a.stars, a.seed, a.clusters)

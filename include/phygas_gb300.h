@@ -24,7 +24,7 @@ extern "C" {
 #define PGX_E_ARG 1        /* a size or pointer is invalid */
 #define PGX_E_CUDA 2       /* a CUDA call or kernel failed */
 #define PGX_E_NOMEM 3      /* device memory exhausted */
-#define PGX_E_TIMEOUT 4    /* a bounded device-side wait ran out */
+#define PGX_E_TIMEOUT 4    /* a bounded wait ran out (pgx_server_wait_for) */
 #define PGX_E_LIMIT 5      /* beyond a documented size limit */
 #define PGX_E_NODEV 6      /* no usable GPU */
 #define PGX_E_PENDING 7    /* pgx_server_query: the job has not finished */
@@ -267,6 +267,8 @@ int pgx_server_open(int device, int slots, double hbm_budget_gb, const PhCluster
                     double r_kernel, int host_threads, PgxServer **out);
 int pgx_server_submit(PgxServer *s, const PgxJob *job, long *id);
 int pgx_server_wait(PgxServer *s, long id, PgxJobResult *out);     /* blocks until the job has finished */
+/* the same for at most timeout_s seconds: PGX_E_TIMEOUT (out = the job's state so far) when it has not finished */
+int pgx_server_wait_for(PgxServer *s, long id, double timeout_s, PgxJobResult *out);
 int pgx_server_query(PgxServer *s, long id, PgxJobResult *out);    /* PGX_E_PENDING until then */
 /* a finished job's results (cap records at most; returns the count, -1 if unknown or unfinished):
  * screen and control rows, or the pair jobs' PhResult with each pair's cluster index */

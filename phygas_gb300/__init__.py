@@ -17,7 +17,8 @@ PAIR_CLI = os.path.join(LIB_DIR, "phygas_cli")
 SERVE_CLI = os.path.join(LIB_DIR, "phygas_serve")
 
 PGX_FP64, PGX_MIXED = 0, 1
-ERRORS = {1: "bad argument", 2: "CUDA error", 3: "out of device memory", 4: "device wait timed out",
+PGX_E_TIMEOUT = 4
+ERRORS = {1: "bad argument", 2: "CUDA error", 3: "out of device memory", 4: "wait timed out",
           5: "size limit", 6: "no usable GPU", 7: "job still running"}
 
 
@@ -140,6 +141,7 @@ SIGNATURES = [
     ("pgx_server_submit", C.c_int, [C.c_void_p, _P(PgxJob), _P(C.c_long)]),
     ("pgx_server_wait", C.c_int, [C.c_void_p, C.c_long, _P(PgxJobResult)]),
     ("pgx_server_query", C.c_int, [C.c_void_p, C.c_long, _P(PgxJobResult)]),
+    ("pgx_server_wait_for", C.c_int, [C.c_void_p, C.c_long, C.c_double, _P(PgxJobResult)]),
     ("pgx_server_rows", C.c_long, [C.c_void_p, C.c_long, C.c_void_p, C.c_long]),
     ("pgx_server_pairs", C.c_long, [C.c_void_p, C.c_long, C.c_void_p, _I, C.c_long]),
     ("pgx_server_release", None, [C.c_void_p, C.c_long]),
@@ -549,9 +551,17 @@ class Server:
             raise GpuError("pgx_server_submit: %s" % ERRORS.get(rc, rc))
         return jid.value
 
-    def wait(self, jid):
+    def wait(self, jid, timeout=None):
+        """The job's result once it has finished; with a timeout (seconds), TimeoutError if it has not by then."""
         r = PgxJobResult()
-        lib().pgx_server_wait(self.h, jid, C.byref(r))
+        if timeout is None:
+            lib().pgx_server_wait(self.h, jid, C.byref(r))
+        else:
+            rc = lib().pgx_server_wait_for(self.h, jid, float(timeout), C.byref(r))
+            if rc == PGX_E_TIMEOUT:
+                raise TimeoutError("job %d has not finished after %g s" % (jid, timeout))
+            if rc:
+                raise GpuError("pgx_server_wait_for: %s" % ERRORS.get(rc, rc))
         return {k: getattr(r, k) for k, _ in PgxJobResult._fields_}
 
     def rows(self, jid):

@@ -280,6 +280,17 @@ int pgx_server_wait(PgxServer *s, long id, PgxJobResult *out) {
     return 0;
 }
 
+int pgx_server_wait_for(PgxServer *s, long id, double timeout_s, PgxJobResult *out) {
+    if (!s || !(timeout_s >= 0.0)) return PGX_E_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    Job *j = find(s, id);
+    if (!j) return PGX_E_ARG;
+    const bool done = s->cv_done.wait_for(lk, std::chrono::duration<double>(std::min(timeout_s, 1e7)),
+                                          [&] { return j->done; });
+    if (out) *out = j->out;
+    return done ? 0 : PGX_E_TIMEOUT;
+}
+
 int pgx_server_query(PgxServer *s, long id, PgxJobResult *out) {
     if (!s) return PGX_E_ARG;
     std::lock_guard<std::mutex> lk(s->mu);

@@ -65,3 +65,16 @@ def test_memory_budget_admits_one_job_at_a_time(inputs):
     assert st["max_running"] == 1
     order = sorted(res, key=lambda r: r["t_start"])
     assert all(a["t_end"] <= b["t_start"] for a, b in zip(order, order[1:]))
+
+
+def test_bounded_wait_times_out_then_the_job_completes(inputs):
+    """pgx_server_wait_for: PGX_E_TIMEOUT (TimeoutError) while a job runs, the result once it has finished."""
+    clusters, stars, pulsars = inputs
+    with pg.Server(clusters, slots=1) as srv:
+        jid = srv.submit(pg.PGX_JOB_PAIRS, pulsars[0:1], n_clones=1000)
+        with pytest.raises(TimeoutError):
+            srv.wait(jid, timeout=0.001)
+        done = srv.wait(jid)
+        again = srv.wait(jid, timeout=0.001)
+    assert done["status"] == 0 and done["n_out"] > 0
+    assert again == done

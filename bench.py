@@ -367,6 +367,8 @@ def reference_arm(args):
         base["value"] = v
         print(json.dumps({"impl": "reference", "metric": "pairs/s", "value": v, "unit": "pairs/s",
                           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": N_STARS * N_CLUSTERS / v * 1e3,
+                          "ms_per_step_note": "the full %d x %d step at the sample's rate" % (N_STARS, N_CLUSTERS),
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                           "data": "synthetic", "config": config(args),
                           "cpu_baseline": base,

@@ -140,6 +140,16 @@ int pgx_prefilter(PgxContext *ctx, const PhTarget *t, int nt, const PhCluster *c
 /* The distance (kpc, >= 0) the GPU's prefilter decisions keep from the threshold, a bound on how far a GPU-traced
  * track point may lie from the host-traced one (default 1e-7). */
 int pgx_prefilter_margin(PgxContext *ctx, double margin_kpc);
+/* Stage-2 pair selection (the reference BOINC app's pair mode, src/main_phygas_boinc.cpp:309-333 and 445-447): a
+ * target whose lists[j] is a non-empty comma-separated list of cluster names ("clusters=" on its work-unit line)
+ * runs exactly the clusters named there, in cluster order; every other target (lists NULL, or lists[j] NULL or "")
+ * runs the clusters that pass the prefilter (pgx_prefilter).  Pairs in (target, cluster) order, at most cap written
+ * to ti/ci, *n = how many. */
+int pgx_pairs_with_lists(PgxContext *ctx, const PhTarget *t, int nt, const char *const *lists, const PhCluster *c,
+                         int nc, int threads, int *ti, int *ci, long cap, long *n);
+/* The clusters a "clusters=" list names (a name matches a whole comma-separated item): their indices, in cluster
+ * order, at most cap written to ci; returns how many match. */
+int pgx_cluster_list(const PhCluster *c, int nc, const char *list, int *ci, int cap);
 /* Coarse tracks of n objects (reference track, src/phygas.c:98-111): from nominal starts ps (6 doubles each; kpc,
  * kpc/Myr), npts[i] points 0.5 Myr apart (10 KDK steps of -0.05 Myr): pos = 3 npts[i] doubles per object, back to
  * back. */

@@ -124,6 +124,9 @@ SIGNATURES = [
     ("pgx_prefilter", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, _P(PhCluster), C.c_int, C.c_int, _I, _I,
                                 C.c_long, _P(C.c_long)]),
     ("pgx_prefilter_margin", C.c_int, [C.c_void_p, C.c_double]),
+    ("pgx_pairs_with_lists", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, _P(C.c_char_p), _P(PhCluster), C.c_int,
+                                       C.c_int, _I, _I, C.c_long, _P(C.c_long)]),
+    ("pgx_cluster_list", C.c_int, [_P(PhCluster), C.c_int, C.c_char_p, _I, C.c_int]),
     ("pgx_tracks", C.c_int, [C.c_void_p, C.c_int, _D, _I, _D]),
     ("pgx_draw_pair_batch", C.c_int, [C.c_int, _P(PhTarget), _I, _P(PhCluster), _I, _I, C.c_double, C.c_int, _I, _D,
                                       _I, _D, _D, _D]),
@@ -398,6 +401,19 @@ class Context:
                                         _ptr(ti, C.c_int), _ptr(ci, C.c_int), cap, C.byref(n)), "pgx_prefilter")
         return ti[:n.value], ci[:n.value]
 
+    def pairs_with_lists(self, targets, lists, clusters, threads=0):
+        """pgx_pairs_with_lists: stage-2 pairs -- a target with a "clusters=" list (lists[j], str or None) gets the
+        clusters it names, the others the prefilter's; (target index, cluster index) arrays."""
+        targets, clusters = as_array(targets, PhTarget), as_array(clusters, PhCluster)
+        arr = (C.c_char_p * max(len(targets), 1))(*[(x or "").encode() for x in lists])
+        n = C.c_long()
+        cap = len(targets) * len(clusters)
+        ti, ci = np.zeros(max(cap, 1), np.int32), np.zeros(max(cap, 1), np.int32)
+        self._check(lib().pgx_pairs_with_lists(self.h, targets, len(targets), arr, clusters, len(clusters),
+                                               int(threads), _ptr(ti, C.c_int), _ptr(ci, C.c_int), cap, C.byref(n)),
+                    "pgx_pairs_with_lists")
+        return ti[:n.value], ci[:n.value]
+
     def prefilter_margin(self, margin_kpc):
         """pgx_prefilter_margin: the distance (kpc) the GPU's prefilter decisions keep from the threshold."""
         self._check(lib().pgx_prefilter_margin(self.h, float(margin_kpc)), "pgx_prefilter_margin")
@@ -596,6 +612,16 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def cluster_list(clusters, names):
+    """pgx_cluster_list: indices, in cluster order, of the clusters a comma-separated "clusters=" list names."""
+    clusters = as_array(clusters, PhCluster)
+    ci = np.zeros(max(len(clusters), 1), np.int32)
+    k = lib().pgx_cluster_list(clusters, len(clusters), names.encode(), _ptr(ci, C.c_int), len(clusters))
+    if k < 0:
+        raise ValueError("pgx_cluster_list: %d" % k)
+    return ci[:k]
 
 
 def prefilter_pairs(targets, clusters, threads=0):

@@ -526,6 +526,65 @@ int pgx_prefilter(PgxContext *ctx, const PhTarget *t, int nt, const PhCluster *c
     return 0;
 }
 
+int pgx_cluster_list(const PhCluster *c, int nc, const char *list, int *ci, int cap) {
+    if (nc < 0 || (nc > 0 && !c) || cap < 0 || (cap > 0 && !ci)) return -PGX_E_ARG;
+    if (!list) return 0;
+    int m = 0;
+    for (int i = 0; i < nc; i++) {
+        // whole items of the list: the name bounded by the list's start or a comma, and by a comma or the end
+        char name[sizeof c[i].name + 1];
+        const size_t len = strnlen(c[i].name, sizeof c[i].name);
+        if (len == 0) continue;
+        memcpy(name, c[i].name, len);
+        name[len] = '\0';
+        bool hit = false;
+        for (const char *p = list; !hit && (p = strstr(p, name)) != nullptr; p += len)
+            hit = (p == list || p[-1] == ',') && (p[len] == ',' || p[len] == '\0');
+        if (!hit) continue;
+        if (m < cap) ci[m] = i;
+        m++;
+    }
+    return m;
+}
+
+int pgx_pairs_with_lists(PgxContext *ctx, const PhTarget *t, int nt, const char *const *lists, const PhCluster *c,
+                         int nc, int threads, int *ti, int *ci, long cap, long *n) {
+    if (!ctx) return PGX_E_ARG;
+    if (nt < 0 || nc < 0 || cap < 0 || !n || (nt > 0 && !t) || (nc > 0 && !c) || (cap > 0 && (!ti || !ci)))
+        return fail(ctx, PGX_E_ARG, "pgx_pairs_with_lists: bad args");
+    *n = 0;
+    // the targets without a list through the GPU prefilter, in one call
+    std::vector<int> pre_idx;
+    std::vector<PhTarget> pre_t;
+    for (int j = 0; j < nt; j++)
+        if (!lists || !lists[j] || !lists[j][0]) {
+            pre_idx.push_back(j);
+            pre_t.push_back(t[j]);
+        }
+    const long pcap = (long)pre_t.size() * nc;
+    std::vector<int> pti(std::max(pcap, 1L)), pci(std::max(pcap, 1L));
+    long np = 0;
+    if (!pre_t.empty()) RET(pgx_prefilter(ctx, pre_t.data(), (int)pre_t.size(), c, nc, threads, pti.data(), pci.data(),
+                                          pcap, &np));
+    // merge in target order: a listed target's clusters from its list, the others' from the prefilter
+    std::vector<int> li(std::max(nc, 1));
+    long m = 0, q = 0;
+    size_t w = 0;
+    for (int j = 0; j < nt; j++) {
+        if (w < pre_idx.size() && pre_idx[w] == j) {
+            for (; q < np && pti[q] == (int)w; q++, m++)
+                if (m < cap) { ti[m] = j; ci[m] = pci[q]; }
+            w++;
+            continue;
+        }
+        const int k = pgx_cluster_list(c, nc, lists[j], li.data(), nc);
+        for (int a = 0; a < k; a++, m++)
+            if (m < cap) { ti[m] = j; ci[m] = li[a]; }
+    }
+    *n = m;
+    return 0;
+}
+
 int pgx_prefilter_margin(PgxContext *ctx, double margin_kpc) {
     if (!ctx) return PGX_E_ARG;
     if (!(margin_kpc >= 0.0 && margin_kpc <= 1e6)) return fail(ctx, PGX_E_ARG, "pgx_prefilter_margin: %g", margin_kpc);

@@ -131,3 +131,18 @@ def test_edge_cases(ctx, inputs):
     assert np.array_equal(ti, gi) and np.array_equal(ci, gc)
     with pytest.raises(pg.GpuError):
         ctx.prefilter_margin(-1.0)
+
+
+def test_stage2_pairs_with_lists(ctx, inputs):
+    """pgx_pairs_with_lists (the reference BOINC pair mode's selection, src/main_phygas_boinc.cpp:445-447): a target
+    with a "clusters=" list gets exactly the listed clusters in cluster order, the others the prefilter's pairs, all
+    in target order."""
+    clusters, targets = inputs
+    tg = targets[:4]
+    names = ",".join(clusters[i].name.decode() for i in (4000, 12, 733))
+    lists = [None, names, "", "no_such_cluster"]
+    ti, ci = ctx.pairs_with_lists(tg, lists, clusters)
+    pti, pci = pg.prefilter_pairs([tg[0], tg[2]], clusters)
+    want = [(0, int(c)) for t, c in zip(pti, pci) if t == 0] + [(1, 12), (1, 733), (1, 4000)] \
+        + [(2, int(c)) for t, c in zip(pti, pci) if t == 1]
+    assert list(zip(ti.tolist(), ci.tolist())) == want

@@ -287,3 +287,15 @@ def test_serving_stream_plan(built, golden):
             assert j["n"] == 1
         else:
             assert min(1000, n_stars) <= j["n"] <= min(20000, n_stars) and j["first"] + j["n"] <= n_stars
+
+
+def test_cluster_list_matches_whole_items(golden):
+    """pgx_cluster_list (the stage-2 "clusters=" list, src/main_phygas_boinc.cpp:309-333): whole comma-separated
+    items only, results in cluster order whatever the list's order, unknown names ignored."""
+    clusters = pg.read_clusters(golden["clusters"])
+    names = [clusters[i].name.decode() for i in (300, 5, 17)]
+    assert pg.cluster_list(clusters, ",".join(names)).tolist() == [5, 17, 300]
+    n5 = clusters[5].name.decode()
+    assert pg.cluster_list(clusters, "x" + n5 + ",y" + n5 + "z," + n5 + "q").tolist() == []
+    assert pg.cluster_list(clusters, "no_such_cluster," + n5).tolist() == [5]
+    assert pg.cluster_list(clusters, "").tolist() == []

@@ -46,8 +46,9 @@ FP64_INSTR_PER_BODY_STEP = 36.0 + 3.0 + 29.0
 FLOPS_PER_CLONE_STEP = 214.9
 FP64_INSTR_PER_CLONE_STEP = 73.3 + 9.3 + 58.9
 # DRAM traffic of one k_stm_orbits launch on this chunk (dram__bytes_read.sum + dram__bytes_write.sum from one ncu
-# capture of `python -m phygas_gb300.run_screen --stars 20000`): 4.9 MB read + 711.8 MB of orbit output written
-ORBIT_TRAFFIC_BYTES = 716.7e6
+# capture of `python -m phygas_gb300.run_screen --stars 20000 --parts 1`): 6.7 MB read + 711.9 MB of orbit output
+# written
+ORBIT_TRAFFIC_BYTES = 718.6e6
 
 
 def log(*a):

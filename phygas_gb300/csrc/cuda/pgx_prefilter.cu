@@ -190,6 +190,8 @@ int prefilter_pairs(cudaStream_t st, PrefilterState &P, const PhTarget *t, int n
 
     // the cluster side, unless these clusters are the ones held; the host draws first, then the device work in one
     // stretch of the stream (timed by the events)
+    // the digest covers the records' bytes, padding included: records equal in every field but not in their padding
+    // only cost a retrace, never a wrong reuse (short of a 64-bit FNV collision)
     const uint64_t digest = fnv_bytes(fnv_bytes(14695981039346656037ULL, &nc, sizeof nc), c, sizeof(PhCluster) * nc);
     const bool fresh = !(P.nc == nc && P.digest == digest && P.c_pos.p);
     std::vector<double> cps, csig, r0;

@@ -457,7 +457,7 @@ def main():
     with Clocks(local) as clk:
         per, stats, n_rows = run(precision, args.steps, args.warmup)
     rows_mixed = ctx.fetch(n_rows)
-    # the plain FP64 comparator: the chunk whole, every stage in turn (no halves, no overlap); its orbit launch is
+    # the plain FP64 comparator: the chunk whole, every stage in turn (no parts, no overlap); its orbit launch is
     # also the roofline's (the whole chunk on the whole GPU)
     ctx.set_split(0)
     ctx.stage(ps0, sig, pre)

@@ -207,8 +207,8 @@ typedef struct {
     long ambiguous;                  /* mixed screen: pairs that may be kept (candidates) whose candidate points
                                         were found by a second walk; rechecked_points = points evaluated in FP64 */
     int kernels;                     /* kernel launches of the call */
-    long orbit_body_steps;           /* body steps of the orbit launch that ms_orbit times (a chunk screened in two
-                                        halves times the first half's; the second's runs beside the first's screen) */
+    long orbit_body_steps;           /* body steps of the orbit launch that ms_orbit times (a chunk screened in parts
+                                        times the first part's; the others run beside the previous part's screen) */
     double ms_prefilter;             /* pgx_prefilter: device time of the tracks and the pair tests */
     long prefilter_pairs, prefilter_rechecked;   /* pairs tested; pairs within the margin, decided on the host */
 } PgxStats;

@@ -49,6 +49,11 @@ FP64_INSTR_PER_CLONE_STEP = 73.3 + 9.3 + 58.9
 # capture of `python -m phygas_gb300.run_screen --stars 20000 --parts 1`): 6.7 MB read + 711.9 MB of orbit output
 # written
 ORBIT_TRAFFIC_BYTES = 718.6e6
+# warp instructions the FP32 filter (k_mx_scan32) issues for this chunk, 4.10e10 (smsp__inst_executed.sum of the same
+# capture; the parts of a split chunk issue the same work between them); its bound is the issue slots, 4 warp
+# instructions per clock per SM (one per scheduler)
+SCAN_WARP_INSTR = 4.10e10
+ISSUE_PER_CLK_SM = 4
 
 
 def log(*a):
@@ -376,6 +381,23 @@ def reference_arm(args):
                           "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def scan_roofline(stats, clocks):
+    """The step's largest kernel, k_mx_scan32, against its bound: warp instructions issued per second over the issue
+    rate of every SM at the SM clock sampled during the timed steps."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    ms = statistics.mean(x["ms_scan"] for x in stats)
+    if not mhz or not ms:
+        return None
+    achieved = SCAN_WARP_INSTR / (ms * 1e-3)
+    peak = ISSUE_PER_CLK_SM * sms * mhz * 1e6
+    return {"bound": "issue", "kernel": "k_mx_scan32", "achieved": achieved, "peak": peak,
+            "unit": "warp instructions/s", "frac": achieved / peak, "ms_per_step": ms,
+            "note": "instructions from one ncu capture of the chunk; time = the step's scan launches (its parts run "
+                    "beside the next part's orbits, which take issue slots too)"}
+
+
 def config(args):
     return {"workload": "screen: %d stars x %d clusters (synthetic, seed %d), chi2_max %g, n_samp %d, r_kernel %g"
                         % (N_STARS, N_CLUSTERS, SEED, CHI2_MAX, N_SAMP, R_KERNEL),
@@ -572,6 +594,7 @@ def main():
                          "fp64_instr_note": "FP64 instructions issued / the FMA instruction rate: DADD and DMUL take "
                                             "a full slot for one flop, so the flop fraction understates how busy the "
                                             "pipe is"},
+            "roofline_scan": scan_roofline(stats, clk.summary()),
             "fp32_peak_tflops": fp32_peak / 1e12,
             "cluster_table_s": table_s,
             "gpu_launches": int(sum(x["kernels"] for x in stats)),

@@ -299,3 +299,41 @@ def test_cluster_list_matches_whole_items(golden):
     assert pg.cluster_list(clusters, "x" + n5 + ",y" + n5 + "z," + n5 + "q").tolist() == []
     assert pg.cluster_list(clusters, "no_such_cluster," + n5).tolist() == [5]
     assert pg.cluster_list(clusters, "").tolist() == []
+
+
+def test_readers_on_awkward_lines(both, tmp_path):
+    """ph_read_clusters / ph_read_targets (reference src/phygas.c:462-506) on lines the reference skips or splits: a
+    header, comments, blank and short lines, non-numbers, `nan` fields, trailing tokens (a stage-2 "clusters=" list),
+    a line longer than its 1,024-byte buffer, no final newline; and a missing file (-1).  Same counts and records as
+    the oracle's readers."""
+    P, O = both
+    cl = ["0 SYN_A m 218.2 -63.4 1016.5 30.5 -2.52 0.05 -0.59 0.05 1.019 3.987 3.2 8.3 54 90 135 100",
+          "# a comment", "", "   ", "1 SHORT o 1 2 3",
+          "2 SYN_B o 174.7 -64.8 1068.3 32.0 5.35 0.07 2.48 0.07 nan nan 7.3 16.7 2.3 3.8 5.7 5.7",
+          "3 SYN_C o 174.7 -64.8 1068.3 32.0 5.35 0.07 2.48 0.07 nan 4.0 7.3 16.7 2.3 3.8 5.7 5.7 extra tokens",
+          "4 SYN_D o x -64.8 1068.3 32.0 5.35 0.07 2.48 0.07 1 2 7.3 16.7 2.3 3.8 5.7 5.7",
+          "5 SYN_E o 1 2 3 4 5 6 7 8 9 10 11 12 13 14 15 16 " + "9" * 1100,
+          "6 SYN_LAST o 10 -5 500 5 1 0.1 2 0.1 -3.2 1.1 2 6 10 20 30 30"]
+    tg = ["PHYGAS 1 pair 100 0.05",
+          "JSYN0 P 104.8 4.06 0.0 0.0 1633.2 0.25 -20.37 0.32 -38.25 0.32 nan nan 79.95",
+          "STAR1 S 10.0 -5.0 2.5 0.2 0.0 0.0 1.0 0.1 -2.0 0.1 12.0 1.5 clusters=SYN_A,SYN_B",
+          "# STAR2 S 10 -5 2.5 0.2 0 0 1 0.1 -2 0.1 12 1.5", "STAR3 S 10 -5 2.5",
+          "STAR4 S 10.0 -5.0 2.5 0.2 0.0 0.0 1.0 0.1 -2.0 0.1 nan 1.5",
+          "X" * 1030 + " S 1 2 3 4 5 6 7 8 9 10 11 12",
+          "STAR5 S 11.0 -6.0 2.0 0.2 0.0 0.0 1.0 0.1 -2.0 0.1 12.0 1.5"]
+    for lines, T, fn in ((cl, pg.PhCluster, "ph_read_clusters"), (tg, pg.PhTarget, "ph_read_targets")):
+        path = tmp_path / (fn + ".txt")
+        path.write_text("\n".join(lines))                 # no final newline
+        pa, pb = C.POINTER(T)(), C.POINTER(T)()
+        getattr(P, fn).argtypes = getattr(O, fn).argtypes = [C.c_char_p, C.POINTER(C.POINTER(T))]
+        na = getattr(P, fn)(str(path).encode(), C.byref(pa))
+        nb = getattr(O, fn)(str(path).encode(), C.byref(pb))
+        assert na == nb >= 3, (fn, na, nb)
+        for i in range(na):
+            for f, ft in T._fields_:
+                va, vb = getattr(pa[i], f), getattr(pb[i], f)
+                if ft is C.c_double:
+                    va, vb = np.float64(va).tobytes(), np.float64(vb).tobytes()
+                assert va == vb, (fn, i, f)
+        missing = str(tmp_path / "no_such_file.txt").encode()
+        assert getattr(P, fn)(missing, C.byref(pa)) == getattr(O, fn)(missing, C.byref(pb)) == -1

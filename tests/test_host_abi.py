@@ -337,3 +337,44 @@ def test_readers_on_awkward_lines(both, tmp_path):
                 assert va == vb, (fn, i, f)
         missing = str(tmp_path / "no_such_file.txt").encode()
         assert getattr(P, fn)(missing, C.byref(pa)) == getattr(O, fn)(missing, C.byref(pb)) == -1
+
+
+def test_track_starts_identical(both, golden):
+    """pgh_track_starts (the host half of the GPU prefilter: each object's nominal start and its 32-draw spread) gives
+    the oracle's ph_sample_* nominal point and ph_track_* sig_pos / sig_vel, bit for bit, for targets and clusters."""
+    P, O = both
+
+    class Track(C.Structure):
+        _fields_ = [("n", C.c_int), ("pos", C.POINTER(C.c_double)), ("sig_pos", C.c_double),
+                    ("sig_vel", C.c_double)]
+
+    class PhaseSpace(C.Structure):
+        _fields_ = [("pos", C.c_double * 3), ("vel", C.c_double * 3)]
+
+    clusters = pg.read_clusters(golden["clusters"])[:200]
+    targets = list(pg.read_targets(golden["pulsar"])[:3]) + list(pg.read_targets(golden["screen"])[:20])
+    P.pgh_track_starts.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double)]
+    O.ph_track_target.argtypes = [C.POINTER(pg.PhTarget), C.c_double, C.c_int, C.c_uint64, C.POINTER(Track)]
+    O.ph_track_cluster.argtypes = [C.POINTER(pg.PhCluster), C.c_int, C.c_uint64, C.POINTER(Track)]
+    O.ph_sample_target.argtypes = [C.POINTER(pg.PhTarget), C.c_void_p, C.POINTER(PhaseSpace)]
+    O.ph_sample_cluster.argtypes = [C.POINTER(pg.PhCluster), C.c_void_p, C.POINTER(PhaseSpace)]
+    O.ph_seed.restype = C.c_uint64
+    O.ph_seed.argtypes = [C.c_char_p, C.c_char_p]
+    tmax = max(c.tmax_myr for c in clusters)
+    for objs, is_t in ((targets, True), (clusters, False)):
+        arr = pg.as_array(objs, pg.PhTarget if is_t else pg.PhCluster)
+        ps, sig = np.zeros(6 * len(objs)), np.zeros(2 * len(objs))
+        P.pgh_track_starts(C.cast(arr, C.c_void_p) if is_t else None, None if is_t else C.cast(arr, C.c_void_p),
+                           len(objs), 4, pg._ptr(ps), pg._ptr(sig))
+        for i, o in enumerate(objs):
+            nom, t = PhaseSpace(), Track()
+            if is_t:
+                O.ph_sample_target(C.byref(o), None, C.byref(nom))
+                O.ph_track_target(C.byref(o), tmax, 32, O.ph_seed(b"track", o.id), C.byref(t))
+            else:
+                O.ph_sample_cluster(C.byref(o), None, C.byref(nom))
+                O.ph_track_cluster(C.byref(o), 32, O.ph_seed(b"track", o.name), C.byref(t))
+            want = np.array(list(nom.pos) + list(nom.vel))
+            assert ps[6 * i:6 * i + 6].tobytes() == want.tobytes(), (is_t, i)
+            assert sig[2 * i:2 * i + 2].tobytes() == np.array([t.sig_pos, t.sig_vel]).tobytes(), (is_t, i)

@@ -134,7 +134,8 @@ int pgx_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhC
  * (at most cap written to ti/ci, *n = how many pass).  The host draws the tracks' starts and spreads on `threads`
  * threads (0 = all cores); the GPU traces the coarse tracks and tests the pairs; the cluster tracks stay in the
  * context for the next call with the same clusters.  A pair the GPU cannot decide with the margin to spare is decided
- * by the host code.  pgx_stats: ms_prefilter (device time), prefilter_pairs, prefilter_rechecked, body_steps. */
+ * by the host code.  Every cluster's tmax_myr must lie in [0, 1e5] (PGX_E_ARG otherwise).  pgx_stats: ms_prefilter
+ * (device time), prefilter_pairs, prefilter_rechecked, body_steps. */
 int pgx_prefilter(PgxContext *ctx, const PhTarget *t, int nt, const PhCluster *c, int nc, int threads, int *ti,
                   int *ci, long cap, long *n);
 /* The distance (kpc, >= 0) the GPU's prefilter decisions keep from the threshold, a bound on how far a GPU-traced

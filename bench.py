@@ -7,20 +7,33 @@ FP64 orbits + STM covariances of the 20,000 stars, the scan of all 81.7 M pairs,
 every kept pair, with the cluster table resident (built once, outside the timed region, as a serving process keeps
 it).
 
-  value     pairs/s of the mixed-precision screen, device time per chunk (CUDA events on the library's stream),
-            star inputs (nominal state + covariance of the draws) already in HBM; L2 flushed between steps
-  e2e       the same metric through the C-ABI call a user makes (pgx_draw_targets + pgx_screen): host star records
-            in, host rows out, host draws and host<->device copies inside the timed region
-  plain_fp64  the plain FP64 screen on the same chunk (the comparison the target is stated against)
-  roofline  the dominant kernel (the FP64 orbit integration): FP64 FLOP/s against the FP64 FMA peak measured in
-            this run by the library's probe kernel
-  cpu_baseline  the oracle (a pinned C restatement of the reference's CPU code) on all host cores, bounded sample
+  value         pairs/s of the mixed-precision screen, device time per chunk (CUDA events on the library's stream),
+                star inputs (nominal state + covariance of the draws) already in HBM; L2 flushed between steps
+  e2e           the same metric through the C-ABI call a user makes (pgx_screen_chunks): host star records in, host
+                rows out, host draws and host<->device copies inside the timed region
+  roofline      the step's largest kernel, the FP32 filter k_mx_scan32: the survey's 126 flops per pair-point over
+                its CUDA-event launch time, against the FP32 FMA peak measured in this run by the library's probe
+  cpu_baseline  the oracle (a pinned C restatement of the reference's CPU code) on all host cores, bounded sample;
+                its rows are kept and compared with the GPU's rows of the same stars (parity_vs_oracle)
+  plain_fp64    the plain FP64 screen on the same chunk (the comparison the target is stated against)
+The line ends with the evidence a reader checks first: the speed-up over the plain FP64 path, the mixed rows against
+the FP64 rows, and the GPU rows against the oracle's on the sampled stars.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun (N > 1) every rank screens its own chunk (weak scaling, no data exchange); rank 0 prints.
+
+Profiling modes (one JSON line each; nothing else runs on the GPU, so a profiler sees only their launches):
+  python bench.py --mode screen [--stars 20000] [--clusters N] [--precision mixed|fp64] [--parts K] [--repeat R]
+      one screen of a synthetic chunk (the cluster-table orbit launch first, then the screen's launches in order)
+  python bench.py --mode pairs [--stars 2000] [--pairs 200] [--pulsars 1] [--streamed]
+      one batch of the pair Monte Carlo: --pairs kept screen pairs (p_r50 >= 0.001, evenly spaced) plus --pulsars
+      synthetic pulsars against their prefiltered clusters, clones U{200,500,1000} at dt 0.05 Myr; with --streamed the
+      pulsars' pairs come from the GPU prefilter and the whole list runs through pgx_pair_targets, timed end to end
+      (--stars 20000 --pairs 10000 --pulsars 702 --streamed is the full batched uneven Monte Carlo configuration)
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -33,31 +46,41 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 N_STARS, N_CLUSTERS, SEED = 20000, 4087, 1001
-CHI2_MAX, N_SAMP, R_KERNEL = 25.0, 64, 2.0
+CHI2_MAX, N_SAMP, R_KERNEL, P_MIN = 25.0, 64, 2.0, 0.001
+# the survey's algorithmic count for one pair-point of the screen (one track point of one star-cluster pair): 9 to
+# build M, 6 for m0/m1, 44 per quad_inv x 2, 19 for the segment's nearest point and the interpolation
+FLOPS_PER_PAIR_POINT = 126.0
 # FP64 flops of one body step (one kick-drift-kick step of one orbit, its force evaluation included), from the
-# executed FP64 instructions of k_stm_orbits per body step: 36.0 DFMA + 3.0 DADD + 29.0 DMUL (ncu sass op counters of
-# the 2,000-star screen of `python -m phygas_gb300.run_pairs`, FMA = 2 flops)
+# executed FP64 instructions of k_stm_orbits per body step: 36.0 DFMA + 3.0 DADD + 29.0 DMUL (ncu sass op counters,
+# FMA = 2 flops)
 FLOPS_PER_BODY_STEP = 104.0
-# the same count as FP64 instructions (each takes one FP64-pipe slot, whatever its flops)
 FP64_INSTR_PER_BODY_STEP = 36.0 + 3.0 + 29.0
 # the same for one clone-step of the pair Monte Carlo (two body steps, and the FP64 segment test where the FP32 bound
-# does not rule it out), from k_pair_mc_t on the batch of `python -m phygas_gb300.run_pairs` (4,052 pairs, 1.49e9
-# clone-steps): 73.3 DFMA + 9.3 DADD + 58.9 DMUL executed
+# does not rule it out), from k_pair_mc_t on the 4,052-pair batch of `bench.py --mode pairs` (200 screen pairs of
+# 2,000 stars + 1 pulsar x 3,852 prefiltered clusters): 73.3 DFMA + 9.3 DADD + 58.9 DMUL executed
 FLOPS_PER_CLONE_STEP = 214.9
 FP64_INSTR_PER_CLONE_STEP = 73.3 + 9.3 + 58.9
-# DRAM traffic of one k_stm_orbits launch on this chunk (dram__bytes_read.sum + dram__bytes_write.sum from one ncu
-# capture of `python -m phygas_gb300.run_screen --stars 20000 --parts 1`): 6.7 MB read + 711.9 MB of orbit output
-# written
+# DRAM traffic of one k_stm_orbits launch on the whole chunk (dram__bytes_read.sum + dram__bytes_write.sum, one ncu
+# capture of `bench.py --mode screen --stars 20000 --parts 1`): 6.7 MB read + 711.9 MB of orbit output written
 ORBIT_TRAFFIC_BYTES = 718.6e6
-# warp instructions the FP32 filter (k_mx_scan32) issues for this chunk, 4.10e10 (smsp__inst_executed.sum of the same
-# capture; the parts of a split chunk issue the same work between them); its bound is the issue slots, 4 warp
-# instructions per clock per SM (one per scheduler)
-SCAN_WARP_INSTR = 4.10e10
+# DRAM traffic of k_mx_scan32 per pair-point (read + write of one ncu capture of the same command, whole-chunk
+# launch: 1,067 MB for 4.99e9 pair-points); a part's launch moves its share
+SCAN_TRAFFIC_PER_PAIR_POINT = 1067e6 / 4.99e9
+# warp instructions k_mx_scan32 issues per pair-point (smsp__inst_executed.sum of the same capture, 4.10e10 for the
+# chunk); its issue bound is 4 warp instructions per clock per SM (one per scheduler)
+SCAN_WARP_INSTR_PER_PAIR_POINT = 4.10e10 / 4.99e9
 ISSUE_PER_CLK_SM = 4
 
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
+
+
+def r4(x):
+    """x to 4 significant digits (the compact evidence at the end of the line)."""
+    if isinstance(x, float) and x != 0 and math.isfinite(x):
+        return float("%.4g" % x)
+    return x
 
 
 def dist_env():
@@ -119,9 +142,18 @@ def make_inputs(tmp, rank):
     return cp, tp
 
 
-def cpu_baseline(cp, tp, stars_per_proc=192, procs=None):
+def pair_points(clusters, n_stars, tmax):
+    """Pair-points of a chunk: per star-cluster pair, the points both tracks have (the scan's loop count)."""
+    npts_star = int(math.ceil(tmax / 0.5)) + 1
+    return n_stars * sum(min(npts_star, int(math.ceil(c.tmax_myr / 0.5)) + 1) for c in clusters)
+
+
+def cpu_baseline(cp, tp, stars_per_proc=192, procs=None, keep_rows=False):
     """Oracle screen on all host cores: P processes, each `stars_per_proc` stars x all clusters; pairs/s from the
-    per-target loop time (the per-cluster precompute, done once per task by the reference, is timed apart)."""
+    per-target loop time (the per-cluster precompute, done once per task by the reference, is timed apart).
+    keep_rows: the processes write their kept pairs as raw records, returned (stars [0, P * stars_per_proc))."""
+    import numpy as np
+    import phygas_gb300 as pg
     from tests import oracle_tools as ot
     procs = procs or os.cpu_count() or 1
     with open(tp) as f:
@@ -131,37 +163,84 @@ def cpu_baseline(cp, tp, stars_per_proc=192, procs=None):
     with open(inp, "w") as f:
         f.write("PHYGAS 1 screen %g %d %g 0\n" % (CHI2_MAX, N_SAMP, R_KERNEL))
         f.writelines(stars[:stars_per_proc * procs])
+    env = dict(os.environ)
+    if keep_rows:
+        env["PHYGAS_WU_RAW"] = "1"
     t0 = time.time()
     ps = [subprocess.Popen([ot.ORACLE_WU, cp, inp, str(p * stars_per_proc), str((p + 1) * stars_per_proc)],
-                           stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True) for p in range(procs)]
-    runs, preps = [], []
+                           stdout=subprocess.PIPE if keep_rows else subprocess.DEVNULL, stderr=subprocess.PIPE,
+                           env=env) for p in range(procs)]
+    runs, preps, outs = [], [], []
     for p in ps:
-        err = p.communicate()[1]
+        out, err = p.communicate()
+        err = err.decode(errors="replace")
         if p.returncode:
             raise RuntimeError("oracle_wu failed: " + err[-500:])
         f = err.split("wu_time")[-1].split()
         preps.append(float(f[1]))
         runs.append(float(f[3]))
+        if keep_rows:
+            outs.append(out)
     wall = time.time() - t0
     pairs = stars_per_proc * procs * N_CLUSTERS
-    return {"value": pairs / max(runs), "unit": "pairs/s", "cores": procs, "kind": "port",
-            "sample": "%d stars x %d clusters on %d processes (%d stars each); per-target loop %.1f s, cluster "
-                      "precompute %.1f s per process (excluded), wall %.1f s" % (
-                          stars_per_proc * procs, N_CLUSTERS, procs, stars_per_proc, max(runs), max(preps), wall)}
+    res = {"value": pairs / max(runs), "unit": "pairs/s", "cores": procs, "kind": "port",
+           "sample": "%d stars x %d clusters on %d processes (%d stars each); per-target loop %.1f s, cluster "
+                     "precompute %.1f s per process (excluded), wall %.1f s" % (
+                         stars_per_proc * procs, N_CLUSTERS, procs, stars_per_proc, max(runs), max(preps), wall),
+           "loop_s": max(runs), "pairs": pairs}
+    rows = np.frombuffer(b"".join(outs), pg.ROW_DTYPE) if keep_rows else None
+    return res, rows
+
+
+def compare_to_oracle(gpu, ora, n_stars, cut=CHI2_MAX, p_cut=P_MIN):
+    """The GPU's rows of stars [0, n_stars) against the oracle's (the reference's CPU algorithm) on the same stars:
+    the kept pair sets (chi2 < cut; pairs within 1e-6 relative of the cut in either are exempt), the emitted sets
+    (p_r50 >= p_cut; exempt within 1e-6 of it), and over the pairs both keep: the largest and 99th-percentile
+    relative error of chi2, t, d_nom, sig and vrel, the largest p_r50 / p_rtot difference and how many differ."""
+    import numpy as np
+    gpu = gpu[gpu["star"] < n_stars]
+    key = lambda r: r["star"].astype(np.int64) * (1 << 32) + r["cluster"]
+    kg, ko = key(gpu), key(ora)
+    near = lambda r: np.abs(r["chi2"] - cut) <= 1e-6 * cut
+    only_g = np.setdiff1d(kg, ko)
+    only_o = np.setdiff1d(ko, kg)
+    exempt = set(kg[near(gpu)].tolist()) | set(ko[near(ora)].tolist())
+    bad_sets = [k for k in np.concatenate([only_g, only_o]).tolist() if k not in exempt]
+    both, ig, io = np.intersect1d(kg, ko, assume_unique=True, return_indices=True)
+    a, b = gpu[ig], ora[io]
+    em_g = set(kg[gpu["p_r50"] >= p_cut].tolist())
+    em_o = set(ko[ora["p_r50"] >= p_cut].tolist())
+    near_p = set(kg[np.abs(gpu["p_r50"] - p_cut) <= 1e-6].tolist()) | set(ko[np.abs(ora["p_r50"] - p_cut) <= 1e-6]
+                                                                          .tolist())
+    em_bad = [k for k in (em_g ^ em_o) if k not in near_p]
+
+    def rel(f):
+        x = np.abs(a[f] - b[f]) / np.maximum(np.abs(b[f]), 1e-300)
+        return {"max": r4(float(x.max())) if len(x) else 0.0,
+                "p99": r4(float(np.quantile(x, 0.99))) if len(x) else 0.0}
+    dp50, dpt = np.abs(a["p_r50"] - b["p_r50"]), np.abs(a["p_rtot"] - b["p_rtot"])
+    return {"stars": int(n_stars), "rows_gpu": int(len(gpu)), "rows_oracle": int(len(ora)),
+            "kept_set_mismatches": len(bad_sets), "emitted_gpu": len(em_g), "emitted_oracle": len(em_o),
+            "emitted_set_mismatches": len(em_bad), "argmin_point_differs": int(np.sum(a["kb"] != b["kb"])),
+            "chi2_rel": rel("chi2"), "t_rel": rel("t_myr"), "d_nom_rel": rel("d_nom_pc"), "sig_rel": rel("sig_pc"),
+            "vrel_rel": rel("vrel_kms"),
+            "p_r50_abs_max": r4(float(dp50.max())) if len(dp50) else 0.0, "p_r50_differ": int(np.sum(dp50 > 0)),
+            "p_rtot_abs_max": r4(float(dpt.max())) if len(dpt) else 0.0, "p_rtot_differ": int(np.sum(dpt > 0)),
+            "contract": "sets identical except within 1e-6 of a cut; d, t within 1e-6 rel; p within 1e-4 abs"}
 
 
 # Batched uneven Monte Carlo (the north star's C3 shape, scaled to a benchmark step): C3_SCREEN_PAIRS pairs from the
 # mixed screen's rows with p_r50 >= 0.001, plus C3_PULSARS synthetic pulsars x their prefiltered clusters; clone
 # counts uniform in {200, 500, 1000}; steps = ceil(tmax / 0.05 Myr).  A synthetic pulsar (pm error 1 mas/yr, no
-# parallax) reaches ~96 % of the 4,087 clusters, so the 702 pulsars of the full configuration are ~1e12 clone-steps;
-# two stand in for them here.
+# parallax) reaches ~96 % of the 4,087 clusters, so the 702 pulsars of the full configuration are ~1e12 clone-steps
+# (about 5 minutes: `bench.py --mode pairs --stars 20000 --pairs 10000 --pulsars 702 --streamed`); two stand in for
+# them here.
 C3_SCREEN_PAIRS, C3_PULSARS, C3_SEED = 10000, 2, 1003
 
 
 def pair_cpu_baseline(cp, pp, n_clones=200, clusters_per_proc=24, procs=None):
     """Oracle pair Monte Carlo on all host cores: process p traces pulsar 0 against clusters
     [p * k, (p + 1) * k) (prefiltered, n_clones clones each); clone-steps/s from the slowest process's loop time."""
-    import math
     from tests import oracle_tools as ot
     import phygas_gb300 as pg
     procs = procs or os.cpu_count() or 1
@@ -193,7 +272,7 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
     import numpy as np
     import phygas_gb300 as pg
     from phygas_gb300 import synth
-    sel = np.flatnonzero(rows["p_r50"] >= 0.001)
+    sel = np.flatnonzero(rows["p_r50"] >= P_MIN)
     take = sel[np.unique(np.linspace(0, len(sel) - 1, min(C3_SCREEN_PAIRS, len(sel))).astype(np.int64))]
     tmp = tempfile.mkdtemp(prefix="phygas_c3_")
     pp = os.path.join(tmp, "pulsars.txt")
@@ -239,24 +318,21 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
         t0 = time.perf_counter()
         ctx.pair_targets(targets_arr, ti, clusters, ci, ncl, 0.05)
         e2e_walls.append(time.perf_counter() - t0)
-    out = {"metric": "clone-steps/s", "value": cs / (statistics.mean(ms) * 1e-3), "unit": "clone-steps/s",
-           "ms_per_batch": statistics.mean(ms),
+    rate = cs / (statistics.mean(ms) * 1e-3)
+    out = {"metric": "clone-steps/s", "value": rate, "unit": "clone-steps/s", "ms_per_batch": statistics.mean(ms),
            "workload": "%d screen pairs (p_r50 >= 0.001) + %d pulsars x %d prefiltered clusters; clones U{200,500,1000}, "
                        "dt 0.05 Myr" % (len(take), C3_PULSARS, len(pti)),
            "pairs": int(len(ti)), "clones": int(st["clones"]), "clone_steps": int(cs),
            "launch": "one captured CUDA graph (prep, persistent trace, reduce) per shape, replayed per batch",
-           "roofline": {"bound": "fp64", "kernel": "k_pair_mc_t",
-                        "achieved": FLOPS_PER_CLONE_STEP * cs / (statistics.mean(ms) * 1e-3) / 1e12,
-                        "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
-                        "frac": FLOPS_PER_CLONE_STEP * cs / (statistics.mean(ms) * 1e-3) / fp64_peak,
+           "roofline": {"bound": "fp64", "kernel": "k_pair_mc_t", "achieved": FLOPS_PER_CLONE_STEP * rate / 1e12,
+                        "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": FLOPS_PER_CLONE_STEP * rate / fp64_peak,
                         "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
                         "flops_per_clone_step": FLOPS_PER_CLONE_STEP,
-                        "fp64_instr_frac": FP64_INSTR_PER_CLONE_STEP * cs / (statistics.mean(ms) * 1e-3)
-                                           / (fp64_peak / 2)},
+                        "fp64_instr_frac": FP64_INSTR_PER_CLONE_STEP * rate / (fp64_peak / 2)},
            "autotune": {"chosen": {"warps_per_block": table[best][0], "clones_per_lane": table[best][1],
                                    "min_blocks_per_sm": table[best][2]},
-                        "ms_on_sample": [{"warps_per_block": w, "clones_per_lane": c, "min_blocks_per_sm": b, "ms": t}
-                                         for w, c, b, t in table]},
+                        "ms_on_sample": [{"warps_per_block": w, "clones_per_lane": c, "min_blocks_per_sm": b,
+                                          "ms": r4(t)} for w, c, b, t in table]},
            "e2e": {"value": cs / min(e2e_walls), "unit": "clone-steps/s", "s_per_step": min(e2e_walls),
                    "how": "pgx_pair_targets: host clone draws of each batch of 1,024 pairs overlap the GPU's tracing "
                           "of the one before (page-locked buffers)",
@@ -276,16 +352,17 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
     return out
 
 
-# Serving (the benchmark spec's C4 shape): SERVE_JOBS jobs of a seeded Poisson stream at SERVE_RATE_HZ through the
-# request loop with SERVE_SLOTS slots -- screen and control chunks of 1,000-20,000 of the benchmark stars and
-# single-pulsar Monte Carlo jobs (4,087 clusters with the prefilter, 1000 clones) -- once with the mixed screen and
-# once with the plain FP64 screen, the same stream both times.
-SERVE_JOBS, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 20, 1.0, 3, 1004
+# Serving (the benchmark spec's C4 shape): a seeded Poisson stream through the request loop with SERVE_SLOTS slots --
+# screen and control chunks of 1,000-20,000 of the benchmark stars and single-pulsar Monte Carlo jobs (4,087
+# clusters with the prefilter, 1000 clones).  SERVE_JOBS jobs with the mixed screen, so that the 99th percentile is
+# one; the first SERVE_JOBS_FP64 of the same stream again with the plain FP64 screen (whose screen jobs are ~35x
+# longer) for the comparison.
+SERVE_JOBS, SERVE_JOBS_FP64, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 200, 40, 8.0, 3, 1004
 # chunks of the benchmark's stars per end-to-end run (the pipeline's fill is spread over them)
 E2E_CHUNKS = 8
 
 
-def compare_rows(mixed, fp64, cut=0.001):
+def compare_rows(mixed, fp64, cut=P_MIN):
     """The mixed-precision rows against the FP64 path's on the same chunk: pair sets (all kept pairs, and those with
     p_r50 >= cut), and the largest and 99th-percentile differences of d_min (relative), t_min (relative), p_r50 and
     p_rtot (absolute) over the pairs both keep."""
@@ -298,7 +375,7 @@ def compare_rows(mixed, fp64, cut=0.001):
 
     def stat(x):
         x = np.abs(x)
-        return {"max": float(x.max()) if len(x) else 0.0, "p99": float(np.quantile(x, 0.99)) if len(x) else 0.0}
+        return {"max": r4(float(x.max())) if len(x) else 0.0, "p99": r4(float(np.quantile(x, 0.99))) if len(x) else 0.0}
     rel = lambda u, v: (u - v) / np.where(v != 0, np.abs(v), 1.0)
     return {"rows_mixed": int(len(mixed)), "rows_fp64": int(len(fp64)), "rows_both": int(len(both)),
             "emitted_mixed": len(em), "emitted_fp64": len(ef), "emitted_differ": len(em ^ ef),
@@ -335,11 +412,12 @@ def serving_measure(cp, tp):
     pp = os.path.join(tempfile.mkdtemp(prefix="phygas_serve_"), "pulsars.txt")
     with open(pp, "w") as f:
         f.write("\n".join(synth.pulsars(64, SERVE_SEED)) + "\n")
-    out = {"workload": "%d jobs, Poisson %.2f/s (seed %d): 40 %% screen, 20 %% control chunks of 1,000-20,000 stars, "
-                       "40 %% single-pulsar jobs (prefilter, 1000 clones); %d slots"
-                       % (SERVE_JOBS, SERVE_RATE_HZ, SERVE_SEED, SERVE_SLOTS)}
-    for prec in ("mixed", "fp64"):
-        r = subprocess.run([pg.SERVE_CLI, cp, tp, pp, str(SERVE_JOBS), str(SERVE_RATE_HZ), str(SERVE_SLOTS), prec,
+    out = {"workload": "Poisson %.2f/s (seed %d): 40 %% screen, 20 %% control chunks of 1,000-20,000 stars, 40 %% "
+                       "single-pulsar jobs (4,087 clusters, prefilter, 1000 clones); %d slots; %d jobs mixed, the "
+                       "first %d of the same stream with the FP64 screen"
+                       % (SERVE_RATE_HZ, SERVE_SEED, SERVE_SLOTS, SERVE_JOBS, SERVE_JOBS_FP64)}
+    for prec, jobs_n in (("mixed", SERVE_JOBS), ("fp64", SERVE_JOBS_FP64)):
+        r = subprocess.run([pg.SERVE_CLI, cp, tp, pp, str(jobs_n), str(SERVE_RATE_HZ), str(SERVE_SLOTS), prec,
                             str(SERVE_SEED)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
         lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
         summ = [x for x in lines if x.get("summary")]
@@ -348,7 +426,7 @@ def serving_measure(cp, tp):
             raise RuntimeError("phygas_serve %s failed: %s" % (prec, r.stderr[-400:]))
         s = dict(summ[0])
         s.pop("summary")
-        s["latency_by_kind_p50_s"] = {k: statistics.median([x["latency_s"] for x in jobs if x["kind"] == k] or [0.0])
+        s["latency_by_kind_p50_s"] = {k: r4(statistics.median([x["latency_s"] for x in jobs if x["kind"] == k] or [0.0]))
                                       for k in ("screen", "control", "pulsar")}
         s["jobs_by_kind"] = {k: sum(1 for x in jobs if x["kind"] == k) for k in ("screen", "control", "pulsar")}
         out[prec] = s
@@ -356,46 +434,56 @@ def serving_measure(cp, tp):
 
 
 def reference_arm(args):
+    """The reference's CPU screen (the oracle port: the reference's own binaries are not built on the GPU machine) on all
+    host cores, each step a bounded sample of the workload: ms_per_step is that sample's measured loop time and
+    pairs_per_step its pairs; the rate is pairs/s as for this build's arm."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from phygas_gb300 import build as B
-    B.build_oracle()
+    import __graft_entry__
+    __graft_entry__.build_oracle()
     with tempfile.TemporaryDirectory() as tmp:
         cp, tp = make_inputs(tmp, 0)
         vals = []
         for i in range(args.warmup + args.steps):
-            r = cpu_baseline(cp, tp, stars_per_proc=32)
+            r, _ = cpu_baseline(cp, tp, stars_per_proc=32)
             if i >= args.warmup:
                 vals.append(r)
         v = statistics.median(x["value"] for x in vals)
         base = dict(vals[-1])
         base["value"] = v
+        ms = statistics.median(x["loop_s"] for x in vals) * 1e3
         print(json.dumps({"impl": "reference", "metric": "pairs/s", "value": v, "unit": "pairs/s",
                           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                          "ms_per_step": N_STARS * N_CLUSTERS / v * 1e3,
-                          "ms_per_step_note": "the full %d x %d step at the sample's rate" % (N_STARS, N_CLUSTERS),
+                          "ms_per_step": ms, "pairs_per_step": vals[-1]["pairs"],
+                          "step": "one bounded sample: %s" % vals[-1]["sample"],
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                           "data": "synthetic", "config": config(args),
                           "cpu_baseline": base,
                           "e2e": {"value": v, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
-def scan_roofline(stats, clocks):
-    """The step's largest kernel, k_mx_scan32, against its bound: warp instructions issued per second over the issue
-    rate of every SM at the SM clock sampled during the timed steps."""
+def scan_roofline(stats, clocks, pp, fp32_peak, parts):
+    """The step's largest kernel, k_mx_scan32 (one launch per part), against the FP32 FMA peak: the survey's 126
+    flops per pair-point over the launches' CUDA-event time; with it the issue-slot fraction (the bound that
+    applies to its mix of FP32, integer and compare work) from the warp instructions per pair-point of an ncu
+    capture, at the SM clock sampled during the steps."""
     import torch
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
     ms = statistics.mean(x["ms_scan"] for x in stats)
-    if not mhz or not ms:
+    if not ms:
         return None
-    achieved = SCAN_WARP_INSTR / (ms * 1e-3)
-    peak = ISSUE_PER_CLK_SM * sms * mhz * 1e6
-    return {"bound": "issue", "kernel": "k_mx_scan32", "achieved": achieved, "peak": peak,
-            "unit": "warp instructions/s", "frac": achieved / peak, "ms_per_step": ms,
-            "note": "instructions from one ncu capture of the chunk; time = the step's scan launches (its parts run "
-                    "beside the next part's orbits, which take issue slots too)"}
+    flops = FLOPS_PER_PAIR_POINT * pp
+    out = {"bound": "fp32", "kernel": "k_mx_scan32", "achieved": flops / (ms * 1e-3) / 1e12,
+           "peak": fp32_peak / 1e12, "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / fp32_peak,
+           "peak_source": "FP32 FMA probe kernel of this run (pgx_peaks); not in MEASURED_PEAKS.json",
+           "traffic": SCAN_TRAFFIC_PER_PAIR_POINT * pp / parts,
+           "flops_per_pair_point": FLOPS_PER_PAIR_POINT, "pair_points_per_launch": pp / parts,
+           "launches_per_step": parts, "ms_per_launch": ms / parts}
+    if mhz:
+        out["issue_frac"] = SCAN_WARP_INSTR_PER_PAIR_POINT * pp / (ms * 1e-3) / (ISSUE_PER_CLK_SM * sms * mhz * 1e6)
+    return out
 
 
 def config(args):
@@ -407,21 +495,123 @@ def config(args):
                            else "single GPU"}
 
 
+def mode_screen(a):
+    """One screen of a synthetic chunk, for profiling: the cluster table first, then the screen `--repeat` times;
+    prints the row count and the last run's device stage times and work counts."""
+    import phygas_gb300 as pg
+    from phygas_gb300 import synth
+    import __graft_entry__
+    __graft_entry__.build()
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "screen", a.stars, a.seed or SEED, a.clusters)
+        clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    tmax = max(c.tmax_myr for c in clusters)
+    prec = pg.PGX_MIXED if a.precision == "mixed" else pg.PGX_FP64
+    with pg.Context(0) as ctx:
+        ctx.set_clusters(clusters)
+        if a.parts is not None:
+            ctx.set_split(0 if a.parts <= 1 else 8192, a.parts if a.parts >= 2 else None)
+        ps0, sig, pre = pg.draw_targets(stars)
+        ctx.stage(ps0, sig, pre)
+        rows = 0
+        for _ in range(a.repeat):
+            rows = ctx.exec(tmax, CHI2_MAX, prec)
+        print(json.dumps({"mode": "screen", "stars": len(stars), "clusters": len(clusters), "precision": a.precision,
+                          "parts": a.parts, "rows": rows, "pair_points": pair_points(clusters, len(stars), tmax),
+                          "stats": ctx.stats()}))
+
+
+def mode_pairs(a):
+    """One batch of the pair Monte Carlo, for profiling (k_pair_mc_t is the only launch of its name), or with
+    --streamed the whole list end to end through pgx_prefilter and pgx_pair_targets."""
+    import numpy as np
+    import phygas_gb300 as pg
+    from phygas_gb300 import synth
+    import __graft_entry__
+    __graft_entry__.build()
+    seed = a.seed or C3_SEED
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "screen", a.stars, seed)
+        clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+        pp = os.path.join(d, "pulsars.txt")
+        with open(pp, "w") as f:
+            f.write("\n".join(synth.pulsars(max(a.pulsars, 1), seed)) + "\n")
+        pulsars = pg.read_targets(pp)[:a.pulsars]
+    tmax = max(c.tmax_myr for c in clusters)
+    with pg.Context(0) as ctx:
+        ctx.set_clusters(clusters)
+        rows = ctx.screen(*pg.draw_targets(stars), tmax)
+        sel = np.flatnonzero(rows["p_r50"] >= P_MIN)
+        take = sel[np.unique(np.linspace(0, len(sel) - 1, min(a.pairs, len(sel))).astype(np.int64))] \
+            if len(sel) and a.pairs > 0 else sel[:0]
+        t0 = time.perf_counter()
+        if not len(pulsars):
+            pti, pci = (np.zeros(0, np.int32),) * 2
+        elif a.streamed:
+            pti, pci = ctx.prefilter(pulsars, clusters)
+        else:
+            pti, pci = pg.prefilter_pairs(pulsars, clusters)
+        pref_s = time.perf_counter() - t0
+        ti = np.concatenate([rows["star"][take], pti + len(stars)]).astype(np.int32)
+        ci = np.concatenate([rows["cluster"][take], pci]).astype(np.int32)
+        ncl = np.random.default_rng(seed).choice([200, 500, 1000], len(ti)).astype(np.int32)
+        if a.streamed:
+            targets = pg.as_array(list(stars) + list(pulsars), pg.PhTarget)
+            t0 = time.perf_counter()
+            res = ctx.pair_targets(targets, ti, clusters, ci, ncl, 0.05)
+            wall = time.perf_counter() - t0
+            st = ctx.stats()
+            print(json.dumps({"mode": "pairs", "streamed": True, "screen_pairs": int(len(take)),
+                              "pulsars": int(len(pulsars)), "pulsar_pairs": int(len(pti)), "pairs": int(len(ti)),
+                              "clones": int(st["clones"]), "clone_steps": int(st["clone_steps"]),
+                              "prefilter_s": pref_s, "wall_s": wall, "clone_steps_per_s_e2e": st["clone_steps"] / wall,
+                              "f_r50_sum": float(res["f_r50"].sum())}))
+            return
+        batch = pg.draw_pair_batch(list(stars) + list(pulsars), ti, clusters, ci, ncl, 0.05)
+        res = None
+        for _ in range(a.repeat):
+            res = ctx.pair(*batch)
+        st = ctx.stats()
+        print(json.dumps({"mode": "pairs", "screen_pairs": int(len(take)), "pulsar_pairs": int(len(pti)),
+                          "pairs": int(len(ti)), "clones": int(st["clones"]), "clone_steps": int(st["clone_steps"]),
+                          "ms_pair": st["ms_pair"], "max_steps": int(batch[2].max()) if len(ti) else 0,
+                          "f_r50_sum": float(res["f_r50"].sum()) if res is not None else 0.0}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "screen", "pairs"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-pair", action="store_true", help="skip the batched Monte Carlo measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-cli", action="store_true", help="skip the end-to-end run of the screen CLI")
     ap.add_argument("--no-control", action="store_true", help="skip the velocity-shuffled control's accuracy check")
+    g = ap.add_argument_group("profiling modes")
+    g.add_argument("--stars", type=int, default=None, help="screen: 20,000; pairs: 2,000")
+    g.add_argument("--clusters", type=int, default=None, help="screen: the workload's 4,087")
+    g.add_argument("--seed", type=int, default=None)
+    g.add_argument("--precision", choices=("mixed", "fp64"), default="mixed")
+    g.add_argument("--parts", type=int, default=None,
+                   help="screen: parts of a chunk of at least 8,192 stars (1 = screened whole; default about 1e7 "
+                        "star-cluster pairs a part)")
+    g.add_argument("--repeat", type=int, default=1)
+    g.add_argument("--pairs", type=int, default=200)
+    g.add_argument("--pulsars", type=int, default=1)
+    g.add_argument("--streamed", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return reference_arm(args)
+    if args.mode == "screen":
+        args.stars = args.stars or N_STARS
+        return mode_screen(args)
+    if args.mode == "pairs":
+        args.stars = args.stars or 2000
+        return mode_pairs(args)
 
     import numpy as np
     import torch
@@ -440,6 +630,7 @@ def main():
     cp, tp = make_inputs(tmp, rank)
     clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
     tmax = max(c.tmax_myr for c in clusters)
+    pp = pair_points(clusters, N_STARS, tmax)
     ctx = pg.Context(local)
     fp64_peak, fp32_peak = ctx.peaks()
     t0 = time.time()
@@ -478,9 +669,10 @@ def main():
         precision = pg.PGX_FP64
     with Clocks(local) as clk:
         per, stats, n_rows = run(precision, args.steps, args.warmup)
+    parts = max(1, stats[-1]["parts"])
     rows_mixed = ctx.fetch(n_rows)
     # the plain FP64 comparator: the chunk whole, every stage in turn (no parts, no overlap); its orbit launch is
-    # also the roofline's (the whole chunk on the whole GPU)
+    # also the orbit roofline's (the whole chunk on the whole GPU)
     ctx.set_split(0)
     ctx.stage(ps0, sig, pre)
     per64, stats64, n_rows64 = run(pg.PGX_FP64, max(2, min(args.steps, 3)), 1)
@@ -488,7 +680,7 @@ def main():
     ctx.set_split(8192)
     ctx.stage(ps0, sig, pre)
     accuracy = {"screen": compare_rows(rows_mixed, rows_fp64)}
-    del rows_mixed, rows_fp64
+    del rows_fp64
     if rank == 0 and not args.no_control:
         # the chance-alignment control: the same stars with velocities shuffled, mixed against FP64
         ctl = pg.control_targets(stars)
@@ -553,61 +745,68 @@ def main():
     s, s64 = stats[-1], stats64[-1]
     orbit_ms = statistics.mean(x["ms_orbit"] for x in stats64)
     achieved = FLOPS_PER_BODY_STEP * s64["orbit_body_steps"] / (orbit_ms * 1e-3)
-    cpu = None
+    cpu, parity = None, None
     if rank == 0 and not args.no_cpu:
         try:
-            cpu = cpu_baseline(cp, tp)
+            cpu, ora_rows = cpu_baseline(cp, tp, keep_rows=True)
+            parity = compare_to_oracle(rows_mixed, ora_rows, int(cpu["pairs"] // N_CLUSTERS))
+            cpu.pop("loop_s", None)
+            cpu.pop("pairs", None)
         except Exception as e:          # the baseline is reported, not required
             log("cpu baseline failed: %s" % e)
+    del rows_mixed
     if rank == 0:
+        scan = scan_roofline(stats, clk.summary(), pp, fp32_peak, parts)
         out = {
             "metric": "pairs/s", "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64+f32" if precision == pg.PGX_MIXED else "f64", "data": "synthetic",
             "precision": "mixed" if precision == pg.PGX_MIXED else "fp64",
             "config": config(args),
-            "plain_fp64": {"value": ws * pairs / (ms64 * 1e-3), "unit": "pairs/s", "ms_per_step": ms64,
-                           "speedup_of_value": ms64 / ms},
-            "rows_per_step": n_rows, "rows_fp64": n_rows64,
-            "mixed_vs_fp64": accuracy,
-            "work_per_step": {k: int(s[k]) for k in ("candidates", "ambiguous", "rechecked_points",
-                                                     "rechecked_draws", "kept")},
-            "stages_ms": {k: statistics.mean(x[k] for x in stats) for k in
-                          ("ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish")},
-            "stages_ms_fp64": {k: statistics.mean(x[k] for x in stats64) for k in
-                               ("ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish")},
+            "gpu_launches": int(sum(x["kernels"] for x in stats)),
+            "clocks": clk.summary(),
             "e2e": {"value": ws * pairs / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_s,
                     "how": "pgx_screen_chunks over %d chunks of the %d stars: host draws of chunk i+2, the orbits of "
                            "chunk i+1 (side stream) and the screen of chunk i overlap; rows copied to page-locked host "
                            "memory" % (E2E_CHUNKS, N_STARS),
                     "host_draw_s_unpipelined": draw_s},
-            "roofline": {"bound": "fp64", "kernel": "k_stm_orbits", "achieved": achieved / 1e12,
-                         "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
-                         "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
-                         "traffic": ORBIT_TRAFFIC_BYTES, "flops_per_body_step": FLOPS_PER_BODY_STEP,
-                         "body_steps_per_launch": s64["orbit_body_steps"], "ms_per_launch": orbit_ms,
-                         "launch": "the orbits of the whole chunk (the plain FP64 run's launch; the same kernel "
-                                   "as the mixed path's)",
-                         "fp64_instr_frac": FP64_INSTR_PER_BODY_STEP * s64["orbit_body_steps"] / (orbit_ms * 1e-3)
-                                            / (fp64_peak / 2),
-                         "fp64_instr_note": "FP64 instructions issued / the FMA instruction rate: DADD and DMUL take "
-                                            "a full slot for one flop, so the flop fraction understates how busy the "
-                                            "pipe is"},
-            "roofline_scan": scan_roofline(stats, clk.summary()),
+            "roofline": scan,
+            "roofline_orbits": {"bound": "fp64", "kernel": "k_stm_orbits", "achieved": achieved / 1e12,
+                                "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                                "peak_source": "FP64 FMA probe kernel of this run (pgx_peaks)",
+                                "traffic": ORBIT_TRAFFIC_BYTES, "flops_per_body_step": FLOPS_PER_BODY_STEP,
+                                "body_steps_per_launch": s64["orbit_body_steps"], "ms_per_launch": orbit_ms,
+                                "launch": "the orbits of the whole chunk (the plain FP64 run's launch; the same kernel "
+                                          "as the mixed path's)",
+                                "fp64_instr_frac": FP64_INSTR_PER_BODY_STEP * s64["orbit_body_steps"]
+                                                   / (orbit_ms * 1e-3) / (fp64_peak / 2)},
+            "cpu_baseline": cpu,
             "fp32_peak_tflops": fp32_peak / 1e12,
             "cluster_table_s": table_s,
-            "gpu_launches": int(sum(x["kernels"] for x in stats)),
-            "clocks": clk.summary(),
-            "cpu_baseline": cpu,
+            "rows_per_step": n_rows, "rows_fp64": n_rows64,
+            "work_per_step": {k: int(s[k]) for k in ("candidates", "ambiguous", "rechecked_points",
+                                                     "rechecked_draws", "kept")},
             "pair_mc": pair_mc,
             "cli": cli,
             "serving": serving,
+            # the evidence a reader checks first, last on the line
+            "stages_ms": {k[3:]: r4(statistics.mean(x[k] for x in stats)) for k in
+                          ("ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish")},
+            "stages_ms_fp64": {k[3:]: r4(statistics.mean(x[k] for x in stats64)) for k in
+                               ("ms_orbit", "ms_cov", "ms_scan", "ms_select", "ms_finish")},
+            "roofline_scan": {k: r4(scan[k]) for k in ("achieved", "frac", "issue_frac", "ms_per_launch")
+                              if scan and k in scan},
+            "plain_fp64": {"value": r4(ws * pairs / (ms64 * 1e-3)), "ms_per_step": r4(ms64),
+                           "speedup_of_value": r4(ms64 / ms)},
+            "mixed_vs_fp64": accuracy,
+            "parity_vs_oracle": parity,
         }
         print(json.dumps(out))
     ctx.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
 
 
 if __name__ == "__main__":

@@ -159,7 +159,7 @@ int pgx_tracks(PgxContext *ctx, int n, const double *ps, const int *npts, double
 /* ---- pair Monte Carlo ------------------------------------------------------------------------------------------ */
 /* Trace every clone of n_pairs pairs back and reduce each pair (reference ph_pair_clone + ph_pair_reduce,
  * src/phygas.c:200-238; GPU pg_pair + the host reduction of src/main_phygas_boinc.cpp:236-246).
- * Clones of pair p are clone_off[p] .. clone_off[p+1]-1 (clone_off[n_pairs] = total, at most 1024 x 16 per pair);
+ * Clones of pair p are clone_off[p] .. clone_off[p+1]-1 (clone_off[n_pairs] = total, at most 2^26 per pair);
  * ps = 12 doubles per clone as ph_pair_draw writes them; steps/dt per pair as ph_pair_draw returns them;
  * r50_pc/rtot_pc per pair.  res[n_pairs] gets the results; clone_out (NULL or 3 x total: best kpc, tbest Myr,
  * vbest kpc/Myr, clone-major blocks) the per-clone closest approaches. */
@@ -190,13 +190,16 @@ int pgx_pair_blocks(PgxContext *ctx, int blocks_per_sm);
 /* pgx_pair for callers that cannot allocate GPU memory (no counterpart in the reference): code running inside
  * another framework's device memory pool, loops that must not stall on the allocator, hosts that can only hand
  * over buffers they already own.  Every pointer is DEVICE memory the caller provides (clone_off[n_pairs + 1],
- * ps[12 * n_clones], steps/dt/r50_pc/rtot_pc[n_pairs], res[n_pairs]); n_clones = clone_off[n_pairs].  The call only
- * enqueues work on `stream` (a cudaStream_t, NULL = the legacy default stream) of the current device and returns;
- * res is complete when the stream reaches that point.  No cudaMalloc, cudaFree or allocating library call: the
- * per-clone scratch is a fixed 24 MiB array inside the library.  The first call on a device looks up that array's
- * address (set-up); make it before any stream capture.  At most 2^20 clones per call (PGX_E_LIMIT beyond);
- * pairs of more than 1024 clones get n = -1.  The scratch is shared by all calls and keeps the last call's
- * contents: calls that overlap on the GPU race, so serialise them. */
+ * ps[12 * n_clones], steps/dt/r50_pc/rtot_pc[n_pairs], res[n_pairs]); n_clones = clone_off[n_pairs].  After the
+ * first call on a device, a call only enqueues work on `stream` (a cudaStream_t, NULL = the legacy default stream)
+ * of the current device and returns; res is complete when the stream reaches that point.  The first call on a
+ * device does its set-up: it looks up the scratch array's address and fills the force tables with one kernel on the
+ * legacy default stream, then synchronizes the whole device -- make it before any stream capture, at start-up.  No
+ * cudaMalloc, cudaFree or allocating library call: the per-clone scratch is a fixed 24 MiB array inside the
+ * library.  At most 2^20 clones per call (PGX_E_LIMIT beyond).  A pair gets n = -1 when it has more than 1024 clones
+ * or when its offsets are not inside [0, n_clones] (a bad clone_off; the device offsets cannot be checked on the
+ * host); a pair without clones gets the reference's zeroed result with n = 0.  The scratch is shared by all calls
+ * and keeps the last call's contents: calls that overlap on the GPU race, so serialise them. */
 int pgx_pair_noalloc(void *stream, int n_pairs, int n_clones, const int *clone_off, const double *ps,
                      const int *steps, const double *dt, const double *r50_pc, const double *rtot_pc, PhResult *res);
 
@@ -212,6 +215,7 @@ typedef struct {
                                         times the first part's; the others run beside the previous part's screen) */
     double ms_prefilter;             /* pgx_prefilter: device time of the tracks and the pair tests */
     long prefilter_pairs, prefilter_rechecked;   /* pairs tested; pairs within the margin, decided on the host */
+    int parts;                       /* screen: the parts the chunk was screened in (1 = whole), one scan launch each */
 } PgxStats;
 int pgx_stats(const PgxContext *ctx, PgxStats *out);
 

@@ -9,6 +9,10 @@
  *       then one target per line (14 fields, optionally "clusters=NAME,...").
  *   Rows of targets [j0,j1) against clusters [i0,i1), in (target, cluster) order.  No "# done" line.
  *   stderr: "wu_time prep <s> run <s>" -- the per-cluster precompute and the per-target loop, timed apart.
+ *   With PHYGAS_WU_RAW set in the environment, screen mode writes each kept pair to stdout as one binary record
+ *   instead of the text row, so a caller can compare the values at full precision: int32 target index, cluster
+ *   index, kb, 0, then doubles sb, chi2, t, d_nom_pc, sig_pc, p_r50, p_rtot, vrel (80 bytes, host byte order; the
+ *   layout of PgxScreenRow in include/phygas_gb300.h).
  */
 #define _POSIX_C_SOURCE 199309L
 #include <math.h>
@@ -63,11 +67,13 @@ int main(int argc, char **argv) {
         t->has_rv = !isnan(t->rv) && !isnan(t->e_rv);
         only[nt] = NULL;
         const char *p = strstr(line + used, "clusters=");
-        if (p) {
+        if (p) {   /* an empty list is no list: the prefilter decides (reference main_phygas_boinc.cpp:318-321, 393) */
             size_t len = strcspn(p + 9, " \r\n");
-            only[nt] = malloc(len + 1);
-            memcpy(only[nt], p + 9, len);
-            only[nt][len] = 0;
+            if (len > 0) {
+                only[nt] = malloc(len + 1);
+                memcpy(only[nt], p + 9, len);
+                only[nt][len] = 0;
+            }
         }
         nt++;
     }
@@ -78,6 +84,7 @@ int main(int argc, char **argv) {
     if (i1 > nc) i1 = nc;
     double tmax = 0;
     for (int i = 0; i < nc; i++) if (cl[i].tmax_myr > tmax) tmax = cl[i].tmax_myr;
+    const int raw = getenv("PHYGAS_WU_RAW") != NULL;
     double t_prep = 0, t_run = 0, t0 = now_s();
     if (!strcmp(mode, "screen")) {
         ph_screen_r = p3 > 0 ? p3 : 2.0;
@@ -95,8 +102,14 @@ int main(int argc, char **argv) {
                 PhScreen s;
                 ph_screen_finish(&tl, &cin[i], &cl[i], ph_seed(tg[j].id, cl[i].name), chi2, kb, sb, &s);
                 if (s.p_r50 < p4) continue;
-                printf("%s %s %c %.3f %.3f %.2f %.2f %.4f %.4f %.2f\n", tg[j].id, cl[i].name, cl[i].kind, s.chi2, s.t,
-                       s.d_nom_pc, s.sig_pc, s.p_r50, s.p_rtot, s.vrel);
+                if (raw) {
+                    struct { int j, i, kb, pad; double v[8]; } rec = {j, i, kb, 0, {sb, s.chi2, s.t, s.d_nom_pc,
+                                                                                    s.sig_pc, s.p_r50, s.p_rtot,
+                                                                                    s.vrel}};
+                    fwrite(&rec, sizeof rec, 1, stdout);
+                } else
+                    printf("%s %s %c %.3f %.3f %.2f %.2f %.4f %.4f %.2f\n", tg[j].id, cl[i].name, cl[i].kind, s.chi2,
+                           s.t, s.d_nom_pc, s.sig_pc, s.p_r50, s.p_rtot, s.vrel);
             }
             ph_lin_free(&tl);
         }

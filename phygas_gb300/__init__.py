@@ -55,7 +55,8 @@ class PgxStats(C.Structure):
                                                                                ("orbit_body_steps", C.c_long),
                                                                                ("ms_prefilter", C.c_double),
                                                                                ("prefilter_pairs", C.c_long),
-                                                                               ("prefilter_rechecked", C.c_long)]
+                                                                               ("prefilter_rechecked", C.c_long),
+                                                                               ("parts", C.c_int)]
 
 
 ROW_DTYPE = np.dtype([("star", "i4"), ("cluster", "i4"), ("kb", "i4"), ("pad", "i4"), ("sb", "f8"), ("chi2", "f8"),

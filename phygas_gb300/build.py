@@ -1,7 +1,7 @@
 """In-tree build of libphygas_gb300 and its two CLIs (nvcc + gcc, sm_103a only, no cmake).
 
 Outputs go to phygas_gb300/_lib/: libphygas_gb300.so (CUDA kernels + C host code, static cudart), phygas_screen,
-phygas_cli, phygas_serve.  Objects are rebuilt only when a source or header is newer; compiles run in parallel.
+phygas_cli, phygas_serve.  (The oracle, the tests' checker, has its own build: oracle/build_oracle.py.)  Objects are rebuilt only when a source or header is newer; compiles run in parallel.
 
     python -m phygas_gb300.build            (or __graft_entry__.build())
 """
@@ -90,31 +90,6 @@ def build(verbose=False, jobs=None):
                   "-I", os.path.join(CSRC, "host"), s, "-o", exe, "-L", LIB, "-lphygas_gb300",
                   "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"])
     return so
-
-
-def build_oracle(with_reference=None):
-    """The checker: oracle/'s C restatement (gcc, the reference's flags), and -- when the reference checkout is
-    present, i.e. in the development container -- the reference itself via oracle/Makefile into oracle/_ref."""
-    odir = os.path.join(REPO, "oracle")
-    b = os.path.join(odir, "_build")
-    os.makedirs(b, exist_ok=True)
-    flags = ["-O2", "-std=c99", "-ffp-contract=off", "-fPIC", "-I", INCLUDE]
-    src = os.path.join(odir, "phygas_oracle.c")
-    obj = os.path.join(b, "phygas_oracle.o")
-    deps = [src, os.path.join(INCLUDE, "phygas.h")]
-    if _stale(obj, deps):
-        _run(["gcc"] + flags + ["-c", src, "-o", obj])
-    outs = [(os.path.join(b, "libphygas_oracle.so"), ["gcc", "-shared", "-o", None, obj, "-lm"], [obj]),
-            (os.path.join(b, "oracle_dump"), ["gcc"] + flags + [os.path.join(odir, "dump_main.c"), obj, "-o", None,
-                                                                "-lm"], [obj, os.path.join(odir, "dump_main.c")]),
-            (os.path.join(b, "oracle_wu"), ["gcc"] + flags + [os.path.join(odir, "wu_main.c"), obj, "-o", None,
-                                                              "-lm"], [obj, os.path.join(odir, "wu_main.c")])]
-    for out, cmd, dep in outs:
-        if _stale(out, dep):
-            _run([out if c is None else c for c in cmd])
-    ref = with_reference if with_reference is not None else "/root/reference"
-    if ref and os.path.isdir(os.path.join(ref, "src")) and shutil.which("make"):
-        _run(["make", "-s", "-C", odir, "ref", "REF=" + ref])
 
 
 if __name__ == "__main__":

@@ -497,7 +497,7 @@ int pgx_draw_pair_batch(int n_pairs, const PhTarget *t, const int *ti, const PhC
     if (n_pairs > 0 && (!t || !ti || !c || !ci || !n_clones || !ps || !steps || !dt || !r50_pc || !rtot_pc))
         return PGX_E_ARG;
     for (int q = 0; q < n_pairs; q++)
-        if (n_clones[q] < 0 || n_clones[q] > 16384) return PGX_E_LIMIT;
+        if (n_clones[q] < 0 || n_clones[q] > pgx::kMaxPairClones) return PGX_E_LIMIT;
     const int r = pgh_draw_pair_batch(n_pairs, t, ti, c, ci, n_clones, dt_myr,
                                       threads > 0 ? threads : pgh_default_threads(), clone_off, ps, steps, dt,
                                       r50_pc, rtot_pc);
@@ -850,7 +850,9 @@ int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision,
     CK(cudaEventRecord(ctx->ev[EV_START], ctx->st));
     if (ctx->nparts == 0) {
         RET(tracks_slot(ctx, ctx->cur, tmax_myr, ctx->st, true));
-        return screen_slot(ctx, ctx->cur, cut, precision, n_rows, true);
+        RET(screen_slot(ctx, ctx->cur, cut, precision, n_rows, true));
+        ctx->stats.parts = 1;
+        return 0;
     }
     // a chunk staged in parts: part p is screened from slot p & 1 while, with the mixed screen, part p + 1's orbits
     // run on the side stream in the other slot (FP64 pipe beside FP32 and integer work); the plain FP64 path runs
@@ -892,6 +894,7 @@ int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision,
         rows += np;
         if (!overlap && p + 1 < K) RET(tracks_slot(ctx, s ^ 1, tmax_myr, ctx->st, false));
     }
+    ctx->stats.parts = K;
     if (n_rows) *n_rows = rows;
     return 0;
 }
@@ -1230,7 +1233,8 @@ int pair_run(PgxContext *ctx, int variant, int n_pairs, const int *clone_off, co
     for (int p = 0; p < n_pairs; p++) {
         const int m = clone_off[p + 1] - clone_off[p];
         if (m < 0) return fail(ctx, PGX_E_ARG, "pgx_pair: clone_off not ascending at %d", p);
-        if (m > 16384) return fail(ctx, PGX_E_LIMIT, "pgx_pair: pair %d has %d clones (limit 16384)", p, m);
+        if (m > pgx::kMaxPairClones)
+            return fail(ctx, PGX_E_LIMIT, "pgx_pair: pair %d has %d clones (limit %d)", p, m, pgx::kMaxPairClones);
         if (steps[p] < 0) return fail(ctx, PGX_E_ARG, "pgx_pair: steps[%d] = %d", p, steps[p]);
         mmax = std::max(mmax, m);
     }
@@ -1243,7 +1247,7 @@ int pair_run(PgxContext *ctx, int variant, int n_pairs, const int *clone_off, co
     long long clone_steps = 0;
     for (int p = 0; p < n_pairs; p++) {
         const int m = clone_off[p + 1] - clone_off[p];
-        if (m > 1024) {
+        if (m > 1024 && m <= pgx::kSortMax) {
             int n2 = 1;
             while (n2 < m) n2 <<= 1;
             big_n2 = std::max(big_n2, n2);
@@ -1555,6 +1559,8 @@ int finish_one(PgxContext *ctx, const PhLin *tl, const PhLin *cl, const PhCluste
 
 int reduce_only(PgxContext *ctx, int m, const double *best, const double *tbest, const double *vbest, double r50,
                 double rt, PhResult *res) {
+    if (m > pgx::kMaxPairClones)
+        return fail(ctx, PGX_E_LIMIT, "ph_pair_reduce: %d clones (limit %d)", m, pgx::kMaxPairClones);
     const int off[2] = {0, m};
     RET(ensure(ctx, ctx->p_off, 8));
     RET(ensure(ctx, ctx->p_cres, (size_t)3 * (m > 0 ? m : 1) * 8));
@@ -1576,8 +1582,7 @@ int reduce_only(PgxContext *ctx, int m, const double *best, const double *tbest,
     CKL();
     int n2 = 1;
     while (n2 < m) n2 <<= 1;
-    const size_t smem = m > 1024 ? (size_t)n2 * 8 : 0;
-    if (m > 16384) return fail(ctx, PGX_E_LIMIT, "ph_pair_reduce: %d clones (limit 16384)", m);
+    const size_t smem = m > 1024 && m <= pgx::kSortMax ? (size_t)n2 * 8 : 0;
     if (smem > 48 * 1024)
         CK(cudaFuncSetAttribute(pgx::k_pair_reduce_big, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     pgx::k_pair_reduce_big<<<1, 256, smem, ctx->st>>>(Pp);

@@ -80,6 +80,11 @@ int mc_variants();
 void mc_variant_shape(int v, int &warps, int &cpl, int &min_blocks);
 cudaError_t mc_variant_grid(int v, int sms, int &grid);
 cudaError_t launch_mc(int v, int grid, int prep_grid, int reduce_grid, cudaStream_t st, const McPairs *Pd);
+// pairs of more than 1024 clones: sorted in shared memory up to kSortMax clones (dynamic shared memory of the launch:
+// the batch's largest such pair rounded up to a power of two, times 8 bytes), beyond that reduced by radix selection
+constexpr int kSortMax = 16384;
+// the most clones of one pair (the clone offsets are 32-bit)
+constexpr int kMaxPairClones = 1 << 26;
 __global__ void k_pair_reduce_big(McPairs P);
 __global__ void k_pair_reduce_only(McPairs P);
 __global__ void k_peak_dfma(double *out, int iters, double a, double b);

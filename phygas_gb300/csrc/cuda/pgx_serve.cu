@@ -241,7 +241,7 @@ int pgx_server_submit(PgxServer *s, const PgxJob *job, long *id) {
     if (!s || !job || !id) return PGX_E_ARG;
     if (job->n_targets <= 0 || !job->targets) return PGX_E_ARG;
     if (job->kind != PGX_JOB_SCREEN && job->kind != PGX_JOB_CONTROL && job->kind != PGX_JOB_PAIRS) return PGX_E_ARG;
-    if (job->kind == PGX_JOB_PAIRS && (job->n_clones < 0 || job->n_clones > 16384 || !(job->dt_myr > 0)))
+    if (job->kind == PGX_JOB_PAIRS && (job->n_clones < 0 || job->n_clones > (1 << 26) || !(job->dt_myr > 0)))
         return PGX_E_ARG;
     if (job->kind != PGX_JOB_PAIRS && job->precision != PGX_MIXED && job->precision != PGX_FP64) return PGX_E_ARG;
     std::unique_ptr<Job> j(new Job());

@@ -6,8 +6,9 @@
  *   target cluster kind n d05 d50 d95 t05 t50 t95 v05 v50 v95 f_r50 f_rtot age16 age84
  * The prefilter runs on the GPU (pgx_prefilter: the same pairs as the reference's tracks and ph_prefilter keep), the
  * clone draws (bit-identical to the reference's) on all host cores; the clones of many pairs and targets are traced
- * and reduced together on the GPU (PHYGAS_BATCH_CLONES per launch, default 2^20), and rows are printed by whole
- * targets.
+ * and reduced together on the GPU (about PHYGAS_BATCH_CLONES per launch, default 2^20, and at least one pair).  Any
+ * clone count up to 2^26 per pair: pairs of more than 16,384 clones take their quantiles by radix selection on the
+ * GPU instead of a shared-memory sort, with the same results.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -101,7 +102,7 @@ int main(int argc, char **argv) {
     PhTarget *tg;
     int nc = ph_read_clusters(argv[1], &cl), nt = ph_read_targets(argv[2], &tg);
     if (nc <= 0 || nt <= 0) { fprintf(stderr, "can't read inputs (%d clusters, %d targets)\n", nc, nt); return 1; }
-    if (n_clones > 16384) { fprintf(stderr, "phygas_cli: n_clones %d above the GPU limit of 16384\n", n_clones); return 1; }
+    if (n_clones > (1 << 26)) { fprintf(stderr, "phygas_cli: n_clones %d above 2^26\n", n_clones); return 1; }
     double tmax = 0;
     for (int i = 0; i < nc; i++) if (cl[i].tmax_myr > tmax) tmax = cl[i].tmax_myr;
     PgxContext *ctx;
@@ -127,10 +128,14 @@ int main(int argc, char **argv) {
     for (long q = 0; q < np;) {
         const int w = pti[q];
         int kept = 0;
-        for (; q < np && pti[q] == w; q++, kept++) push(&P, widx[w], pci[q]);
+        for (; q < np && pti[q] == w; q++, kept++) {
+            push(&P, widx[w], pci[q]);
+            /* a batch holds about PHYGAS_BATCH_CLONES clones (at least one pair), whatever n_clones is */
+            if ((long)P.n * (n_clones > 0 ? n_clones : 1) >= batch && flush(ctx, &P, tg, cl, n_clones, dt, threads))
+                return 1;
+        }
         pairs += kept;
         done++;
-        if ((long)P.n * n_clones >= batch && flush(ctx, &P, tg, cl, n_clones, dt, threads)) return 1;
         fprintf(stderr, "%s: %d of %d clusters reachable (%.1f s so far)\n", tg[widx[w]].id, kept, nc, now_s() - t0);
     }
     done = nw;

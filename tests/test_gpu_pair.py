@@ -49,11 +49,14 @@ def test_reduction_bit_exact(built, golden):
 
 
 def test_reduction_large_pairs(ctx):
-    """Pairs of 1,000 (one warp, registers and shuffles) and 3,000 clones (shared-memory path) reduce exactly like a
-    sort on the host."""
+    """Pairs of 1,000 (one warp, registers and shuffles), 3,000 clones (shared-memory sort) and more than 16,384
+    (radix selection from global memory; the reference has no limit) reduce exactly like a sort on the host, ties
+    included."""
     rng = np.random.default_rng(5)
-    for m in (1, 31, 200, 1000, 1024, 1025, 3000):
+    for m in (1, 31, 200, 1000, 1024, 1025, 3000, 16384, 16385, 70001):
         cl = np.abs(rng.normal(size=(3, m))) * np.array([[1e-3], [10.0], [0.05]])
+        if m > 3000:                     # repeated values: ties at the order statistics
+            cl[:, ::7] = cl[:, :1]
         b, t, v = cl
         L = pg.lib()
         L.ph_pair_reduce.argtypes = [C.POINTER(pg.PhCluster), C.c_int, C.POINTER(C.c_double),

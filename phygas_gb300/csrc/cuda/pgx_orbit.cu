@@ -526,7 +526,59 @@ __global__ void __launch_bounds__(kMcThreads) k_pair_reduce_only(McPairs P) {
     if (m > 0 && m <= 1024) reduce_dispatch(P, p, smem[w], lane);
 }
 
-// pairs of 0 clones never get an item: their (empty) result is written here, with the big-pair reduction
+// A pair's clone value e of array `which` (0 best, 1 tbest, 2 vbest) in the units of the reduction, as the bit
+// pattern that orders it: the values are non-negative, so their IEEE patterns sort as unsigned integers.
+__device__ __forceinline__ unsigned long long reduce_key(const double *src, int which, int e) {
+    double v = src[e];
+    if (which == 0) v = __dmul_rn(v, 1000.0);
+    else if (which == 2) v = __dmul_rn(v, kKms);
+    return (unsigned long long)__double_as_longlong(v);
+}
+
+// The k-th smallest (0-based) of a pair's m values of array `which`, read from global memory by the whole block: an
+// MSB radix selection, 8 bits a pass, each pass counting the values that share the prefix found so far.  Exact: the
+// element a sort would put at index k.  For pairs too large to sort in shared memory.
+__device__ double radix_select(const double *src, int which, int m, int k) {
+    __shared__ unsigned hist[256];
+    __shared__ unsigned long long s_prefix;
+    __shared__ int s_k;
+    if (threadIdx.x == 0) { s_prefix = 0; s_k = k; }
+    unsigned long long mask = 0;
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b] = 0;
+        __syncthreads();
+        const unsigned long long prefix = s_prefix;
+        for (int e = threadIdx.x; e < m; e += blockDim.x) {
+            const unsigned long long key = reduce_key(src, which, e);
+            if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int kk = s_k, b = 0;
+            for (; b < 255 && kk >= (int)hist[b]; b++) kk -= (int)hist[b];
+            s_k = kk;
+            s_prefix = prefix | ((unsigned long long)b << shift);
+        }
+        mask |= 255ull << shift;
+        __syncthreads();
+    }
+    const double v = __longlong_as_double((long long)s_prefix);
+    __syncthreads();
+    return v;
+}
+
+// interp_q of the sorted values, the two order statistics it reads found by radix_select
+__device__ double select_q(const double *src, int which, int m, double q) {
+    const double pos = __dmul_rn(q, (double)(m - 1));
+    const int i = (int)pos;
+    if (i >= m - 1) return radix_select(src, which, m, m - 1);
+    const double a = radix_select(src, which, m, i), b = radix_select(src, which, m, i + 1);
+    return __dadd_rn(a, __dmul_rn(__dsub_rn(pos, (double)i), __dsub_rn(b, a)));
+}
+
+// pairs of 0 clones never get an item: their (empty) result is written here, with the big-pair reduction.  Pairs of
+// up to kSortMax clones are sorted in shared memory (launched with room for the batch's largest such pair); larger
+// pairs take their order statistics by radix selection from global memory.
 __global__ void k_pair_reduce_big(McPairs P) {
     extern __shared__ double sm[];
     const int p = blockIdx.x;
@@ -551,7 +603,25 @@ __global__ void k_pair_reduce_big(McPairs P) {
     __shared__ double res[9];
     if (threadIdx.x == 0) { c50 = 0; ctot = 0; }
     __syncthreads();
-    for (int which = 0; which < 3; which++) {
+    if (m > kSortMax) {
+        int l50 = 0, ltot = 0;
+        for (int e = threadIdx.x; e < m; e += blockDim.x) {
+            const double v = __dmul_rn(P.cres[o + e], 1000.0);
+            l50 += v < P.r50_pc[p];
+            ltot += v < P.rtot_pc[p];
+        }
+        atomicAdd(&c50, l50);
+        atomicAdd(&ctot, ltot);
+        for (int which = 0; which < 3; which++) {
+            const double *src = P.cres + (size_t)which * P.n_clones + o;
+            const double q05 = select_q(src, which, m, 0.05), q50 = select_q(src, which, m, 0.5),
+                         q95 = select_q(src, which, m, 0.95);
+            if (threadIdx.x == 0) { res[3 * which] = q05; res[3 * which + 1] = q50; res[3 * which + 2] = q95; }
+        }
+        __syncthreads();
+        n2 = 0;                             // nothing left to sort below
+    }
+    for (int which = 0; which < 3 && n2 > 0; which++) {
         const double *src = P.cres + (size_t)which * P.n_clones + o;
         int l50 = 0, ltot = 0;
         for (int e = threadIdx.x; e < n2; e += blockDim.x) {
@@ -640,9 +710,11 @@ __global__ void k_peak_ffma(float *out, int iters, float a, float b) {
 // GPU that loads the library until the process exits).  It calls no allocating routine.
 //
 // Limits: at most kNoAllocMaxClones clones per call (24 MiB of scratch); pairs of more than 1024 clones get a result
-// with n = -1 (pgx_pair handles them).  Every call shares the one scratch array and leaves its contents behind; two
-// calls whose work overlaps on the GPU (different streams, or different host threads) race on it and must be
-// serialised by the caller.
+// with n = -1 (pgx_pair handles them), and so does a pair whose offsets leave [0, n_clones).  Every call shares the
+// one scratch array and leaves its contents behind; two calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on it and must be serialised by the caller.  The first call on a device runs the
+// set-up below, which fills the force tables with a kernel on the legacy default stream and synchronizes the whole
+// device: make it before any stream capture, and outside latency-critical work.
 namespace pgx {
 
 constexpr int kNoAllocMaxClones = 1 << 20;
@@ -681,8 +753,11 @@ __global__ void __launch_bounds__(kMcThreads) k_pair_mc_noalloc(int n_pairs, int
     }
 }
 
-// one warp per pair, after all clones are traced (stream order)
-__global__ void __launch_bounds__(kMcThreads) k_pair_reduce_noalloc(int n_pairs, const int *__restrict__ clone_off,
+// one warp per pair, after all clones are traced (stream order).  The offsets are device memory the host cannot
+// check: a pair whose clones do not lie inside [0, n_clones) -- the clones this call traced -- gets n = -1 instead
+// of reading scratch the call did not write (or memory past it).
+__global__ void __launch_bounds__(kMcThreads) k_pair_reduce_noalloc(int n_pairs, int n_clones,
+                                                                    const int *__restrict__ clone_off,
                                                                     const double *__restrict__ r50,
                                                                     const double *__restrict__ rt,
                                                                     const double *cres, PhResultDev *res) {
@@ -690,11 +765,13 @@ __global__ void __launch_bounds__(kMcThreads) k_pair_reduce_noalloc(int n_pairs,
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int p = blockIdx.x * (kMcThreads / 32) + w;
     if (p >= n_pairs) return;
-    const int o = clone_off[p], m = clone_off[p + 1] - o;
+    const int o = clone_off[p], e = clone_off[p + 1];
+    const bool bad = o < 0 || e < o || e > n_clones;
+    const int m = bad ? -1 : e - o;
     if (m <= 0 || m > 1024) {
         if (lane == 0) {
             PhResultDev z;
-            z.n = m <= 0 ? 0 : -1;
+            z.n = m == 0 ? 0 : -1;
             z.pad = 0;
             z.d05 = z.d50 = z.d95 = z.t05 = z.t50 = z.t95 = z.v05 = z.v50 = z.v95 = z.f_r50 = z.f_rtot = 0.0;
             res[p] = z;
@@ -779,7 +856,7 @@ extern "C" int pgx_pair_noalloc(void *stream, int n_pairs, int n_clones, const i
     if (e == cudaSuccess) {
         const int wpb = pgx::kMcThreads / 32;
         pgx::k_pair_reduce_noalloc<<<(n_pairs + wpb - 1) / wpb, pgx::kMcThreads, 0, st>>>(
-            n_pairs, clone_off, r50_pc, rtot_pc, d->cres, reinterpret_cast<pgx::PhResultDev *>(res));
+            n_pairs, n_clones, clone_off, r50_pc, rtot_pc, d->cres, reinterpret_cast<pgx::PhResultDev *>(res));
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) {

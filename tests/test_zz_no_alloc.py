@@ -1,7 +1,7 @@
 """pgx_pair_noalloc -- the pair Monte Carlo for callers that cannot allocate GPU memory (they run inside another
 framework's device memory pool, or in a loop that must not stall on the allocator, and can only hand over device
-buffers they already own).  It must give what the allocating entry point pgx_pair gives, call after call, although
-all calls share one fixed scratch array inside the library.
+buffers they already own).  It must give what the allocating entry point pgx_pair gives, bit for bit, call after
+call, although all calls share one fixed scratch array inside the library, and it must not allocate device memory.
 
 This file is collected last on purpose: if it fails, a run that stops at the first failure has run everything else.
 """
@@ -46,29 +46,97 @@ def _workloads():
     return [a, b]
 
 
+class _Dev:
+    """The batch in device memory (torch tensors), and a device result buffer: the caller's own buffers."""
+
+    def __init__(self, torch, off, ps, steps, dt, r50, rt):
+        self.t = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in
+                  dict(off=off, ps=ps, steps=steps, dt=dt, r50=r50, rt=rt).items()}
+        self.n_pairs, self.n_clones = len(steps), int(off[-1])
+        self.res = torch.zeros(max(self.n_pairs, 1) * pg.RESULT_DTYPE.itemsize // 8, dtype=torch.float64,
+                               device="cuda")
+
+    def call(self, f, stream, n_clones):
+        t = self.t
+        return f(stream.cuda_stream, self.n_pairs, n_clones, t["off"].data_ptr(), t["ps"].data_ptr(),
+                 t["steps"].data_ptr(), t["dt"].data_ptr(), t["r50"].data_ptr(), t["rt"].data_ptr(),
+                 self.res.data_ptr())
+
+    def result(self, stream):
+        stream.synchronize()
+        return self.res.cpu().numpy().view(pg.RESULT_DTYPE)[:self.n_pairs]
+
+
+def _same_bits(got, want):
+    assert got.tobytes() == want.tobytes(), [(i, got[i], want[i]) for i in range(len(got))
+                                             if got[i].tobytes() != want[i].tobytes()][:3]
+
+
 def test_noalloc_equals_pgx_pair_twice(built):
+    """Two calls in a row on different batches: each result row is pgx_pair's, bit for bit."""
     torch = pytest.importorskip("torch")
     noalloc = _bind()
     torch.cuda.set_device(0)
     stream = torch.cuda.current_stream()
     with pg.Context(0) as ctx:
-        for off, ps, steps, dt, r50, rt in _workloads():     # two calls in a row, different inputs
+        for off, ps, steps, dt, r50, rt in _workloads():
             want = ctx.pair(off, ps, steps, dt, r50, rt)
-            n_pairs, n_clones = len(steps), int(off[-1])
-            dev = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in
-                   dict(off=off, ps=ps, steps=steps, dt=dt, r50=r50, rt=rt).items()}
-            res = torch.zeros(n_pairs * pg.RESULT_DTYPE.itemsize // 8, dtype=torch.float64, device="cuda")
-            rc = noalloc(stream.cuda_stream, n_pairs, n_clones, dev["off"].data_ptr(), dev["ps"].data_ptr(),
-                         dev["steps"].data_ptr(), dev["dt"].data_ptr(), dev["r50"].data_ptr(), dev["rt"].data_ptr(),
-                         res.data_ptr())
-            assert rc == 0
-            stream.synchronize()
-            got = res.cpu().numpy().view(pg.RESULT_DTYPE)
-            assert np.array_equal(got["n"], want["n"])
-            for k in ("f_r50", "f_rtot"):
-                assert np.all(np.abs(got[k] - want[k]) <= ot.PROB_TOL), k
-            for k in ("d05", "d50", "d95", "t05", "t50", "t95", "v05", "v50", "v95"):
-                assert np.all(np.abs(got[k] - want[k]) <= ot.REL_TOL * np.abs(want[k])), k
+            d = _Dev(torch, off, ps, steps, dt, r50, rt)
+            assert d.call(noalloc, stream, int(off[-1])) == 0
+            _same_bits(d.result(stream), want)
+
+
+def test_noalloc_empty_big_and_bad_pairs(built):
+    """A batch with a pair without clones (n = 0, the reference's zeroed result), a pair of 1,025 clones (beyond the
+    fixed scratch's per-pair reduction: n = -1) and ordinary pairs (pgx_pair's bits); then offsets that reach past
+    n_clones, which the device cannot trust: that pair gets n = -1, the others their own results."""
+    torch = pytest.importorskip("torch")
+    noalloc = _bind()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    off, ps, steps, dt, r50, rt = _workloads()[1]
+    rng = np.random.default_rng(11)
+    # pairs 0..3 of the synthetic batch with 0, 1,025 (clones repeated), 200 and 37 clones
+    m = [0, 1025, 200, 37]
+    blocks = []
+    for q, k in enumerate(m):
+        src = ps[12 * off[q]:12 * off[q + 1]].reshape(-1, 12)
+        blocks.append(src[rng.integers(0, len(src), k)] if k else np.zeros((0, 12)))
+    ps2 = np.concatenate(blocks).ravel()
+    off2 = np.concatenate([[0], np.cumsum(m)]).astype(np.int32)
+    args = (off2, ps2, steps[:4], dt[:4], r50[:4], rt[:4])
+    with pg.Context(0) as ctx:
+        want = ctx.pair(*args)
+    d = _Dev(torch, *args)
+    assert d.call(noalloc, stream, int(off2[-1])) == 0
+    got = d.result(stream)
+    assert got["n"].tolist() == [0, -1, 200, 37]
+    assert want["n"].tolist() == [0, 1025, 200, 37]
+    _same_bits(got[[0, 2, 3]], want[[0, 2, 3]])
+    # the last pair's offsets claim 37 clones, the call traces only n_clones = off2[3] + 10 of them
+    assert d.call(noalloc, stream, int(off2[3]) + 10) == 0
+    got = d.result(stream)
+    assert got["n"].tolist() == [0, -1, 200, -1]
+    _same_bits(got[[0, 2]], want[[0, 2]])
+
+
+def test_noalloc_leaves_device_memory_alone(built):
+    """After the first call on the device (its set-up), further calls allocate nothing: the device's free memory is
+    the same before and after them."""
+    torch = pytest.importorskip("torch")
+    noalloc = _bind()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    devs = [_Dev(torch, *w) for w in _workloads()]
+    for d in devs:                                        # set-up and warm-up
+        assert d.call(noalloc, stream, d.n_clones) == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        for d in devs:
+            assert d.call(noalloc, stream, d.n_clones) == 0
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_noalloc_rejects_oversize(built):

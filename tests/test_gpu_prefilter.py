@@ -12,6 +12,7 @@ import pytest
 
 import phygas_gb300 as pg
 from phygas_gb300 import synth
+from tests import oracle_tools as ot
 
 pytestmark = pytest.mark.gpu
 
@@ -146,3 +147,38 @@ def test_stage2_pairs_with_lists(ctx, inputs):
     want = [(0, int(c)) for t, c in zip(pti, pci) if t == 0] + [(1, 12), (1, 733), (1, 4000)] \
         + [(2, int(c)) for t, c in zip(pti, pci) if t == 1]
     assert list(zip(ti.tolist(), ci.tolist())) == want
+
+
+def test_stage2_pairs_match_the_oracle_work_unit(ctx, inputs, golden):
+    """The same selection against the oracle's work-unit runner (the reference BOINC app's pair-mode loop over
+    "clusters=" lines, src/main_phygas_boinc.cpp:304-321, 445-447): the (target, cluster) pairs it runs, in its
+    order, from a work unit with a list, an empty list (the prefilter decides), a list naming no cluster, and no
+    list -- for stars and a pulsar."""
+    import tempfile
+    clusters, _ = inputs
+    with open(golden["screen"]) as f:
+        star_lines = [ln.rstrip("\n") for ln in f if ln.strip() and not ln.startswith(("#", "PHYGAS"))][:3]
+    with open(golden["pulsar"]) as f:
+        pulsar_lines = [ln.rstrip("\n") for ln in f if ln.strip() and not ln.startswith(("#", "PHYGAS"))][:1]
+    names = ",".join(clusters[i].name.decode() for i in (4000, 12, 733, 2048))
+    renamed = "X" + pulsar_lines[0]              # the same pulsar under another id (ids key the rows)
+    lines = [star_lines[0] + " clusters=" + names, star_lines[1] + " clusters=", star_lines[2],
+             renamed + " clusters=no_such_cluster", pulsar_lines[0]]
+    with tempfile.TemporaryDirectory() as d:
+        wu = os.path.join(d, "in")
+        with open(wu, "w") as f:
+            f.write("PHYGAS 1 pair 2 0.05\n" + "\n".join(lines) + "\n")
+        out = ot.run([ot.ORACLE_WU, golden["clusters"], wu])
+        tp = os.path.join(d, "targets")
+        with open(tp, "w") as f:
+            f.write("\n".join(ln.split(" clusters=")[0] for ln in lines) + "\n")
+        targets = pg.read_targets(tp)
+    lists = [ln.split(" clusters=")[1] if " clusters=" in ln else None for ln in lines]
+    ti, ci = ctx.pairs_with_lists(targets, lists, clusters)
+    index = {c.name.decode(): i for i, c in enumerate(clusters)}
+    ids = {t.id.decode(): j for j, t in enumerate(targets)}
+    assert len(ids) == len(targets)
+    want = [(ids[row.split()[0]], index[row.split()[1]]) for row in out.splitlines()]
+    got = list(zip(ti.tolist(), ci.tolist()))
+    assert got == want
+    assert {t for t, _ in got} == {0, 1, 2, 4}

@@ -25,6 +25,10 @@ Under torchrun (N > 1) every rank screens its own chunk (weak scaling, no data e
 Profiling modes (one JSON line each; nothing else runs on the GPU, so a profiler sees only their launches):
   python bench.py --mode screen [--stars 20000] [--clusters N] [--precision mixed|fp64] [--parts K] [--repeat R]
       one screen of a synthetic chunk (the cluster-table orbit launch first, then the screen's launches in order)
+  python bench.py --mode refgpu [--stars 20000]
+      the reference's own GPU kernels (oracle/_ref/ref_kernels.ptx, built from its source for sm_103a) driven as its
+      app drives them, timed stage by stage beside this build's kernels on the benchmark chunk and a pulsar pair job,
+      with the rows compared
   python bench.py --mode pairs [--stars 2000] [--pairs 200] [--pulsars 1] [--streamed]
       one batch of the pair Monte Carlo: --pairs kept screen pairs (p_r50 >= 0.001, evenly spaced) plus --pulsars
       synthetic pulsars against their prefiltered clusters, clones U{200,500,1000} at dt 0.05 Myr; with --streamed the
@@ -214,15 +218,21 @@ def compare_to_oracle(gpu, ora, n_stars, cut=CHI2_MAX, p_cut=P_MIN):
                                                                           .tolist())
     em_bad = [k for k in (em_g ^ em_o) if k not in near_p]
 
-    def rel(f):
-        x = np.abs(a[f] - b[f]) / np.maximum(np.abs(b[f]), 1e-300)
+    def rel(f, floor=1e-300):
+        x = np.abs(a[f] - b[f]) / np.maximum(np.abs(b[f]), floor)
         return {"max": r4(float(x.max())) if len(x) else 0.0,
                 "p99": r4(float(np.quantile(x, 0.99))) if len(x) else 0.0}
     dp50, dpt = np.abs(a["p_r50"] - b["p_r50"]), np.abs(a["p_rtot"] - b["p_rtot"])
+    gi, oi = {k: i for i, k in enumerate(kg.tolist())}, {k: i for i, k in enumerate(ko.tolist())}
+    detail = [{"star": int(k >> 32), "cluster": int(k & 0xffffffff),
+               "chi2_gpu": float(gpu["chi2"][gi[k]]) if k in gi else None,
+               "chi2_oracle": float(ora["chi2"][oi[k]]) if k in oi else None} for k in bad_sets[:4]]
     return {"stars": int(n_stars), "rows_gpu": int(len(gpu)), "rows_oracle": int(len(ora)),
-            "kept_set_mismatches": len(bad_sets), "emitted_gpu": len(em_g), "emitted_oracle": len(em_o),
+            "kept_set_mismatches": len(bad_sets), "kept_set_mismatch_pairs": detail,
+            "emitted_gpu": len(em_g), "emitted_oracle": len(em_o),
             "emitted_set_mismatches": len(em_bad), "argmin_point_differs": int(np.sum(a["kb"] != b["kb"])),
-            "chi2_rel": rel("chi2"), "t_rel": rel("t_myr"), "d_nom_rel": rel("d_nom_pc"), "sig_rel": rel("sig_pc"),
+            "chi2_rel_floor1": rel("chi2", 1.0), "t_rel": rel("t_myr"), "d_nom_rel": rel("d_nom_pc"),
+            "sig_rel": rel("sig_pc"),
             "vrel_rel": rel("vrel_kms"),
             "p_r50_abs_max": r4(float(dp50.max())) if len(dp50) else 0.0, "p_r50_differ": int(np.sum(dp50 > 0)),
             "p_rtot_abs_max": r4(float(dpt.max())) if len(dpt) else 0.0, "p_rtot_differ": int(np.sum(dpt > 0)),
@@ -357,7 +367,9 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
 # clusters with the prefilter, 1000 clones).  SERVE_JOBS jobs with the mixed screen, so that the 99th percentile is
 # one; the first SERVE_JOBS_FP64 of the same stream again with the plain FP64 screen (whose screen jobs are ~35x
 # longer) for the comparison.
-SERVE_JOBS, SERVE_JOBS_FP64, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 200, 40, 8.0, 3, 1004
+# The rate keeps the GPU about 60 % busy with the mixed screen (a pulsar job is ~0.7 s of clone tracing): latency, not
+# a queue that grows without end.
+SERVE_JOBS, SERVE_JOBS_FP64, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 200, 40, 2.0, 3, 1004
 # chunks of the benchmark's stars per end-to-end run (the pipeline's fill is spread over them)
 E2E_CHUNKS = 8
 
@@ -578,13 +590,127 @@ def mode_pairs(a):
                           "f_r50_sum": float(res["f_r50"].sum()) if res is not None else 0.0}))
 
 
+def _ref_gpu_run(cp, wu, j0=None, j1=None):
+    """The reference's own GPU kernels driven as its app drives them (oracle/_build/ref_gpu): rows and times."""
+    ptx = os.path.join(REPO, "oracle", "_ref", "ref_kernels.ptx")
+    exe = os.path.join(REPO, "oracle", "_build", "ref_gpu")
+    if not (os.path.exists(ptx) and os.path.exists(exe)):
+        raise RuntimeError("reference-GPU comparator not built (%s, %s)" % (ptx, exe))
+    cmd = [exe, cp, wu, ptx] + ([str(j0), str(j1)] if j0 is not None else [])
+    t0 = time.perf_counter()
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    wall = time.perf_counter() - t0
+    if r.returncode:
+        raise RuntimeError("ref_gpu failed: %s" % r.stderr[-800:])
+    f = r.stderr.split("ref_gpu_time")[-1].split()
+    t = {f[i]: float(f[i + 1]) for i in range(0, len(f) - 1, 2) if f[i] in ("prep", "total", "host")}
+    for i, k in enumerate(f):
+        if k in ("lin", "chi2", "finish", "pair"):
+            t[k + "_s"], t[k + "_launches"] = float(f[i + 1]), int(f[i + 2])
+        if k in ("pairs", "clones", "clone_steps"):
+            t[k] = int(f[i + 1])
+    t["process_wall_s"] = wall
+    return r.stdout.splitlines(), t, [ln for ln in r.stderr.splitlines() if ln.startswith("GPU ")]
+
+
+def mode_refgpu(a):
+    """The reference's GPU kernels (built from its source for sm_103a, driven as its BOINC app drives them) timed
+    on this GPU beside this build's kernels on the same inputs, stage by stage, with the rows compared:
+      screen  20,000 stars x 4,087 clusters (the benchmark chunk), work unit "PHYGAS 1 screen 25 64 2 0.001"
+      pairs   1 synthetic pulsar x 4,087 clusters (prefilter) x 100 clones, "PHYGAS 1 pair 100 0.05"."""
+    import numpy as np
+    import phygas_gb300 as pg
+    from phygas_gb300 import synth
+    import __graft_entry__
+    __graft_entry__.build()
+    out = {"mode": "refgpu"}
+    tmp = tempfile.mkdtemp(prefix="phygas_refgpu_")
+    cp, tp = synth.write_workload(tmp, "screen", a.stars or N_STARS, a.seed or SEED)
+    clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    tmax = max(c.tmax_myr for c in clusters)
+    wu = os.path.join(tmp, "wu_screen")
+    with open(tp) as f, open(wu, "w") as g:
+        g.write("PHYGAS 1 screen %g %d %g %g\n" % (CHI2_MAX, N_SAMP, R_KERNEL, P_MIN))
+        g.writelines(f.readlines())
+    with Clocks(0) as clk:
+        ref_rows, ref_t, ref_msg = _ref_gpu_run(cp, wu)
+    out["screen_reference_gpu"] = dict(ref_t, summary=ref_msg, clocks=clk.summary())
+    mine = {}
+    with pg.Context(0) as ctx:
+        ctx.set_clusters(clusters, N_SAMP, R_KERNEL)
+        ps0, sig, pre = pg.draw_targets(stars, N_SAMP)
+        for prec, name in ((pg.PGX_FP64, "fp64"), (pg.PGX_MIXED, "mixed")):
+            ctx.set_split(0 if prec == pg.PGX_FP64 else 8192)
+            ctx.stage(ps0, sig, pre)
+            ctx.exec(tmax, CHI2_MAX, prec)                    # warm-up
+            n = ctx.exec(tmax, CHI2_MAX, prec)
+            st = ctx.stats()
+            mine[name] = {k: r4(st[k]) for k in ("ms_total", "ms_orbit", "ms_cov", "ms_scan", "ms_select",
+                                                 "ms_finish")}
+            rows = ctx.fetch(n)
+        # the end-to-end call a user makes, for the app's whole-loop time
+        t0 = time.perf_counter()
+        ctx.screen_chunks(pg.as_array(stars, pg.PhTarget), 20000, tmax, lambda first, r: None, CHI2_MAX,
+                          pg.PGX_MIXED)
+        mine["e2e_s"] = r4(time.perf_counter() - t0)
+    out["screen_this_build_ms"] = mine
+    got = []
+    for r in rows[rows["p_r50"] >= P_MIN]:
+        t, c = stars[r["star"]], clusters[r["cluster"]]
+        got.append("%s %s %s %.3f %.3f %.2f %.2f %.4f %.4f %.2f" % (
+            t.id.decode(), c.name.decode(), c.kind.decode(), r["chi2"], r["t_myr"], r["d_nom_pc"], r["sig_pc"],
+            r["p_r50"], r["p_rtot"], r["vrel_kms"]))
+    key = lambda ln: tuple(ln.split()[:2])
+    kr, kg = {key(x): x for x in ref_rows}, {key(x): x for x in got}
+    out["screen_rows"] = {"reference_gpu": len(ref_rows), "this_build": len(got),
+                          "only_reference_gpu": len(set(kr) - set(kg)), "only_this_build": len(set(kg) - set(kr)),
+                          "identical_lines": sum(1 for k in set(kr) & set(kg) if kr[k] == kg[k])}
+    rt = ref_t
+    out["screen_stage_speedup"] = {
+        "orbits (pg_lin_k vs k_stm_orbits + k_stm_cov, FP64)": r4(rt["lin_s"] * 1e3 / (mine["fp64"]["ms_orbit"] +
+                                                                                      mine["fp64"]["ms_cov"])),
+        "chi2 (pg_chi2_k vs k_scan64, FP64)": r4(rt["chi2_s"] * 1e3 / mine["fp64"]["ms_scan"]),
+        "chi2 (pg_chi2_k vs k_mx_scan32 + the FP64 selection, mixed)": r4(
+            rt["chi2_s"] * 1e3 / (mine["mixed"]["ms_scan"] + mine["mixed"]["ms_select"])),
+        "finish (pg_finish_k vs k_finish64, FP64)": r4(rt["finish_s"] * 1e3 / mine["fp64"]["ms_finish"]),
+        "finish (pg_finish_k vs k_mx_finish32, mixed)": r4(rt["finish_s"] * 1e3 / mine["mixed"]["ms_finish"]),
+        "step (the app's loop vs the mixed device step)": r4(rt["total"] * 1e3 / mine["mixed"]["ms_total"]),
+        "end to end (the app's loop vs pgx_screen_chunks)": r4(rt["total"] / mine["e2e_s"])}
+    # pair mode: one synthetic pulsar against every cluster (the prefilter's pairs), 100 clones
+    pp = os.path.join(tmp, "pulsars.txt")
+    with open(pp, "w") as f:
+        f.write("\n".join(synth.pulsars(1, C3_SEED)) + "\n")
+    wu = os.path.join(tmp, "wu_pair")
+    with open(pp) as f, open(wu, "w") as g:
+        g.write("PHYGAS 1 pair 100 0.05\n" + f.read())
+    with Clocks(0) as clk:
+        ref_rows, ref_t, ref_msg = _ref_gpu_run(cp, wu)
+    out["pair_reference_gpu"] = dict(ref_t, summary=ref_msg, clocks=clk.summary())
+    pulsars = pg.read_targets(pp)
+    with pg.Context(0) as ctx:
+        ti, ci = ctx.prefilter(pulsars, clusters)
+        batch = pg.draw_pair_batch(pulsars, ti, clusters, ci, 100, 0.05)
+        ctx.pair(*batch)
+        res = ctx.pair(*batch)
+        st = ctx.stats()
+    got = ["%s %s %s %d %.3f %.3f %.3f %.4f %.4f %.4f %.2f %.2f %.2f %.4f %.4f" % (
+        pulsars[0].id.decode(), clusters[c].name.decode(), clusters[c].kind.decode(), r["n"], r["d05"], r["d50"],
+        r["d95"], r["t05"], r["t50"], r["t95"], r["v05"], r["v50"], r["v95"], r["f_r50"], r["f_rtot"])
+        for c, r in zip(ci.tolist(), res)]
+    out["pair_this_build_ms"] = {"ms_pair": r4(st["ms_pair"]), "clone_steps": int(st["clone_steps"])}
+    out["pair_rows"] = {"reference_gpu": len(ref_rows), "this_build": len(got),
+                        "identical_lines": sum(1 for x, y in zip(ref_rows, got) if x == y)}
+    out["pair_stage_speedup"] = {"clones (pg_pair_k vs k_pair_mc_t graph)": r4(ref_t["pair_s"] * 1e3 / st["ms_pair"])}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--mode", default="bench", choices=["bench", "screen", "pairs"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "screen", "pairs", "refgpu"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-pair", action="store_true", help="skip the batched Monte Carlo measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
@@ -612,6 +738,8 @@ def main():
     if args.mode == "pairs":
         args.stars = args.stars or 2000
         return mode_pairs(args)
+    if args.mode == "refgpu":
+        return mode_refgpu(args)
 
     import numpy as np
     import torch

@@ -232,6 +232,13 @@ int pgx_peaks(PgxContext *ctx, double *fp64_flops, double *fp32_flops);
 int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S, const double *R2, double chi2_max,
                      double *v64, float *lb, float *ub, int *rej);
 
+/* Self-check of the mixed-precision filter's block test (no counterpart in the reference): on the chunk staged by
+ * pgx_screen_stage (unsplit: pgx_screen_split(ctx, 0), or fewer stars than the split threshold), traces its tracks
+ * (tmax_myr), runs the block test on every (pair, block of 8 points) as the filter does, and evaluates the FP64 point
+ * chi2 of every point of each block it settles: counts[4] = blocks tested, blocks settled, points of settled blocks,
+ * violations (points under chi2_max; 0 when the test's bounds hold). */
+int pgx_check_blocks(PgxContext *ctx, double tmax_myr, double chi2_max, long *counts);
+
 /* Self-check of the mixed-precision finish's FP32 draws (no counterpart in the reference): for n pairs given by
  * fin11[11n] = (mx my mz, the covariance's Cholesky factor l00 l10 l20 l11 l21 l22, r50, rtot; kpc) and their draw
  * seeds, ratio[i] = the largest |x_j - x_j,64| / bound over the pair's 512 draws and three components, where x is

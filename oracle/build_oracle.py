@@ -6,7 +6,9 @@ Compiles oracle/'s C restatement of the reference's CPU algorithm with the refer
 no FP contraction) into oracle/_build/: libphygas_oracle.so, oracle_dump and oracle_wu.  When the reference's
 sources are present -- PHYGAS_REF, default /root/reference, the read-only checkout of the development container --
 it also compiles the reference itself from its own sources through `make -C oracle ref` into oracle/_ref/ (the pin
-of the restatement).  The GPU machine has no reference checkout; there only the restatement is built.
+of the restatement), and the reference's GPU kernels into oracle/_ref/ref_kernels.ptx (`make -C oracle ref-gpu-ptx`).
+The GPU machine has no reference checkout; there the restatement is built, and the reference-GPU comparator's host
+program (oracle/_build/ref_gpu, `make -C oracle ref-gpu`) when the PTX came with the repository.
 """
 import os
 import shutil
@@ -49,6 +51,12 @@ def build_oracle(reference=None):
     ref = reference if reference is not None else os.environ.get("PHYGAS_REF", "/root/reference")
     if ref and os.path.isdir(os.path.join(ref, "src")) and shutil.which("make"):
         _run(["make", "-s", "-C", ORACLE, "ref", "REF=" + ref])
+        _run(["make", "-s", "-C", ORACLE, "ref-gpu-ptx", "REF=" + ref])
+    # the reference-GPU comparator's host program, wherever the reference's kernels (PTX) came with the repository
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    if os.path.exists(os.path.join(ORACLE, "_ref", "ref_kernels.ptx")) and os.path.exists(
+            os.path.join(cuda, "include", "cuda.h")) and shutil.which("make"):
+        _run(["make", "-s", "-C", ORACLE, "ref-gpu", "CUDA=" + cuda])
 
 
 if __name__ == "__main__":

@@ -139,6 +139,7 @@ SIGNATURES = [
     ("pgx_check_bounds", C.c_int, [C.c_void_p, C.c_int, _D, _D, _D, C.c_double, _D, _P(C.c_float),
                                    _P(C.c_float), _I]),
     ("pgx_check_draws", C.c_int, [C.c_void_p, C.c_int, _D, _P(C.c_uint64), _D]),
+    ("pgx_check_blocks", C.c_int, [C.c_void_p, C.c_double, C.c_double, _P(C.c_long)]),
     ("pgx_control_targets", C.c_int, [_P(PhTarget), C.c_int, _P(PhTarget)]),
     ("pgx_server_open", C.c_int, [C.c_int, C.c_int, C.c_double, _P(PhCluster), C.c_int, C.c_int, C.c_double, C.c_int,
                                   _P(C.c_void_p)]),
@@ -275,6 +276,13 @@ class Context:
                                            _ptr(lb, C.c_float), _ptr(ub, C.c_float), _ptr(rej, C.c_int)),
                     "pgx_check_bounds")
         return v, lb, ub, rej
+
+    def check_blocks(self, tmax, chi2_max=25.0):
+        """The filter's block test on the staged (unsplit) chunk, each settled block's points checked in FP64
+        (pgx_check_blocks): {tested, settled, points, violations}."""
+        c = (C.c_long * 4)()
+        self._check(lib().pgx_check_blocks(self.h, tmax, chi2_max, c), "pgx_check_blocks")
+        return dict(zip(("tested", "settled", "points", "violations"), list(c)))
 
     def check_draws(self, fin11, seeds):
         """Per pair, the FP32 draws' largest error relative to their own bound (see pgx_check_draws)."""

@@ -56,7 +56,7 @@ constexpr double kPartPairs = 1.0e7;
 
 struct TrackSlot {
     int nt = 0, ns = 0;
-    Buf ps0, sig21, prefix, opos, ovel, t64, t32, tlm, ids;
+    Buf ps0, sig21, prefix, opos, ovel, t64, t32, tlm, ids, blk;
     // the inputs the slot's tracks and screen read: its own buffers, or a part of a split chunk
     const double *in_ps0 = nullptr, *in_sig21 = nullptr;
     const uint64_t *in_prefix = nullptr;
@@ -72,7 +72,10 @@ struct PgxContext {
     std::string err;
     // resident cluster table (original cluster order)
     int nc = 0, ncp = 0;
-    Buf c64, c32, clm, cn, cR2, cr50, crt, cname;
+    Buf c64, c32, clm, cn, cR2, cr50, crt, cname, cblk;
+    // the mixed filter's block test (one test settles eight points of a pair); PHYGAS_SCAN_BLOCKS=0 at pgx_open
+    // turns it off, so that every point is walked (the same rows either way)
+    bool scan_blocks = true;
     // the staged star chunks: two track slots, so that one chunk's orbits can run on the side stream while the
     // previous chunk is screened (pgx_screen_chunks); the single-chunk entry points use slot `cur`
     TrackSlot trk[2];
@@ -209,6 +212,10 @@ pgx::ScreenTables tables(PgxContext *ctx, TrackSlot &k) {
     T.c64 = P<double>(ctx->c64); T.c32 = P<float4>(ctx->c32); T.lm_c = P<float>(ctx->clm); T.cn = P<int>(ctx->cn);
     T.R2 = P<double>(ctx->cR2); T.r50 = P<double>(ctx->cr50); T.rtot = P<double>(ctx->crt);
     T.cname = P<char>(ctx->cname);
+    if (ctx->scan_blocks && k.blk.p && ctx->cblk.p) {
+        T.blk_t = P<float4>(k.blk);
+        T.blk_c = P<float4>(ctx->cblk);
+    }
     return T;
 }
 
@@ -267,6 +274,12 @@ int tracks_slot(PgxContext *ctx, int s, double tmax_myr, cudaStream_t st, bool t
     RET(ensure(ctx, k.tlm, (size_t)ns * nt * 4));
     RET(run_lin(ctx, st, nt, k.in_ps0, k.in_sig21, nullptr, ns, k.opos, k.ovel, P<double>(k.t64),
                 P<float4>(k.t32), P<float>(k.tlm), timed, orbit_blocks));
+    if (ctx->scan_blocks) {
+        RET(ensure(ctx, k.blk, (size_t)((ns + pgx::kBlockPoints - 1) / pgx::kBlockPoints) * nt * 64));
+        MRET(pgx::block_tables(st, nt, ns, nullptr, P<double>(k.t64), P<float>(k.tlm), nullptr, P<float4>(k.blk),
+                               ctx->mixed.err));
+        ctx->stats.kernels++;
+    }
     CK(cudaEventRecord(k.done, st));
     k.ns = ns;
     return 0;
@@ -397,6 +410,7 @@ int pgx_open(int device, PgxContext **out) {
     if (device >= n) return PGX_E_ARG;
     ctx = new PgxContext();
     ctx->device = device;
+    if (const char *e = getenv("PHYGAS_SCAN_BLOCKS")) ctx->scan_blocks = atoi(e) != 0;
     int rc = 0;
     {
         auto init = [&]() -> int {
@@ -655,6 +669,24 @@ int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S,
     return 0;
 }
 
+int pgx_check_blocks(PgxContext *ctx, double tmax_myr, double chi2_max, long *counts) {
+    if (!ctx) return PGX_E_ARG;
+    if (!counts || !(chi2_max > 0) || !(tmax_myr > 0)) return fail(ctx, PGX_E_ARG, "pgx_check_blocks: bad args");
+    if (ctx->nc <= 0 || ctx->nparts != 0 || ctx->trk[ctx->cur].nt <= 0)
+        return fail(ctx, PGX_E_ARG, "pgx_check_blocks: stage one unsplit chunk against a cluster table first");
+    if (!ctx->scan_blocks) return fail(ctx, PGX_E_ARG, "pgx_check_blocks: the block test is off (PHYGAS_SCAN_BLOCKS)");
+    CK(cudaSetDevice(ctx->device));
+    RET(tracks_slot(ctx, ctx->cur, tmax_myr, ctx->st, false));
+    RET(ensure(ctx, ctx->total, 64));
+    const pgx::ScreenTables T = tables(ctx, ctx->trk[ctx->cur]);
+    MRET(pgx::mixed_check_blocks(ctx->st, T, chi2_max, P<unsigned long long>(ctx->total), ctx->mixed.err));
+    unsigned long long h[4];
+    CK(cudaMemcpyAsync(h, ctx->total.p, sizeof h, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    for (int i = 0; i < 4; i++) counts[i] = (long)h[i];
+    return 0;
+}
+
 int pgx_check_draws(PgxContext *ctx, int n, const double *fin11, const uint64_t *seed, double *ratio) {
     if (!ctx) return PGX_E_ARG;
     if (n <= 0 || !fin11 || !seed || !ratio) return fail(ctx, PGX_E_ARG, "pgx_check_draws");
@@ -776,6 +808,9 @@ int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double
     ctx->ncp = nmax;
     MRET(pgx::mixed_cluster_aux(ctx->st, nc, nmax, P<int>(ctx->cn), P<double>(ctx->c64), P<double>(ctx->cR2),
                                P<float4>(ctx->c32), P<float>(ctx->clm), ctx->mixed));
+    RET(ensure(ctx, ctx->cblk, (size_t)((nmax + pgx::kBlockPoints - 1) / pgx::kBlockPoints) * nc * 64));
+    MRET(pgx::block_tables(ctx->st, nc, nmax, P<int>(ctx->cn), P<double>(ctx->c64), P<float>(ctx->clm),
+                           P<double>(ctx->cR2), P<float4>(ctx->cblk), ctx->mixed.err));
     CK(cudaStreamSynchronize(ctx->st));
     return 0;
 }

@@ -52,14 +52,19 @@ PGX_HD bool trace_far32(float a, float dd, float m00, float m11, float tr, float
 // worst case (PTX rcp.approx.f32: 1 ulp; rsqrt.approx.f32: relative error 2^-22.9; both over the full range).  The
 // .ftz forms flush subnormal arguments and results, which never occur here: every argument is checked or clamped to
 // be at least 1e-30, and a reciprocal's argument at most 1e30, so arguments and results are normal -- and they issue
-// as one special-function instruction, without the subnormal scaling around it.  Host builds use the exact operations, which the same margins cover.
+// as one special-function instruction, without the subnormal scaling around it.  Host builds use the exact operations,
+// which the same margins cover, scaled by (1 + host_fast_err): a host test sets it to put the results at either end
+// of the device units' error band (it is 0 otherwise, and does not exist in device code).
+#ifndef __CUDA_ARCH__
+inline float host_fast_err = 0.f;
+#endif
 PGX_HD float fast_rcp(float x) {
 #ifdef __CUDA_ARCH__
     float r;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 #else
-    return 1.f / x;
+    return 1.f / x * (1.f + host_fast_err);
 #endif
 }
 PGX_HD float fast_rsqrt(float x) {
@@ -68,7 +73,7 @@ PGX_HD float fast_rsqrt(float x) {
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 #else
-    return 1.f / sqrtf(x);
+    return 1.f / sqrtf(x) * (1.f + host_fast_err);
 #endif
 }
 
@@ -121,6 +126,73 @@ PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float lmt, 
     if (!(d > 0.f)) return false;
     const float r64 = kAdj64 * 3.f * (1.f + 16.f * kEps32) * tl * tl;
     return d * d * (1.f - r64) * (1.f - 8.f * kEps32) >= cut;
+}
+
+// ---- block culling: eight points of a pair settled by one test ---------------------------------------------------
+// A block is track points [8b, 8b + 8) of a pair with the segment end 8b + 8 (those that exist: k < n).  Per object
+// (star or cluster) and block, computed in FP64 from its track (k_block_tables), with km = 8b + 4 the position
+// reference and ke = min(8b + 8, n_obj - 1) the last point of the block's range:
+//   v, a     FP32 velocity and acceleration at km, and eps >= |p(k) - p(km) - v tau_k - a tau_k^2 / 2| over the range
+//            (tau_k = (km - k) h, h = 0.5 Myr: the track runs back in time) plus a h^2 / 8 for the chords between
+//            points, so every point the FP64 path evaluates for the block -- m0 at a track point, or its nearest
+//            point on a chord -- lies in the tube p(km) + v tau + a tau^2 / 2 + e, |e| <= eps, |tau| <= 4 h;
+//   S        an FP32 matrix that dominates S(k) (+ R^2 I for a cluster) at every point of the range: S(ke) + delta I,
+//            delta >= the largest eigenvalue of S(k) - S(ke) over the range (0 when the covariance only grows, as it
+//            mostly does going back in time), the FP32 rounding absorbed into delta;
+//   lam      <= lambda_min(S) (the point's FP64 lower bound at ke + delta, rounded down);
+//   lam_lo   <= lambda_min(S(k)) at every point of the range (the point bounds' minimum), for the adjugate's error.
+// For a pair, M(k) = S_t(k) + S_c(k) + R^2 I <= N = S_t + S_c (Loewner order), so x^T M(k)^-1 x >= x^T N^-1 x, and
+// every evaluated x = m_ref + dv tau + da tau^2 / 2 + e (m_ref = the separation at km, dv and da the differences)
+// has, by the triangle inequality in the N^-1 norm,
+//   |x|_N >= |m_ref|_N - 4h |dv|_N - 8h^2 |da|_N - (eps_t + eps_c + 3 eps |m_ref|) / sqrt(lam_t + lam_c).
+// The N^-1 forms come from one FP32 LDL^T with point_skip32's margins.  When the square of the bound, less the FP64
+// adjugate's rounding at M(k) (tr M(k) <= tr N, lambda_min M(k) >= lam_lo_t + lam_lo_c), is >= cut, every point of
+// the block has v >= cut: none can be a kept pair's minimum or bring the pair under the cut.
+constexpr int kBlk = 8;                       // points per block
+constexpr float kBlkTau = 2.0f;               // Myr: the largest |tau| in a block's tube (4 steps of 0.5 Myr)
+
+PGX_HD bool block_skip32(const float4 (&bt)[4], const float4 (&bc)[4], const float (&mref)[3], float cut) {
+    const float N0 = bt[2].x + bc[2].x, N1 = bt[2].y + bc[2].y, N2 = bt[2].z + bc[2].z;
+    const float N3 = bt[2].w + bc[2].w, N4 = bt[3].x + bc[3].x, N5 = bt[3].y + bc[3].y;
+    const float tr = N0 + N3 + N5;
+    const float lam = (bt[1].w + bc[1].w) * (1.f - 16.f * kEps32);
+    const float lam_lo = (bt[3].z + bc[3].z) * (1.f - 16.f * kEps32);
+    if (!(lam > 1e-30f && lam_lo > 1e-30f && N0 > 1e-30f && tr < 1e30f)) return false;
+    const float i1 = fast_rcp(N0);
+    const float l10 = N1 * i1, l20 = N2 * i1;
+    const float D2 = fmaf(-l10, N1, N3);
+    if (!(D2 > 1e-30f)) return false;
+    const float i2 = fast_rcp(D2);
+    const float uu = fmaf(-l20, N1, N4);
+    const float l21 = uu * i2;
+    const float D3 = fmaf(-l21, uu, fmaf(-l20, N2, N5));
+    if (!(D3 > 1e-30f)) return false;
+    const float i3 = fast_rcp(D3);
+    const float il = fast_rcp(lam);
+    const float tl = tr * il * (1.f + 8.f * kEps32);
+    const float rho = kSkipC1 * kEps32 * tl;
+    if (!(rho <= 0.25f)) return false;
+    const float dvx = bt[0].x - bc[0].x, dvy = bt[0].y - bc[0].y, dvz = bt[0].z - bc[0].z;
+    const float dax = bt[1].x - bc[1].x, day = bt[1].y - bc[1].y, daz = bt[1].z - bc[1].z;
+    const float qa = ldl_form(l10, l20, l21, i1, i2, i3, mref[0], mref[1], mref[2]);
+    const float qv = ldl_form(l10, l20, l21, i1, i2, i3, dvx, dvy, dvz);
+    const float qc = ldl_form(l10, l20, l21, i1, i2, i3, dax, day, daz);
+    // the differences dv, da are FP32 subtractions of the stored values (relative 1 eps each): 2 eps more
+    const float r = rho + 12.f * kEps32, rs = r + 2.f * kEps32;
+    const float m2 = fmaxf(fmaf(mref[0], mref[0], fmaf(mref[1], mref[1], mref[2] * mref[2])), 1e-30f);
+    const float mn = m2 * fast_rsqrt(m2) * (1.f + 8.f * kEps32);
+    const float sa = fmaxf(qa * (1.f - r), 1e-30f), sv = fmaxf(qv * (1.f + rs), 1e-30f),
+                sc = fmaxf(qc * (1.f + rs), 1e-30f);
+    const float e = (bt[0].w + bc[0].w) * (1.f + 4.f * kEps32) + 3.f * kEps32 * mn + 1e-12f;
+    const float d = sa * fast_rsqrt(sa) * (1.f - 8.f * kEps32) -
+                    kBlkTau * (sv * fast_rsqrt(sv)) * (1.f + 8.f * kEps32) -
+                    (0.5f * kBlkTau * kBlkTau) * (sc * fast_rsqrt(sc)) * (1.f + 8.f * kEps32) -
+                    e * fast_rsqrt(lam) * (1.f + 8.f * kEps32);
+    if (!(d > 0.f)) return false;
+    const float tlo = tr * fast_rcp(lam_lo) * (1.f + 8.f * kEps32);
+    const float r64 = kAdj64 * 3.f * (1.f + 16.f * kEps32) * tlo * tlo;
+    if (!(r64 < 0.5f)) return false;
+    return d * d * (1.f - r64) * (1.f - 12.f * kEps32) >= cut;
 }
 
 // Bounds on the FP64 path's point chi2 v = min(q(m0), q(ms)) -- the forms at the step's start and at the segment's

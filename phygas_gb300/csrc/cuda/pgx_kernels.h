@@ -28,6 +28,9 @@ struct McPairs {
     PhResultDev *res;         // per pair
 };
 
+// points per block of the mixed filter's block test (pgx_bounds32.cuh kBlk)
+constexpr int kBlockPoints = 8;
+
 // The screen's device tables.  Star tracks: FP64 t64[k][12][nt] (pos, vel, S) and FP32 t32[k][nt][3] float4
 // (pos hi, pos lo, S).  Cluster table: the same two layouts over nc, plus per cluster its point count, kernel
 // radius^2, r50 and rtot (kpc) and its name (for the pair seeds).
@@ -41,6 +44,9 @@ struct ScreenTables {
     const double *c64;
     const float4 *c32;               // the cluster table in FP32 with the kernel radius folded in: S + R^2 I
     const float *lm_c;               // [k][nc]: lower bound on lambda_min(S) + R^2 (FP32, rounded down)
+    // per object and block of kBlockPoints points, the block test's data ([b][n][4] float4, pgx_bounds32.cuh
+    // block_skip32); nullptr: the mixed filter walks every point
+    const float4 *blk_t = nullptr, *blk_c = nullptr;
     const int *cn;
     const double *R2, *r50, *rtot;
     const char *cname;               // nc * 40 bytes

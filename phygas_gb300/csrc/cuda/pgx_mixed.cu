@@ -33,6 +33,8 @@
 
 namespace pgx {
 
+static_assert(kBlk == kBlockPoints, "the block tables and the filter's block test agree on the block size");
+
 int grow(DevBuf &b, size_t bytes, std::string &err) {
     if (bytes == 0) bytes = 16;
     if (b.cap >= bytes) return 0;
@@ -118,6 +120,91 @@ int mixed_cluster_aux(cudaStream_t st, int nc, int nmax, const int *cn, const do
     return check(cudaGetLastError(), m.err, "k_fold_r2");
 }
 
+// ---- block tables: per object (star or cluster) and block of kBlk points, the data block_skip32 reads --------------
+// t64 [k][12][N] (pos, vel, S), lm [k][N] (FP32 lower bounds on lambda_min(S), with R^2 for the clusters), npts[i]
+// points (nullptr: nmax for every object), R2[i] on the diagonal of S (clusters; nullptr for stars).  Out: blk
+// [b][N][4] float4 = (v, eps) (a, lam) (S0 S1 S2 S3) (S4 S5 lam_lo 0), as pgx_bounds32.cuh describes; a block whose
+// position reference km = kBlk b + kBlk/2 lies past the object's track is zeroed (no pair tests it: a pair tests
+// block b only when km < its point count, which is at most the object's).
+__global__ void k_block_tables(int N, int nmax, const int *__restrict__ npts, const double *__restrict__ t64,
+                               const float *__restrict__ lm, const double *__restrict__ R2,
+                               float4 *__restrict__ blk) {
+    const int nblk = (nmax + kBlk - 1) / kBlk;
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)N * nblk) return;
+    const size_t NN = N;
+    const int i = (int)(idx % NN), b = (int)(idx / NN);
+    const int n = npts ? npts[i] : nmax;
+    float4 *o = blk + ((size_t)b * NN + i) * 4;
+    const int km = b * kBlk + kBlk / 2;
+    if (km >= n) {
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        o[0] = z; o[1] = z; o[2] = z; o[3] = z;
+        return;
+    }
+    const int k0 = b * kBlk, ke = min(b * kBlk + kBlk, n - 1);
+    auto at = [&](int k, int f) { return t64[((size_t)k * 12 + f) * NN + i]; };
+    const double h = kStepMyr;
+    // velocity and acceleration at km in FP32: the tube is measured against the stored values themselves
+    const int kp = min(km + 1, n - 1), kq = km - 1;
+    float v32[3], a32[3];
+    for (int c = 0; c < 3; c++) {
+        v32[c] = (float)at(km, 3 + c);
+        a32[c] = (float)((at(kq, 3 + c) - at(kp, 3 + c)) / ((double)(kp - kq) * h));
+    }
+    const double pm[3] = {at(km, 0), at(km, 1), at(km, 2)};
+    double e2 = 0.0;
+    for (int k = k0; k <= ke; k++) {
+        const double tau = (double)(km - k) * h;
+        double s = 0.0;
+        for (int c = 0; c < 3; c++) {
+            const double d = at(k, c) - pm[c] - (double)v32[c] * tau - 0.5 * (double)a32[c] * tau * tau;
+            s += d * d;
+        }
+        e2 = fmax(e2, s);
+    }
+    const double an = sqrt((double)a32[0] * a32[0] + (double)a32[1] * a32[1] + (double)a32[2] * a32[2]);
+    // the residual (FP64: rounding far below the margins), and the chords between points, a h^2 / 8
+    const double eps = sqrt(e2) * (1.0 + 1e-12) + 1e-13 + 0.125 * an * h * h * (1.0 + 1e-12);
+    // covariance: S(ke) dominates the range after delta >= the largest eigenvalue of S(k) - S(ke) is added
+    const double r2 = R2 ? R2[i] : 0.0;
+    double Se[6];
+    for (int q = 0; q < 6; q++) Se[q] = at(ke, 6 + q);
+    Se[0] += r2; Se[3] += r2; Se[5] += r2;
+    double delta = 0.0;
+    float lam_lo = __int_as_float(0x7f800000);
+    for (int k = k0; k <= ke; k++) {
+        if (k < ke) {
+            double D[6];
+            for (int q = 0; q < 6; q++) D[q] = at(k, 6 + q) - at(ke, 6 + q);
+            // lambda_max(D) = -lambda_min(-D) <= -(a lower bound on lambda_min(-D))
+            const double up = -sym3_min_eig_lb(-D[0], -D[1], -D[2], -D[3], -D[4], -D[5]);
+            delta = fmax(delta, up);
+        }
+        lam_lo = fminf(lam_lo, lm[(size_t)k * NN + i]);
+    }
+    // S(ke) + (delta + r) I rounded to FP32: each entry's rounding is within 2^-24 of its magnitude, so the rounding
+    // error E has ||E|| <= 3 * 2^-24 (mx + r) < r: the stored matrix still dominates S(ke) + delta I
+    double mx = 0.0;
+    for (int q = 0; q < 6; q++) mx = fmax(mx, fabs(Se[q]));
+    mx += delta;
+    const double r = 4.0 * 5.9604644775390625e-8 * mx;
+    double Sd[6] = {Se[0] + delta + r, Se[1], Se[2], Se[3] + delta + r, Se[4], Se[5] + delta + r};
+    const float lam = __double2float_rd((double)lm[(size_t)ke * NN + i] + delta);
+    o[0] = make_float4(v32[0], v32[1], v32[2], __double2float_ru(eps));
+    o[1] = make_float4(a32[0], a32[1], a32[2], lam);
+    o[2] = make_float4((float)Sd[0], (float)Sd[1], (float)Sd[2], (float)Sd[3]);
+    o[3] = make_float4((float)Sd[4], (float)Sd[5], lam_lo, 0.f);
+}
+
+int block_tables(cudaStream_t st, int N, int nmax, const int *npts, const double *t64, const float *lm,
+                 const double *R2, float4 *blk, std::string &err) {
+    const size_t work = (size_t)N * ((nmax + kBlk - 1) / kBlk);
+    if (work == 0) return 0;
+    k_block_tables<<<(unsigned)((work + 127) / 128), 128, 0, st>>>(N, nmax, npts, t64, lm, R2, blk);
+    return check(cudaGetLastError(), err, "k_block_tables");
+}
+
 // separation of star and cluster at one point from the split FP32 positions
 __device__ __forceinline__ void sep32(const float4 &t0, const float4 &t1, const float4 &c0, const float4 &c1,
                                       float (&m)[3]) {
@@ -162,19 +249,24 @@ __device__ __forceinline__ bool point_at32(const ScreenTables &T, int s, int c, 
                          more, cut, b);
 }
 
-// One block: kScanStars stars x one cluster; a warp walks its 32 pairs' points in step.  Clusters are the grid's fast
-// axis, so the blocks resident at one time share one block of stars, whose track data stays in L2.
-// Each lane runs the cheap test (point_skip32) on its point; the few points it cannot settle are queued per warp in
-// shared memory and given their full bounds 32 at a time, one per lane, so the long evaluation runs on full warps
-// instead of diverging on most steps; the owner lane then folds the results into its pair's state.  The state (min
-// ub and the candidate slots) does not depend on the order the points are folded in.
-// six resident blocks per SM asked of the compiler (80 registers, a 4-byte spill): 24 warps to issue from, where 95
-// registers left 20; the kernel is issue-bound and runs 7 % faster so (5, 7 and 8 blocks measured slower)
+// One block: kScanStars stars x one cluster; a warp walks its 32 pairs in step.  Clusters are the grid's fast axis,
+// so the blocks resident at one time share one block of stars, whose track data stays in L2.
+// The walk has two levels.  First a block test per lane (block_skip32, with the block tables): one test settles the
+// eight points of a block -- most blocks of most pairs.  The blocks it cannot settle are queued per warp in shared
+// memory and walked 32 at a time, one per lane (different pairs and blocks), point by point: each point gets the
+// cheap point test (point_skip32), and the few points it cannot settle either are queued again, per warp, for their
+// full bounds, 32 at a time on full warps.  The owner lane of each point then folds the results into its pair's state
+// (min ub and the candidate slots), which does not depend on the order the points are folded in.  Points past the
+// last testable block (fewer than five left) are walked by every lane in step, as are all points when the tables
+// have no block data.  A settled block's points all have chi2 >= cut in the FP64 path: they can neither be a kept
+// pair's minimum nor bring a pair under the cut, and they are left out of min ub, which only admits more candidates.
+// six resident blocks per SM asked of the compiler: 24 warps to issue from; the kernel is issue-bound
 __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32(ScreenTables T, float cut,
                                                              unsigned char *__restrict__ flag,
                                                              float *__restrict__ ubmin,
                                                              unsigned long long *__restrict__ klist) {
-    __shared__ int s_q[kScanStars / 32][kQueue];
+    __shared__ int s_q[kScanStars / 32][kQueue];                  // points waiting for their full bounds
+    __shared__ int s_bq[kScanStars / 32][kQueue];                 // blocks waiting to be walked point by point
     __shared__ float s_lb[kScanStars / 32][32], s_ub[kScanStars / 32][32];
     __shared__ unsigned s_own[kScanStars / 32][32];                // per owner lane: its entries of the drain
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, c = blockIdx.x;
@@ -219,28 +311,11 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32(ScreenTables T, flo
         }
         __syncwarp();
     };
-    const size_t NT = T.nt, NC = T.nc;
-    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
-    const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
-    float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
-    float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2);
-    float mcur[3];
-    sep32(t0, t1, c0, c1, mcur);
     int qn = 0;
-    for (int k = 0; k < n; k++) {
-        const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
-        const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
-        const float lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
-        float mnext[3] = {mcur[0], mcur[1], mcur[2]};
-        if (k + 1 < n) {
-            const float4 *tn = tp + (size_t)(k + 1) * NT * 3, *cn = cp + (size_t)(k + 1) * NC * 3;
-            t0 = tn[0]; t1 = tn[1]; t2 = tn[2];
-            c0 = __ldg(cn); c1 = __ldg(cn + 1); c2 = __ldg(cn + 2);
-            sep32(t0, t1, c0, c1, mnext);
-        }
-        const bool need = active && !point_skip32(St, Sc, lmt, lmc, mcur, mnext, cut);
+    // every lane in step: its entry (owner | k << 5) when `need`, draining 32 at a time
+    auto push_point = [&](bool need, int entry) {
         const unsigned mask = __ballot_sync(0xffffffffu, need);
-        if (need) s_q[w][qn + __popc(mask & ((1u << lane) - 1u))] = lane | (k << 5);
+        if (need) s_q[w][qn + __popc(mask & ((1u << lane) - 1u))] = entry;
         qn += __popc(mask);
         if (qn >= 32) {
             drain(32);
@@ -250,7 +325,104 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32(ScreenTables T, flo
             if (lane < rest) s_q[w][lane] = v;
             qn = rest;
         }
-        mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
+    };
+    const size_t NT = T.nt, NC = T.nc;
+    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
+    // the point test of point k of star st's pair (its separations at k and k + 1 in mc / mn), as every walk runs it
+    auto point_needs = [&](int st, int k, const float4 &t1, const float4 &t2, const float4 &c1, const float4 &c2,
+                           const float (&mc)[3], const float (&mn)[3]) {
+        const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+        const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
+        const float lmt = T.lm_t[(size_t)k * NT + st], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
+        return !point_skip32(St, Sc, lmt, lmc, mc, mn, cut);
+    };
+    // ---- level 1: blocks of kBlk points whose position reference km = kBlk b + kBlk/2 lies on the pair's track
+    const int nbt = (T.blk_t && T.blk_c && n > kBlk / 2) ? (n - kBlk / 2 - 1) / kBlk + 1 : 0;
+    if (nbt > 0) {
+        // walk the queued blocks [0, cnt) point by point, one block per lane
+        auto walk_blocks = [&](int cnt) {
+            __syncwarp();
+            const int e = lane < cnt ? s_bq[w][lane] : 0;
+            const int o = e & 31, b = e >> 5, st = s0 + o;
+            const int k0 = b * kBlk, k1 = min(k0 + kBlk, n);
+            const float4 *tp = T.t32 + (size_t)st * 3, *cp = T.c32 + (size_t)c * 3;
+            float4 t0, t1, t2, c0, c1, c2;
+            float mc[3] = {0.f, 0.f, 0.f};
+            if (lane < cnt) {
+                const float4 *a = tp + (size_t)k0 * NT * 3, *q = cp + (size_t)k0 * NC * 3;
+                t0 = a[0]; t1 = a[1]; t2 = a[2];
+                c0 = __ldg(q); c1 = __ldg(q + 1); c2 = __ldg(q + 2);
+                sep32(t0, t1, c0, c1, mc);
+            }
+            for (int j = 0; j < kBlk; j++) {
+                const int k = k0 + j;
+                const bool valid = lane < cnt && k < k1;
+                bool need = false;
+                if (valid) {
+                    const float4 T1 = t1, T2 = t2, C1 = c1, C2 = c2;
+                    float mn[3] = {mc[0], mc[1], mc[2]};
+                    if (k + 1 < n) {
+                        const float4 *a = tp + (size_t)(k + 1) * NT * 3, *q = cp + (size_t)(k + 1) * NC * 3;
+                        t0 = a[0]; t1 = a[1]; t2 = a[2];
+                        c0 = __ldg(q); c1 = __ldg(q + 1); c2 = __ldg(q + 2);
+                        sep32(t0, t1, c0, c1, mn);
+                    }
+                    need = point_needs(st, k, T1, T2, C1, C2, mc, mn);
+                    mc[0] = mn[0]; mc[1] = mn[1]; mc[2] = mn[2];
+                }
+                push_point(need, o | (k << 5));
+            }
+        };
+        int bn = 0;
+        const float4 *bt = T.blk_t + (size_t)s * 4, *bc = T.blk_c + (size_t)c * 4;
+        for (int b = 0; b < nbt; b++) {
+            bool need = false;
+            if (active) {
+                const int km = b * kBlk + kBlk / 2;
+                const float4 *a = bt + (size_t)b * NT * 4, *q = bc + (size_t)b * NC * 4;
+                const float4 BT[4] = {a[0], a[1], a[2], a[3]};
+                const float4 BC[4] = {__ldg(q), __ldg(q + 1), __ldg(q + 2), __ldg(q + 3)};
+                const float4 *tm = T.t32 + ((size_t)km * NT + s) * 3, *cm = T.c32 + ((size_t)km * NC + c) * 3;
+                float mref[3];
+                sep32(tm[0], tm[1], __ldg(cm), __ldg(cm + 1), mref);
+                need = !block_skip32(BT, BC, mref, cut);
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, need);
+            if (need) s_bq[w][bn + __popc(mask & ((1u << lane) - 1u))] = lane | (b << 5);
+            bn += __popc(mask);
+            if (bn >= 32) {
+                walk_blocks(32);
+                const int rest = bn - 32;
+                const int v = lane < rest ? s_bq[w][32 + lane] : 0;
+                __syncwarp();
+                if (lane < rest) s_bq[w][lane] = v;
+                bn = rest;
+            }
+        }
+        if (bn > 0) walk_blocks(bn);
+    }
+    // ---- level 0: the points after the tested blocks, every lane in step
+    const int kt = nbt * kBlk;
+    if (kt < n) {
+        const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
+        const float4 *a = tp + (size_t)kt * NT * 3, *q = cp + (size_t)kt * NC * 3;
+        float4 t0 = a[0], t1 = a[1], t2 = a[2];
+        float4 c0 = __ldg(q), c1 = __ldg(q + 1), c2 = __ldg(q + 2);
+        float mcur[3];
+        sep32(t0, t1, c0, c1, mcur);
+        for (int k = kt; k < n; k++) {
+            const float4 T1 = t1, T2 = t2, C1 = c1, C2 = c2;
+            float mnext[3] = {mcur[0], mcur[1], mcur[2]};
+            if (k + 1 < n) {
+                const float4 *tn = tp + (size_t)(k + 1) * NT * 3, *cn = cp + (size_t)(k + 1) * NC * 3;
+                t0 = tn[0]; t1 = tn[1]; t2 = tn[2];
+                c0 = __ldg(cn); c1 = __ldg(cn + 1); c2 = __ldg(cn + 2);
+                sep32(t0, t1, c0, c1, mnext);
+            }
+            const bool need = active && point_needs(s, k, T1, T2, C1, C2, mcur, mnext);
+            push_point(need, lane | (k << 5));
+            mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
+        }
     }
     if (qn > 0) drain(qn);
     if (!active) return;
@@ -787,9 +959,11 @@ __device__ __forceinline__ void draw32(const Fin32 &g, uint64_t w, float &x, flo
 
 // The 512 draws of a kept pair, in two phases.  A draw's first coordinate x = mx + l00 z0 depends on its first
 // Gaussian alone, and |x| >= max(r50, rtot) puts the draw outside both spheres whatever z1 and z2 are (r >= |x|, in
-// the FP64 path's arithmetic as well).  Phase 1 draws z0 for all 512 and settles the draws whose x, less its error
-// bound (4 eps |mx| + |l00| (4 eps |z0| + e0 (1 + 2 eps)), the x row of draw32's bound), clears the larger radius;
-// with sigma of hundreds of pc against radii of tens, most do.  The rest are queued per warp in shared memory with
+// the FP64 path's arithmetic as well).  Phase 1 settles most draws with one generator output each: level A (below)
+// settles a draw from its u1 alone when even |z0| = sqrt(-2 ln u1) keeps x clear of both radii; the others get z0
+// (level B) and are settled when x, less its error bound (4 eps |mx| + |l00| (4 eps |z0| + e0 (1 + 2 eps)), the x
+// row of draw32's bound), clears the larger radius; with sigma of hundreds of pc against radii of tens, most do.
+// The rest are queued per warp in shared memory with
 // z0 and its bound, and phase 2 completes them 32 at a time on full warps: z1, z2, the position and its bound as
 // draw32 computes them, and the FP64 recheck of a draw within its bound of a radius -- the counts are the FP64
 // path's, and the same as drawing every draw in full.
@@ -800,6 +974,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
                                                                 int *__restrict__ nrecheck) {
     __shared__ int s_i[kFinWarps][kFinQueue];
     __shared__ float s_z[kFinWarps][kFinQueue], s_a[kFinWarps][kFinQueue], s_e[kFinWarps][kFinQueue];
+    __shared__ int s_ia[kFinWarps][kFinQueue];                   // level A: draws left open, and their first output
+    __shared__ uint64_t s_ga[kFinWarps][kFinQueue];
     const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
     if (h >= n) return;                                           // the whole warp: uniform
     const Fin32 g = fin32(fin[h], lane);
@@ -840,20 +1016,41 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
         }
         __syncwarp();
     };
-    // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden
-    uint64_t w = seed + (uint64_t)(6 * lane) * kGolden;
-    int qn = 0;
-#pragma unroll 1
-    for (int q = 0; q < 16; q++, w += 192 * kGolden) {
-        float z0, a0, e0;
-        gauss32(splitmix_mix(w + kGolden), splitmix_mix(w + 2 * kGolden), z0, a0, e0);
-        const float x = fmaf(g.l00, z0, g.mx);
-        const float ex0 = fmaf(eA0, a0, fmaf(eE0, e0, eM0));
-        const bool open = !(fabsf(x) * (1.f - 4.f * kEps32) - ex0 >= rout);
+    // Level A, before any transcendental: |z0| <= sqrt(-2 ln u1) in the FP64 path, so a draw whose u1 is at least
+    // U* = exp(-R*^2 / 2), R* = (|mx| - max(r50, rtot)) / |l00|, has |x| >= max(r50, rtot) whatever its angle: outside
+    // both spheres.  U* is taken in FP64 once per pair with relative margins of 1e-12 on R* and 1e-10 on R*^2 (far
+    // above the FP64 log's and exp's last-bit errors and the rounding of x = mx + l00 z0), and the test is an integer
+    // compare of u1's 53 bits with ceil(U* 2^53).  The draws it cannot settle are queued (index, first generator
+    // output) and get the z0 test above 32 at a time on full warps.
+    uint64_t kstar = (1ull << 53) + 1;                           // no draw settles at level A
+    {
+        const double mxa = fabs(fin[h].mx), l00a = fabs(fin[h].l00), ro = fmax(fin[h].r50, fin[h].rt);
+        if (mxa > ro) {
+            const double R = (mxa - ro) / l00a * (1.0 - 1e-12);
+            const double U = exp(-0.5 * R * R * (1.0 - 1e-10)) * (1.0 + 1e-12);
+            if (U < 1.0) kstar = (uint64_t)ceil(U * 9007199254740992.0);
+        }
+    }
+    int qn = 0, an = 0;
+    // level B for level-A queue entries [0, cnt), one per lane: z0 and its bound; the draws still open go to the
+    // phase-2 queue
+    auto level_b = [&](int cnt) {
+        __syncwarp();
+        bool open = false;
+        int i = 0;
+        float z0 = 0.f, a0 = 0.f, e0 = 0.f;
+        if (lane < cnt) {
+            i = s_ia[wq][lane];
+            const uint64_t w = seed + (uint64_t)(6 * i) * kGolden;
+            gauss32(s_ga[wq][lane], splitmix_mix(w + 2 * kGolden), z0, a0, e0);
+            const float x = fmaf(g.l00, z0, g.mx);
+            const float ex0 = fmaf(eA0, a0, fmaf(eE0, e0, eM0));
+            open = !(fabsf(x) * (1.f - 4.f * kEps32) - ex0 >= rout);
+        }
         const unsigned m = __ballot_sync(0xffffffffu, open);
         if (open) {
             const int at = qn + __popc(m & ((1u << lane) - 1u));
-            s_i[wq][at] = lane + 32 * q;
+            s_i[wq][at] = i;
             s_z[wq][at] = z0;
             s_a[wq][at] = a0;
             s_e[wq][at] = e0;
@@ -873,7 +1070,33 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
             }
             qn = rest;
         }
+        __syncwarp();
+    };
+    // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden
+    uint64_t w = seed + (uint64_t)(6 * lane) * kGolden;
+#pragma unroll 1
+    for (int q = 0; q < 16; q++, w += 192 * kGolden) {
+        const uint64_t ga = splitmix_mix(w + kGolden);
+        const bool open = (ga >> 11) < kstar;
+        const unsigned m = __ballot_sync(0xffffffffu, open);
+        if (open) {
+            const int at = an + __popc(m & ((1u << lane) - 1u));
+            s_ia[wq][at] = lane + 32 * q;
+            s_ga[wq][at] = ga;
+        }
+        an += __popc(m);
+        if (an >= 32) {
+            level_b(32);
+            const int rest = an - 32;
+            int vi = 0;
+            uint64_t vg = 0;
+            if (lane < rest) { vi = s_ia[wq][32 + lane]; vg = s_ga[wq][32 + lane]; }
+            __syncwarp();
+            if (lane < rest) { s_ia[wq][lane] = vi; s_ga[wq][lane] = vg; }
+            an = rest;
+        }
     }
+    if (an > 0) level_b(an);
     if (qn > 0) complete(qn);
     in50 = __reduce_add_sync(0xffffffffu, in50);
     intot = __reduce_add_sync(0xffffffffu, intot);
@@ -974,5 +1197,59 @@ int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *
                        double *v64, float *lb, float *ub, int *rej, std::string &err) {
     k_mx_check_bounds<<<(n + 127) / 128, 128, 0, st>>>(n, pos, S, R2, cut, v64, lb, ub, rej);
     return check(cudaGetLastError(), err, "k_mx_check_bounds");
+}
+
+// Self-check of the block test on a staged chunk: every (pair, testable block) gets block_skip32 as the filter runs
+// it, and every point of a block it settles gets the FP64 path's point chi2 (pgx_screen_math.cuh): a point under the
+// cut there is a violation.  cnt: blocks tested, blocks settled, points of settled blocks, violations.
+__global__ void k_mx_check_blocks(ScreenTables T, double cut, unsigned long long *__restrict__ cnt) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t NT = T.nt, NC = T.nc;
+    if (p >= NT * NC) return;
+    const int s = (int)(p % NT), c = (int)(p / NT);
+    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
+    const int nbt = n > kBlk / 2 ? (n - kBlk / 2 - 1) / kBlk + 1 : 0;
+    unsigned long long tested = 0, settled = 0, points = 0, bad = 0;
+    const double R2 = T.R2[c];
+    for (int b = 0; b < nbt; b++) {
+        const int km = b * kBlk + kBlk / 2;
+        const float4 *a = T.blk_t + ((size_t)b * NT + s) * 4, *q = T.blk_c + ((size_t)b * NC + c) * 4;
+        const float4 BT[4] = {a[0], a[1], a[2], a[3]};
+        const float4 BC[4] = {q[0], q[1], q[2], q[3]};
+        const float4 *tm = T.t32 + ((size_t)km * NT + s) * 3, *cm = T.c32 + ((size_t)km * NC + c) * 3;
+        float mref[3];
+        sep32(tm[0], tm[1], cm[0], cm[1], mref);
+        tested++;
+        if (!block_skip32(BT, BC, mref, (float)cut)) continue;
+        settled++;
+        for (int k = b * kBlk; k < min(b * kBlk + kBlk, n); k++) {
+            const double *tk = T.t64 + (size_t)k * 12 * NT + s, *ck = T.c64 + (size_t)k * 12 * NC + c;
+            double M[6], m0[3], m1[3], sv;
+            for (int i = 0; i < 6; i++) M[i] = tk[(6 + i) * NT] + ck[(6 + i) * NC];
+            for (int i = 0; i < 3; i++) m0[i] = tk[i * NT] - ck[i * NC];
+            const bool more = k + 1 < n;
+            for (int i = 0; i < 3; i++) m1[i] = more ? tk[(12 + i) * NT] - ck[(12 + i) * NC] : m0[i];
+            const double v = point_chi2_64(M, R2, m0, m1, more, cut, sv);
+            points++;
+            bad += v >= 0 && v < cut;
+        }
+    }
+    atomicAdd(cnt, tested);
+    atomicAdd(cnt + 1, settled);
+    atomicAdd(cnt + 2, points);
+    atomicAdd(cnt + 3, bad);
+}
+
+int mixed_check_blocks(cudaStream_t st, const ScreenTables &T, double cut, unsigned long long *cnt,
+                       std::string &err) {
+    if (!T.blk_t || !T.blk_c) {
+        err = "no block tables";
+        return PGX_E_ARG;
+    }
+    int rc = check(cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), st), err, "memset");
+    if (rc) return rc;
+    const size_t pairs = (size_t)T.nt * T.nc;
+    k_mx_check_blocks<<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(T, cut, cnt);
+    return check(cudaGetLastError(), err, "k_mx_check_blocks");
 }
 }  // namespace pgx

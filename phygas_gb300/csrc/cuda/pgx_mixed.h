@@ -29,6 +29,10 @@ int gather_columns(cudaStream_t st, int nc, int nmax, const int *order_host, con
 // the kernel radius folded into the FP32 cluster table the filter reads: S + R^2 I and lmin + R^2 (once per table)
 int mixed_cluster_aux(cudaStream_t st, int nc, int nmax, const int *cn, const double *c64, const double *R2,
                       float4 *c32, float *clm, MixedBufs &m);
+// the block tables of N objects' tracks (t64 [k][12][N], lm [k][N], npts[i] points or nmax for all, R2[i] on S's
+// diagonal or none) into blk [ceil(nmax / kBlk)][N][4] float4: what the filter's block test reads
+int block_tables(cudaStream_t st, int N, int nmax, const int *npts, const double *t64, const float *lm,
+                 const double *R2, float4 *blk, std::string &err);
 // FP32 filter + FP64 recheck: the kept pairs in (star, cluster) order, identical to the FP64 path's
 int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &m, cudaEvent_t ev_scan, int *total,
                  PgxStats *stats);
@@ -41,5 +45,7 @@ int mixed_finish(cudaStream_t st, int n, const FinishIn *fin, ScreenRowDev *rows
 int mixed_check_draws(cudaStream_t st, int n, const FinishIn *fin, double *ratio, std::string &err);
 int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *S, const double *R2, double cut,
                        double *v64, float *lb, float *ub, int *rej, std::string &err);
+// self-check of the filter's block test on the staged chunk's tracks (pgx_check_blocks): cnt[4] on the device
+int mixed_check_blocks(cudaStream_t st, const ScreenTables &T, double cut, unsigned long long *cnt, std::string &err);
 
 }  // namespace pgx

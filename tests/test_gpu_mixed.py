@@ -115,3 +115,49 @@ def test_cli_control_run_mixed_equals_fp64(built):
                                        stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, check=True).stdout)
     assert outs[0] == outs[1]
     assert len(outs[0].splitlines()) > 1000
+
+
+def test_block_test_is_sound_and_settles_most_blocks(ctx):
+    """The filter's block test (one test for eight points of a pair) on the tracks of 768 synthetic stars x 4,087
+    clusters of the benchmark workload: every point of every block it settles has the FP64 path's chi2 >= the cut
+    (pgx_check_blocks evaluates each in FP64), and it settles most blocks."""
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "screen", 768, 1001)
+        clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    tmax = max(c.tmax_myr for c in clusters)
+    ctx.set_clusters(clusters)
+    ctx.set_split(0)
+    try:
+        ctx.stage(*pg.draw_targets(stars))
+        for cut in (25.0, 9.0, 100.0):
+            r = ctx.check_blocks(tmax, cut)
+            assert r["violations"] == 0, (cut, r)
+            assert r["settled"] > 0.6 * r["tested"], (cut, r)
+    finally:
+        ctx.set_split(8192)
+
+
+def test_block_test_changes_no_row(built):
+    """The same chunk with the block test and with every point walked (PHYGAS_SCAN_BLOCKS=0): identical rows."""
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "screen", 512, 1002)
+        clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    tmax = max(c.tmax_myr for c in clusters)
+    draws = pg.draw_targets(stars)
+    rows = {}
+    old = os.environ.get("PHYGAS_SCAN_BLOCKS")
+    try:
+        for flag in ("1", "0"):
+            os.environ["PHYGAS_SCAN_BLOCKS"] = flag
+            with pg.Context(0) as c:
+                c.set_clusters(clusters)
+                rows[flag] = c.screen(*draws, tmax, 25.0, pg.PGX_MIXED)
+                if flag == "1":
+                    rows["fp64"] = c.screen(*draws, tmax, 25.0, pg.PGX_FP64)
+    finally:
+        if old is None:
+            os.environ.pop("PHYGAS_SCAN_BLOCKS", None)
+        else:
+            os.environ["PHYGAS_SCAN_BLOCKS"] = old
+    assert len(rows["1"]) > 1000
+    assert rows["1"].tobytes() == rows["0"].tobytes() == rows["fp64"].tobytes()

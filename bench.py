@@ -170,13 +170,14 @@ def cpu_baseline(cp, tp, stars_per_proc=192, procs=None, keep_rows=False):
     env = dict(os.environ)
     if keep_rows:
         env["PHYGAS_WU_RAW"] = "1"
+    # each process writes its rows to a file of its own (pipes read one after another would hold the others up)
+    outf = [open(os.path.join(tmp, "rows%d" % p), "wb") if keep_rows else subprocess.DEVNULL for p in range(procs)]
     t0 = time.time()
     ps = [subprocess.Popen([ot.ORACLE_WU, cp, inp, str(p * stars_per_proc), str((p + 1) * stars_per_proc)],
-                           stdout=subprocess.PIPE if keep_rows else subprocess.DEVNULL, stderr=subprocess.PIPE,
-                           env=env) for p in range(procs)]
+                           stdout=outf[p], stderr=subprocess.PIPE, env=env) for p in range(procs)]
     runs, preps, outs = [], [], []
-    for p in ps:
-        out, err = p.communicate()
+    for i, p in enumerate(ps):
+        _, err = p.communicate()
         err = err.decode(errors="replace")
         if p.returncode:
             raise RuntimeError("oracle_wu failed: " + err[-500:])
@@ -184,7 +185,9 @@ def cpu_baseline(cp, tp, stars_per_proc=192, procs=None, keep_rows=False):
         preps.append(float(f[1]))
         runs.append(float(f[3]))
         if keep_rows:
-            outs.append(out)
+            outf[i].close()
+            with open(os.path.join(tmp, "rows%d" % i), "rb") as g:
+                outs.append(g.read())
     wall = time.time() - t0
     pairs = stars_per_proc * procs * N_CLUSTERS
     res = {"value": pairs / max(runs), "unit": "pairs/s", "cores": procs, "kind": "port",

@@ -73,9 +73,9 @@ struct PgxContext {
     // resident cluster table (original cluster order)
     int nc = 0, ncp = 0;
     Buf c64, c32, clm, cn, cR2, cr50, crt, cname, cblk;
-    // the mixed filter's block test (one test settles eight points of a pair); PHYGAS_SCAN_BLOCKS=0 at pgx_open
-    // turns it off, so that every point is walked (the same rows either way)
-    bool scan_blocks = true;
+    // the mixed filter's block test (one test settles eight points of a pair), PHYGAS_SCAN_BLOCKS=1 at pgx_open;
+    // off, every point is walked (the same rows either way)
+    bool scan_blocks = false;
     // the staged star chunks: two track slots, so that one chunk's orbits can run on the side stream while the
     // previous chunk is screened (pgx_screen_chunks); the single-chunk entry points use slot `cur`
     TrackSlot trk[2];

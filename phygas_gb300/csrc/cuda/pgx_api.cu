@@ -76,6 +76,8 @@ struct PgxContext {
     // the mixed filter's block test (one test settles eight points of a pair), PHYGAS_SCAN_BLOCKS=1 at pgx_open;
     // off, every point is walked (the same rows either way)
     bool scan_blocks = false;
+    // device allocations made by ensure(), and the one that fails on purpose (PHYGAS_FAIL_ALLOC_AT; 0 = none)
+    long allocs = 0, fail_alloc_at = 0;
     // the staged star chunks: two track slots, so that one chunk's orbits can run on the side stream while the
     // previous chunk is screened (pgx_screen_chunks); the single-chunk entry points use slot `cur`
     TrackSlot trk[2];
@@ -156,6 +158,10 @@ int ensure(PgxContext *ctx, Buf &b, size_t bytes) {
     b.p = nullptr;
     b.cap = 0;
     const size_t want = bytes + bytes / 4;
+    // fault injection on the host (PHYGAS_FAIL_ALLOC_AT=N at pgx_open): the context's N-th device allocation reports
+    // that the device is out of memory, as a failed cudaMalloc would, without touching the device
+    if (++ctx->allocs == ctx->fail_alloc_at)
+        return fail(ctx, PGX_E_NOMEM, "device allocation %ld of %zu bytes: out of memory (injected)", ctx->allocs, want);
     CK(cudaMalloc(&b.p, want));
     b.cap = want;
     return 0;
@@ -411,6 +417,7 @@ int pgx_open(int device, PgxContext **out) {
     ctx = new PgxContext();
     ctx->device = device;
     if (const char *e = getenv("PHYGAS_SCAN_BLOCKS")) ctx->scan_blocks = atoi(e) != 0;
+    if (const char *e = getenv("PHYGAS_FAIL_ALLOC_AT")) ctx->fail_alloc_at = atol(e);
     int rc = 0;
     {
         auto init = [&]() -> int {

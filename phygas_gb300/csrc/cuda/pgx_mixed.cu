@@ -357,6 +357,11 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32(ScreenTables T, flo
     }
 }
 
+// the full bounds of a point, out of line (the block kernel's single copy of point_bound32)
+__device__ __noinline__ bool point_at32_ol(const ScreenTables *T, int s, int c, int k, float cut, Bound *b) {
+    return point_at32(*T, s, c, k, cut, *b);
+}
+
 // k_mx_scan32 with block culling.  One block: kScanStars stars x one cluster; a warp walks its 32 pairs in step.
 // Clusters are the grid's fast axis, so the blocks resident at one time share one block of stars, whose track data
 // stays in L2.
@@ -370,7 +375,7 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32(ScreenTables T, flo
 // have no block data.  A settled block's points all have chi2 >= cut in the FP64 path: they can neither be a kept
 // pair's minimum nor bring a pair under the cut, and they are left out of min ub, which only admits more candidates.
 // six resident blocks per SM asked of the compiler: 24 warps to issue from; the kernel is issue-bound
-__global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32_blocks(ScreenTables T, float cut,
+__global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32_blocks(const __grid_constant__ ScreenTables T, float cut,
                                                              unsigned char *__restrict__ flag,
                                                              float *__restrict__ ubmin,
                                                              unsigned long long *__restrict__ klist) {
@@ -408,7 +413,7 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32_blocks(ScreenTables
         if (lane < cnt) {
             const int e = s_q[w][lane];
             Bound b;
-            const bool keep = point_at32(T, s0 + (e & 31), c, e >> 5, cut, b);
+            const bool keep = point_at32_ol(&T, s0 + (e & 31), c, e >> 5, cut, &b);
             s_lb[w][lane] = keep ? b.lb : inf;
             s_ub[w][lane] = keep ? b.ub : inf;
             atomicOr(&s_own[w][e & 31], 1u << lane);
@@ -446,8 +451,8 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32_blocks(ScreenTables
         return !point_skip32(St, Sc, lmt, lmc, mc, mn, cut);
     };
     // ---- level 1: blocks of kBlk points whose position reference km = kBlk b + kBlk/2 lies on the pair's track
-    const int nbt = (T.blk_t && T.blk_c && n > kBlk / 2) ? (n - kBlk / 2 - 1) / kBlk + 1 : 0;
-    if (nbt > 0) {
+    const int nbt = n > kBlk / 2 ? (n - kBlk / 2 - 1) / kBlk + 1 : 0;
+    {
         // walk the queued blocks [0, cnt) point by point, one block per lane
         auto walk_blocks = [&](int cnt) {
             __syncwarp();
@@ -484,9 +489,12 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32_blocks(ScreenTables
         };
         int bn = 0;
         const float4 *bt = T.blk_t + (size_t)s * 4, *bc = T.blk_c + (size_t)c * 4;
-        for (int b = 0; b < nbt; b++) {
+        // blocks 0 .. nbt-1 get the test; block nbt, the points after them (fewer than five), is walked untested;
+        // the last pass tests nothing and walks what is left (one call site keeps the kernel's code small)
+        const int kt = nbt * kBlk, nball = nbt + (kt < n ? 1 : 0);
+        for (int b = 0; b <= nball; b++) {
             bool need = false;
-            if (active) {
+            if (b < nbt && active) {
                 const int km = b * kBlk + kBlk / 2;
                 const float4 *a = bt + (size_t)b * NT * 4, *q = bc + (size_t)b * NC * 4;
                 const float4 BT[4] = {a[0], a[1], a[2], a[3]};
@@ -495,42 +503,21 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32_blocks(ScreenTables
                 float mref[3];
                 sep32(tm[0], tm[1], __ldg(cm), __ldg(cm + 1), mref);
                 need = !block_skip32(BT, BC, mref, cut);
+            } else if (b < nball) {
+                need = active;
             }
             const unsigned mask = __ballot_sync(0xffffffffu, need);
             if (need) s_bq[w][bn + __popc(mask & ((1u << lane) - 1u))] = lane | (b << 5);
             bn += __popc(mask);
-            if (bn >= 32) {
-                walk_blocks(32);
-                const int rest = bn - 32;
-                const int v = lane < rest ? s_bq[w][32 + lane] : 0;
+            if (bn >= 32 || (b == nball && bn > 0)) {
+                const int cnt = min(bn, 32);
+                walk_blocks(cnt);
+                const int rest = bn - cnt;
+                const int v = lane < rest ? s_bq[w][cnt + lane] : 0;
                 __syncwarp();
                 if (lane < rest) s_bq[w][lane] = v;
                 bn = rest;
             }
-        }
-        if (bn > 0) walk_blocks(bn);
-    }
-    // ---- level 0: the points after the tested blocks, every lane in step
-    const int kt = nbt * kBlk;
-    if (kt < n) {
-        const float4 *tp = T.t32 + (size_t)s * 3, *cp = T.c32 + (size_t)c * 3;
-        const float4 *a = tp + (size_t)kt * NT * 3, *q = cp + (size_t)kt * NC * 3;
-        float4 t0 = a[0], t1 = a[1], t2 = a[2];
-        float4 c0 = __ldg(q), c1 = __ldg(q + 1), c2 = __ldg(q + 2);
-        float mcur[3];
-        sep32(t0, t1, c0, c1, mcur);
-        for (int k = kt; k < n; k++) {
-            const float4 T1 = t1, T2 = t2, C1 = c1, C2 = c2;
-            float mnext[3] = {mcur[0], mcur[1], mcur[2]};
-            if (k + 1 < n) {
-                const float4 *tn = tp + (size_t)(k + 1) * NT * 3, *cn = cp + (size_t)(k + 1) * NC * 3;
-                t0 = tn[0]; t1 = tn[1]; t2 = tn[2];
-                c0 = __ldg(cn); c1 = __ldg(cn + 1); c2 = __ldg(cn + 2);
-                sep32(t0, t1, c0, c1, mnext);
-            }
-            const bool need = active && point_needs(s, k, T1, T2, C1, C2, mcur, mnext);
-            push_point(need, lane | (k << 5));
-            mcur[0] = mnext[0]; mcur[1] = mnext[1]; mcur[2] = mnext[2];
         }
     }
     if (qn > 0) drain(qn);
@@ -1081,6 +1068,10 @@ __device__ __forceinline__ void draw32(const Fin32 &g, uint64_t w, float &x, flo
 // draw32 computes them, and the FP64 recheck of a draw within its bound of a radius -- the counts are the FP64
 // path's, and the same as drawing every draw in full.
 constexpr int kFinWarps = 8, kFinQueue = 64;
+constexpr double kLevelA = 1.5;         // R* from which level A is worth its queue (it settles >= 67.5 % of draws)
+
+// the FP64 recheck of a draw (rare: about one draw in 3e6), kept out of line so the kernel's code stays small
+__device__ __noinline__ int draw_inside64_at(const FinishIn *f, int i) { return draw_inside64(*f, i); }
 
 __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const FinishIn *__restrict__ fin,
                                                                 ScreenRowDev *__restrict__ rows,
@@ -1121,7 +1112,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
                 in50 += d50 < 0.f;
                 intot += dt < 0.f;
             } else {
-                const int v = draw_inside64(fin[h], i);             // the FP64 path's own draw
+                const int v = draw_inside64_at(fin + h, i);         // the FP64 path's own draw
                 in50 += v & 1;
                 intot += v >> 1;
                 rechecks++;
@@ -1133,21 +1124,22 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
     // U* = exp(-R*^2 / 2), R* = (|mx| - max(r50, rtot)) / |l00|, has |x| >= max(r50, rtot) whatever its angle: outside
     // both spheres.  U* is taken in FP64 once per pair with relative margins of 1e-12 on R* and 1e-10 on R*^2 (far
     // above the FP64 log's and exp's last-bit errors and the rounding of x = mx + l00 z0), and the test is an integer
-    // compare of u1's 53 bits with ceil(U* 2^53).  The draws it cannot settle are queued (index, first generator
-    // output) and get the z0 test above 32 at a time on full warps.
+    // compare of u1's 53 bits with ceil(U* 2^53).  It is used for pairs with R* >= kLevelA (then it settles at least
+    // 1 - exp(-kLevelA^2 / 2) of the draws); for the others every draw goes on.  The open draws are queued (index,
+    // first generator output) and get the z0 test above (level B), 32 at a time on full warps.
     uint64_t kstar = (1ull << 53) + 1;                           // no draw settles at level A
     {
         const double mxa = fabs(fin[h].mx), l00a = fabs(fin[h].l00), ro = fmax(fin[h].r50, fin[h].rt);
-        if (mxa > ro) {
-            const double R = (mxa - ro) / l00a * (1.0 - 1e-12);
+        const double R = mxa > ro ? (mxa - ro) / l00a * (1.0 - 1e-12) : 0.0;
+        if (R >= kLevelA) {
             const double U = exp(-0.5 * R * R * (1.0 - 1e-10)) * (1.0 + 1e-12);
             if (U < 1.0) kstar = (uint64_t)ceil(U * 9007199254740992.0);
         }
     }
     int qn = 0, an = 0;
     // level B for level-A queue entries [0, cnt), one per lane: z0 and its bound; the draws still open go to the
-    // phase-2 queue
-    auto level_b = [&](int cnt) {
+    // phase-2 queue, completed 32 at a time (all of them when `last`)
+    auto level_b = [&](int cnt, bool last) {
         __syncwarp();
         bool open = false;
         int i = 0;
@@ -1169,13 +1161,14 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
             s_e[wq][at] = e0;
         }
         qn += __popc(m);
-        if (qn >= 32) {
-            complete(32);
-            const int rest = qn - 32;
+        while (qn >= 32 || (last && qn > 0)) {
+            const int c = min(qn, 32);
+            complete(c);
+            const int rest = qn - c;
             int vi = 0;
             float vz = 0.f, va = 0.f, ve = 0.f;
             if (lane < rest) {
-                vi = s_i[wq][32 + lane]; vz = s_z[wq][32 + lane]; va = s_a[wq][32 + lane]; ve = s_e[wq][32 + lane];
+                vi = s_i[wq][c + lane]; vz = s_z[wq][c + lane]; va = s_a[wq][c + lane]; ve = s_e[wq][c + lane];
             }
             __syncwarp();
             if (lane < rest) {
@@ -1185,12 +1178,17 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
         }
         __syncwarp();
     };
-    // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden
+    // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden; the 17th
+    // pass draws nothing and flushes both queues (one call site for each stage keeps the kernel's code small)
     uint64_t w = seed + (uint64_t)(6 * lane) * kGolden;
 #pragma unroll 1
-    for (int q = 0; q < 16; q++, w += 192 * kGolden) {
-        const uint64_t ga = splitmix_mix(w + kGolden);
-        const bool open = (ga >> 11) < kstar;
+    for (int q = 0; q <= 16; q++, w += 192 * kGolden) {
+        bool open = false;
+        uint64_t ga = 0;
+        if (q < 16) {
+            ga = splitmix_mix(w + kGolden);
+            open = (ga >> 11) < kstar;
+        }
         const unsigned m = __ballot_sync(0xffffffffu, open);
         if (open) {
             const int at = an + __popc(m & ((1u << lane) - 1u));
@@ -1198,19 +1196,18 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
             s_ga[wq][at] = ga;
         }
         an += __popc(m);
-        if (an >= 32) {
-            level_b(32);
-            const int rest = an - 32;
+        if (an >= 32 || q == 16) {
+            const int c = min(an, 32);
+            level_b(c, q == 16);
+            const int rest = an - c;
             int vi = 0;
             uint64_t vg = 0;
-            if (lane < rest) { vi = s_ia[wq][32 + lane]; vg = s_ga[wq][32 + lane]; }
+            if (lane < rest) { vi = s_ia[wq][c + lane]; vg = s_ga[wq][c + lane]; }
             __syncwarp();
             if (lane < rest) { s_ia[wq][lane] = vi; s_ga[wq][lane] = vg; }
             an = rest;
         }
     }
-    if (an > 0) level_b(an);
-    if (qn > 0) complete(qn);
     in50 = __reduce_add_sync(0xffffffffu, in50);
     intot = __reduce_add_sync(0xffffffffu, intot);
     rechecks = __reduce_add_sync(0xffffffffu, rechecks);

@@ -3,7 +3,7 @@
 // as "%s %s %c %.3f %.3f %.2f %.2f %.4f %.4f %.2f %.3f %.3f\n", byte for byte the C library's text (pgx_fmt.cuh).
 //   k_row_len   one thread per row: the line's length
 //   (exclusive scan of the lengths: each line's offset)
-//   k_row_text  one thread per row: the line written at its offset
+//   k_row_text  one thread per row: the line formatted into shared memory, the block's lines written out together
 // Rows go in batches of at most kTextBatch, so that a batch's offsets fit in an int.
 #include <algorithm>
 #include <initializer_list>
@@ -43,10 +43,33 @@ __global__ void k_row_len(int n, const ScreenRowDev *__restrict__ rows, TextLabe
     if (h < n) len[h] = row_text(nullptr, rows[h], L);
 }
 
-__global__ void k_row_text(int n, const ScreenRowDev *__restrict__ rows, TextLabels L, const int *__restrict__ off,
-                           char *__restrict__ out) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h < n) row_text(out + off[h], rows[h], L);
+// A block's lines are contiguous in the output.  They are formatted into shared memory first (byte stores there are
+// cheap), placed at the output's alignment modulo 16, and the block writes the span out with 16-byte stores (bytes
+// at its two ends): whole sectors, where one thread per line storing bytes to global memory wrote partial sectors.
+// A span too long for the staging area (lines of very large numbers) is written line by line.
+constexpr int kTextRows = 128, kTextStage = 24576;
+
+__global__ void __launch_bounds__(kTextRows) k_row_text(int n, const ScreenRowDev *__restrict__ rows, TextLabels L,
+                                                        const int *__restrict__ off, const int *__restrict__ len,
+                                                        char *__restrict__ out) {
+    __shared__ __align__(16) char buf[kTextStage + 16];
+    const int h0 = blockIdx.x * kTextRows, h = h0 + threadIdx.x, hl = min(h0 + kTextRows, n) - 1;
+    const long b0 = off[h0], span = (long)off[hl] + len[hl] - b0;
+    char *dst = out + b0;
+    const int a = (int)((uintptr_t)dst & 15);
+    if (span + a > kTextStage) {
+        if (h < n) row_text(out + off[h], rows[h], L);
+        return;
+    }
+    if (h < n) row_text(buf + a + (off[h] - b0), rows[h], L);
+    __syncthreads();
+    const int head = (int)min((long)((16 - a) & 15), span);
+    if ((int)threadIdx.x < head) dst[threadIdx.x] = buf[a + threadIdx.x];
+    const long nvec = (span - head) / 16;
+    const uint4 *src4 = reinterpret_cast<const uint4 *>(buf + a + head);
+    uint4 *dst4 = reinterpret_cast<uint4 *>(dst + head);
+    for (long i = threadIdx.x; i < nvec; i += kTextRows) dst4[i] = src4[i];
+    for (long i = head + nvec * 16 + threadIdx.x; i < span; i += kTextRows) dst[i] = buf[a + i];
 }
 
 int format_rows(cudaStream_t st, long n, const ScreenRowDev *rows, const TextLabels &L, TextBufs &b, char *out,
@@ -75,7 +98,7 @@ int format_rows(cudaStream_t st, long n, const ScreenRowDev *rows, const TextLab
             err = "text buffer too small";
             return PGX_E_LIMIT;
         }
-        k_row_text<<<(m + 255) / 256, 256, 0, st>>>(m, rows + h0, L, off, out + base);
+        k_row_text<<<(m + kTextRows - 1) / kTextRows, kTextRows, 0, st>>>(m, rows + h0, L, off, len, out + base);
         if ((rc = check(cudaGetLastError(), err, "k_row_text"))) return rc;
         base += (size_t)total;
     }

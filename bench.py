@@ -315,6 +315,13 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
     t0 = time.perf_counter()
     batch = pg.draw_pair_batch(targets, ti, clusters, ci, ncl, 0.05, out_ps=pinned.array)
     t_draw = time.perf_counter() - t0
+    # the same draws on the GPU (pgx_draw_pair_batch_gpu): wall time of the call (records in, clones out) and the
+    # draw kernel's device time
+    ctx.draw_pair_batch(targets, ti[:64], clusters, ci[:64], ncl[:64], 0.05)        # warm-up
+    t0 = time.perf_counter()
+    ctx.draw_pair_batch(targets, ti, clusters, ci, ncl, 0.05)
+    t_draw_gpu = time.perf_counter() - t0
+    draw_gpu_ms = ctx.stats()["ms_total"]
     best, table = ctx.tune_pair(*pg.draw_pair_batch(targets, ti[::25], clusters, ci[::25], ncl[::25], 0.05))
     ctx.pair(*batch)                                         # warm-up
     ms = []
@@ -350,6 +357,8 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
                    "how": "pgx_pair_targets: host clone draws of each batch of 1,024 pairs overlap the GPU's tracing "
                           "of the one before (page-locked buffers)",
                    "host_draw_s_unpipelined": t_draw,
+                   "device_draws": {"call_s": t_draw_gpu, "kernel_ms": draw_gpu_ms,
+                                    "how": "pgx_draw_pair_batch_gpu: the same clones drawn on the GPU"},
                    "prefilter_s": {"gpu_first_call": pref_s[0], "gpu_clusters_kept": pref_s[1],
                                    "gpu_device_ms": pref_st["ms_prefilter"],
                                    "host_decided_pairs": pref_st["prefilter_rechecked"],
@@ -770,6 +779,10 @@ def main():
     t0 = time.perf_counter()
     ps0, sig, pre = pg.draw_targets(stars, N_SAMP)
     draw_s = time.perf_counter() - t0
+    ctx.draw_targets(stars[:256], N_SAMP)                                          # warm-up
+    t0 = time.perf_counter()
+    ctx.draw_targets(stars, N_SAMP)
+    draw_gpu_s, draw_gpu_ms = time.perf_counter() - t0, ctx.stats()["ms_total"]
     ctx.stage(ps0, sig, pre)
 
     def barrier():
@@ -792,9 +805,14 @@ def main():
         barrier()
         return per, stats, rows
 
+    scan_tune = None
     try:
         run(pg.PGX_MIXED, 0, 1)
         precision = pg.PGX_MIXED
+        # the screen autotuner: the block filter's launch shapes on this chunk, the fastest kept for the steps
+        best, table = ctx.tune_screen(tmax, CHI2_MAX)
+        scan_tune = {"chosen_min_blocks_per_sm": table[best][0],
+                     "scan_ms": [{"min_blocks_per_sm": b, "ms": r4(t)} for b, t in table]}
     except pg.GpuError as e:
         log("mixed-precision screen unavailable (%s); timing the FP64 screen as the value" % e)
         precision = pg.PGX_FP64
@@ -901,7 +919,9 @@ def main():
                     "how": "pgx_screen_chunks over %d chunks of the %d stars: host draws of chunk i+2, the orbits of "
                            "chunk i+1 (side stream) and the screen of chunk i overlap; rows copied to page-locked host "
                            "memory" % (E2E_CHUNKS, N_STARS),
-                    "host_draw_s_unpipelined": draw_s},
+                    "host_draw_s_unpipelined": draw_s,
+                    "device_draws": {"call_s": draw_gpu_s, "kernel_ms": draw_gpu_ms,
+                                     "how": "pgx_draw_targets_gpu: the chunk's draws on the GPU"}},
             "roofline": scan,
             "roofline_orbits": {"bound": "fp64", "kernel": "k_stm_orbits", "achieved": achieved / 1e12,
                                 "peak": fp64_peak / 1e12, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
@@ -915,6 +935,7 @@ def main():
             "cpu_baseline": cpu,
             "fp32_peak_tflops": fp32_peak / 1e12,
             "cluster_table_s": table_s,
+            "scan_autotune": scan_tune,
             "rows_per_step": n_rows, "rows_fp64": n_rows64,
             "work_per_step": {k: int(s[k]) for k in ("candidates", "ambiguous", "rechecked_points",
                                                      "rechecked_draws", "kept")},

@@ -111,6 +111,17 @@ int pgx_screen_chunks_text(PgxContext *ctx, const PhTarget *t, int nt, const PhC
 int pgx_draw_targets(const PhTarget *t, int n, int n_samp, int threads, double *ps0, double *sig,
                      uint64_t *seed_prefix);
 int pgx_draw_clusters(const PhCluster *c, int n, int n_samp, int threads, double *ps0, double *sig);
+/* The same draws on the GPU (the device-side draws): pgx_draw_targets' outputs for n targets, and
+ * pgx_draw_pair_batch's for n_pairs pairs, from the same seeds and random streams (the same draws taken, retries
+ * included), with the device's log / exp / sin / cos / sqrt / pow in place of the C library's, so the values agree
+ * with the host's within the last bits of those functions rather than bit for bit (the host versions stay the
+ * reference's draws exactly).  Host buffers in and out, as the host versions; pgx_stats: ms_total = the draw
+ * kernel's device time, clones and pairs for the pair batch. */
+int pgx_draw_targets_gpu(PgxContext *ctx, const PhTarget *t, int n, int n_samp, double *ps0, double *sig,
+                         uint64_t *seed_prefix);
+int pgx_draw_pair_batch_gpu(PgxContext *ctx, int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c,
+                            const int *ci, const int *n_clones, double dt_myr, int *clone_off, double *ps,
+                            int *steps, double *dt, double *r50_pc, double *rtot_pc);
 uint64_t pgx_seed_prefix(const char *target_id);
 
 /* Pair jobs on the host (the reference's pair mode: phygas_cli's target loop, src/phygas_cli.c:37-51, and
@@ -175,6 +186,14 @@ int pgx_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *p
  * replayed with the batch's parameters; the tuner's runs also capture each shape's graph. */
 int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,
                   const double *dt, const double *r50_pc, const double *rtot_pc, double *ms, int *best);
+/* Launch-shape autotuner of the screen's block filter (no counterpart in the reference): screens the staged chunk
+ * (pgx_screen_stage) with every shape of the filter -- resident blocks per SM asked of the compiler, which sets its
+ * register cap -- and keeps the fastest for this context's later screens.  ms[pgx_screen_shapes(0, NULL)] (or NULL)
+ * gets each shape's filter time (ms_scan), *best (or NULL) its index.  The shapes differ in register allocation only,
+ * so they give the same rows; a shape that keeps another number of pairs fails the call (PGX_E_CUDA). */
+int pgx_tune_screen(PgxContext *ctx, double tmax_myr, double chi2_max, double *ms, int *best);
+/* number of the filter's launch shapes; the first n minimum resident blocks per SM into min_blocks */
+int pgx_screen_shapes(int n, int *min_blocks);
 /* number of launch shapes; the first n as (warps per block, clones per lane, minimum resident blocks per SM) */
 int pgx_pair_shapes(int n, int *warps, int *clones_per_lane, int *min_blocks);
 /* ph_pair over a list of (target, cluster) pairs -- pair q = (t[ti[q]], c[ci[q]]) with n_clones[q] clones, seeds

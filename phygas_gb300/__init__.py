@@ -119,6 +119,9 @@ SIGNATURES = [
                                          C.c_int, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p]),
     ("pgx_draw_targets", C.c_int, [_P(PhTarget), C.c_int, C.c_int, C.c_int, _D, _D, _U64]),
     ("pgx_draw_clusters", C.c_int, [_P(PhCluster), C.c_int, C.c_int, C.c_int, _D, _D]),
+    ("pgx_draw_targets_gpu", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, C.c_int, _D, _D, _U64]),
+    ("pgx_draw_pair_batch_gpu", C.c_int, [C.c_void_p, C.c_int, _P(PhTarget), _I, _P(PhCluster), _I, _I, C.c_double,
+                                          _I, _D, _I, _D, _D, _D]),
     ("pgx_seed_prefix", C.c_uint64, [C.c_char_p]),
     ("pgx_prefilter_pairs", C.c_int, [_P(PhTarget), C.c_int, _P(PhCluster), C.c_int, C.c_int, _I, _I, C.c_long,
                                       _P(C.c_long)]),
@@ -134,6 +137,8 @@ SIGNATURES = [
     ("pgx_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, C.c_void_p, _D]),
     ("pgx_tune_pair", C.c_int, [C.c_void_p, C.c_int, _I, _D, _I, _D, _D, _D, _D, _I]),
     ("pgx_pair_shapes", C.c_int, [C.c_int, _I, _I, _I]),
+    ("pgx_tune_screen", C.c_int, [C.c_void_p, C.c_double, C.c_double, _D, _I]),
+    ("pgx_screen_shapes", C.c_int, [C.c_int, _I]),
     ("pgx_stats", C.c_int, [C.c_void_p, _P(PgxStats)]),
     ("pgx_peaks", C.c_int, [C.c_void_p, _D, _D]),
     ("pgx_check_bounds", C.c_int, [C.c_void_p, C.c_int, _D, _D, _D, C.c_double, _D, _P(C.c_float),
@@ -276,6 +281,40 @@ class Context:
                                            _ptr(lb, C.c_float), _ptr(ub, C.c_float), _ptr(rej, C.c_int)),
                     "pgx_check_bounds")
         return v, lb, ub, rej
+
+    def draw_targets(self, targets, n_samp=64):
+        """pgx_draw_targets_gpu: the targets' nominal states, covariances of their draws and seed prefixes, drawn on
+        the GPU (the same draws as pg.draw_targets, within the last bits of the device's math functions)."""
+        targets = as_array(targets, PhTarget)
+        n = len(targets)
+        ps0, sig, pre = np.zeros((n, 6)), np.zeros((n, 36)), np.zeros(n, np.uint64)
+        self._check(lib().pgx_draw_targets_gpu(self.h, targets, n, n_samp, _ptr(ps0), _ptr(sig),
+                                               _ptr(pre, C.c_uint64)), "pgx_draw_targets_gpu")
+        return ps0, sig, pre
+
+    def draw_pair_batch(self, targets, ti, clusters, ci, n_clones, dt_myr=0.05):
+        """pgx_draw_pair_batch_gpu: pg.draw_pair_batch's outputs (clone_off, ps, steps, dt, r50, rtot), the clones
+        drawn on the GPU."""
+        targets, clusters = as_array(targets, PhTarget), as_array(clusters, PhCluster)
+        ti, ci = np.ascontiguousarray(ti, np.int32), np.ascontiguousarray(ci, np.int32)
+        nc = np.ascontiguousarray(np.broadcast_to(n_clones, ti.shape), np.int32)
+        n = len(ti)
+        ps = np.zeros(12 * max(int(nc.sum()), 1))
+        off = np.zeros(n + 1, np.int32)
+        steps, dt, r50, rt = np.zeros(n, np.int32), np.zeros(n), np.zeros(n), np.zeros(n)
+        self._check(lib().pgx_draw_pair_batch_gpu(self.h, n, targets, _ptr(ti, C.c_int), clusters, _ptr(ci, C.c_int),
+                                                  _ptr(nc, C.c_int), dt_myr, _ptr(off, C.c_int), _ptr(ps),
+                                                  _ptr(steps, C.c_int), _ptr(dt), _ptr(r50), _ptr(rt)),
+                    "pgx_draw_pair_batch_gpu")
+        return off, ps[:12 * int(off[-1])], steps, dt, r50, rt
+
+    def tune_screen(self, tmax, chi2_max=25.0):
+        """pgx_tune_screen on the staged chunk: -> (index of the chosen shape, [(min blocks per SM, scan ms), ...])."""
+        n = lib().pgx_screen_shapes(0, None)
+        mb, ms, best = np.zeros(n, np.int32), np.zeros(n), C.c_int()
+        lib().pgx_screen_shapes(n, _ptr(mb, C.c_int))
+        self._check(lib().pgx_tune_screen(self.h, tmax, chi2_max, _ptr(ms), C.byref(best)), "pgx_tune_screen")
+        return best.value, list(zip(mb.tolist(), ms.tolist()))
 
     def check_blocks(self, tmax, chi2_max=25.0):
         """The filter's block test on the staged (unsplit) chunk, each settled block's points checked in FP64

@@ -20,9 +20,9 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-# FP contraction off where a result must follow the reference's operation order, and for the orbits, whose fused
+# FP contraction off where a result must follow the reference's operation order (the draws too), and for the orbits, whose fused
 # multiply-adds are all written out: then every launch shape of a kernel rounds alike
-FMAD_OFF = {"pgx_scan.cu", "pgx_mixed.cu", "pgx_orbit.cu"}
+FMAD_OFF = {"pgx_scan.cu", "pgx_mixed.cu", "pgx_orbit.cu", "pgx_draws.cu"}
 
 
 def nvcc():

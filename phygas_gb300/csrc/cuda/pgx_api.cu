@@ -73,9 +73,10 @@ struct PgxContext {
     // resident cluster table (original cluster order)
     int nc = 0, ncp = 0;
     Buf c64, c32, clm, cn, cR2, cr50, crt, cname, cblk;
-    // the mixed filter's block test (one test settles eight points of a pair), PHYGAS_SCAN_BLOCKS=1 at pgx_open;
-    // off, every point is walked (the same rows either way)
-    bool scan_blocks = false;
+    Buf x_draw, x_draw_ps;                     // device draws: records, seeds and outputs; clone slots
+    // the mixed filter's block test (one test settles eight points of a pair); PHYGAS_SCAN_BLOCKS=0 at pgx_open
+    // turns it off, and every point is walked (the same rows either way)
+    bool scan_blocks = true;
     // device allocations made by ensure(), and the one that fails on purpose (PHYGAS_FAIL_ALLOC_AT; 0 = none)
     long allocs = 0, fail_alloc_at = 0;
     // the staged star chunks: two track slots, so that one chunk's orbits can run on the side stream while the
@@ -452,12 +453,13 @@ void pgx_close(PgxContext *ctx) {
                    &ctx->p_q, &ctx->p_done, &ctx->p_cres, &ctx->p_res, &ctx->p_params, &ctx->x_ps0, &ctx->x_sig21,
                    &ctx->x_npts,
                    &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32, &ctx->rows_b[0], &ctx->rows_b[1],
-                   &ctx->lab_names, &ctx->lab_kinds, &ctx->lab_age16, &ctx->lab_age84, &ctx->part_in};
+                   &ctx->lab_names, &ctx->lab_kinds, &ctx->lab_age16, &ctx->lab_age84, &ctx->part_in,
+                   &ctx->cblk, &ctx->x_draw, &ctx->x_draw_ps};
     for (Buf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (ctx->h_part) cudaFreeHost(ctx->h_part);
     for (auto &k : ctx->trk) {
-        for (Buf *b : {&k.ps0, &k.sig21, &k.prefix, &k.opos, &k.ovel, &k.t64, &k.t32, &k.tlm, &k.ids})
+        for (Buf *b : {&k.ps0, &k.sig21, &k.prefix, &k.opos, &k.ovel, &k.t64, &k.t32, &k.tlm, &k.ids, &k.blk})
             if (b->p) cudaFree(b->p);
         if (k.done) cudaEventDestroy(k.done);
         if (k.h_stage) cudaFreeHost(k.h_stage);
@@ -486,6 +488,113 @@ uint64_t pgx_seed_prefix(const char *id) { return pgh_seed_prefix(id); }
 int pgx_draw_targets(const PhTarget *t, int n, int n_samp, int threads, double *ps0, double *sig, uint64_t *prefix) {
     if (n < 0 || (n > 0 && (!t || !ps0 || !sig)) || n_samp < 0) return PGX_E_ARG;
     pgh_draw_targets(t, n, n_samp, threads > 0 ? threads : pgh_default_threads(), ps0, sig, prefix);
+    return 0;
+}
+
+int pgx_draw_targets_gpu(PgxContext *ctx, const PhTarget *t, int n, int n_samp, double *ps0, double *sig,
+                         uint64_t *prefix) {
+    if (!ctx) return PGX_E_ARG;
+    if (n < 0 || n_samp < 0 || (n > 0 && (!t || !ps0 || !sig))) return fail(ctx, PGX_E_ARG, "pgx_draw_targets_gpu");
+    if (n == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    std::vector<uint64_t> seed(n);
+    for (int i = 0; i < n; i++) {
+        seed[i] = ph_seed("lin", t[i].id);
+        if (prefix) prefix[i] = pgh_seed_prefix(t[i].id);
+    }
+    const size_t bt = (size_t)n * sizeof(PhTarget), bs = (size_t)n * 8, bo = (size_t)n * 42 * 8;
+    RET(ensure(ctx, ctx->x_draw, bt + bs + bo + 64));
+    char *b = P<char>(ctx->x_draw);
+    PhTarget *dt = (PhTarget *)b;
+    uint64_t *ds = (uint64_t *)(b + ((bt + 15) & ~(size_t)15));
+    double *dp = (double *)(ds + n), *dg = dp + (size_t)6 * n;
+    CK(cudaMemcpyAsync(dt, t, bt, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(ds, seed.data(), bs, cudaMemcpyHostToDevice, ctx->st));
+    ctx->stats = PgxStats();
+    CK(cudaEventRecord(ctx->ev[EV_PAIR0], ctx->st));
+    MRET(pgx::draw_targets_gpu(ctx->st, n, dt, n_samp, ds, dp, dg, ctx->mixed.err));
+    CK(cudaEventRecord(ctx->ev[EV_PAIR1], ctx->st));
+    CK(cudaMemcpyAsync(ps0, dp, (size_t)n * 6 * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaMemcpyAsync(sig, dg, (size_t)n * 36 * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->stats.ms_total = elapsed(ctx, EV_PAIR0, EV_PAIR1);
+    ctx->stats.kernels = 1;
+    return 0;
+}
+
+int pgx_draw_pair_batch_gpu(PgxContext *ctx, int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c,
+                            const int *ci, const int *n_clones, double dt_myr, int *clone_off, double *ps,
+                            int *steps, double *dt, double *r50_pc, double *rtot_pc) {
+    if (!ctx) return PGX_E_ARG;
+    if (n_pairs < 0 || !clone_off || !(dt_myr > 0)) return fail(ctx, PGX_E_ARG, "pgx_draw_pair_batch_gpu");
+    if (n_pairs > 0 && (!t || !ti || !c || !ci || !n_clones || !ps || !steps || !dt || !r50_pc || !rtot_pc))
+        return fail(ctx, PGX_E_ARG, "pgx_draw_pair_batch_gpu");
+    clone_off[0] = 0;
+    if (n_pairs == 0) return 0;
+    CK(cudaSetDevice(ctx->device));
+    // per pair on the host: seed, steps and dt as ph_pair_draw sets them, and a slot of n_clones clones
+    int nt = 0, nc = 0;
+    std::vector<uint64_t> seed(n_pairs);
+    std::vector<long long> slot(n_pairs + 1, 0);
+    for (int q = 0; q < n_pairs; q++) {
+        if (ti[q] < 0 || ci[q] < 0 || n_clones[q] < 0 || n_clones[q] > pgx::kMaxPairClones)
+            return fail(ctx, n_clones[q] > pgx::kMaxPairClones ? PGX_E_LIMIT : PGX_E_ARG,
+                        "pgx_draw_pair_batch_gpu: pair %d", q);
+        nt = std::max(nt, ti[q] + 1);
+        nc = std::max(nc, ci[q] + 1);
+        const PhCluster &cq = c[ci[q]];
+        seed[q] = ph_seed(t[ti[q]].id, cq.name);
+        steps[q] = (int)std::ceil(cq.tmax_myr / dt_myr);
+        dt[q] = -cq.tmax_myr / steps[q];
+        r50_pc[q] = cq.r50_pc;
+        rtot_pc[q] = cq.rtot_pc;
+        slot[q + 1] = slot[q] + n_clones[q];
+    }
+    const long long cap = slot[n_pairs];
+    const size_t bt = ((size_t)nt * sizeof(PhTarget) + 15) & ~(size_t)15;
+    const size_t bc = ((size_t)nc * sizeof(PhCluster) + 15) & ~(size_t)15;
+    const size_t bi = (((size_t)n_pairs * 4 + 15) & ~(size_t)15);
+    const size_t b8 = (size_t)n_pairs * 8;
+    RET(ensure(ctx, ctx->x_draw, bt + bc + 4 * bi + 2 * b8 + 64));
+    RET(ensure(ctx, ctx->x_draw_ps, (size_t)std::max(cap, 1LL) * 12 * 8 * 2));
+    char *b = P<char>(ctx->x_draw);
+    PhTarget *d_t = (PhTarget *)b;
+    PhCluster *d_c = (PhCluster *)(b + bt);
+    int *d_ti = (int *)(b + bt + bc), *d_ci = (int *)((char *)d_ti + bi), *d_n = (int *)((char *)d_ci + bi);
+    int *d_m = (int *)((char *)d_n + bi);
+    uint64_t *d_seed = (uint64_t *)((char *)d_m + bi);
+    long long *d_slot = (long long *)(d_seed + n_pairs);
+    double *d_ps = P<double>(ctx->x_draw_ps), *d_out = d_ps + (size_t)std::max(cap, 1LL) * 12;
+    CK(cudaMemcpyAsync(d_t, t, (size_t)nt * sizeof(PhTarget), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_c, c, (size_t)nc * sizeof(PhCluster), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_ti, ti, (size_t)n_pairs * 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_ci, ci, (size_t)n_pairs * 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_n, n_clones, (size_t)n_pairs * 4, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_seed, seed.data(), b8, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(d_slot, slot.data(), b8, cudaMemcpyHostToDevice, ctx->st));
+    ctx->stats = PgxStats();
+    CK(cudaEventRecord(ctx->ev[EV_PAIR0], ctx->st));
+    MRET(pgx::draw_pairs_gpu(ctx->st, n_pairs, d_t, d_ti, d_c, d_ci, d_n, d_seed, d_slot, d_ps, d_m,
+                             ctx->mixed.err));
+    std::vector<int> m(n_pairs);
+    CK(cudaMemcpyAsync(m.data(), d_m, (size_t)n_pairs * 4, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    // the successful clones of pair q follow those of pair q - 1 (as ph_pair_draw leaves a pair's clones)
+    long long off = 0;
+    for (int q = 0; q < n_pairs; q++) {
+        off += m[q];
+        if (off > 2147483647LL) return fail(ctx, PGX_E_LIMIT, "pgx_draw_pair_batch_gpu: more than 2^31 clones");
+        clone_off[q + 1] = (int)off;
+    }
+    CK(cudaMemcpyAsync(d_n, clone_off, (size_t)n_pairs * 4, cudaMemcpyHostToDevice, ctx->st));   // offsets
+    MRET(pgx::compact_pairs_gpu(ctx->st, n_pairs, d_slot, d_n, d_m, d_ps, d_out, ctx->mixed.err));
+    CK(cudaEventRecord(ctx->ev[EV_PAIR1], ctx->st));
+    if (off > 0) CK(cudaMemcpyAsync(ps, d_out, (size_t)off * 12 * 8, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->stats.ms_total = elapsed(ctx, EV_PAIR0, EV_PAIR1);
+    ctx->stats.clones = off;
+    ctx->stats.pairs = n_pairs;
+    ctx->stats.kernels = 1;
     return 0;
 }
 
@@ -1443,6 +1552,36 @@ int pgx_pair_targets(PgxContext *ctx, int n_pairs, const PhTarget *t, const int 
     sum.ms_total = sum.ms_pair;
     ctx->stats = sum;
     return rc;
+}
+
+int pgx_screen_shapes(int n, int *min_blocks) {
+    const int k = pgx::scan_shapes();
+    for (int v = 0; v < n && v < k && min_blocks; v++) min_blocks[v] = pgx::scan_shape(v);
+    return k;
+}
+
+int pgx_tune_screen(PgxContext *ctx, double tmax_myr, double chi2_max, double *ms, int *best) {
+    if (!ctx) return PGX_E_ARG;
+    if (!ctx->scan_blocks) return fail(ctx, PGX_E_ARG, "pgx_tune_screen: the block filter is off (PHYGAS_SCAN_BLOCKS)");
+    const int k = pgx::scan_shapes();
+    int b = 0;
+    double bms = 0.0;
+    long rows0 = -1;
+    for (int v = 0; v < k; v++) {
+        ctx->mixed.scan_variant = v;
+        long n = 0;
+        // twice: the first run of a shape loads its code
+        RET(pgx_screen_exec(ctx, tmax_myr, chi2_max, PGX_MIXED, &n));
+        RET(pgx_screen_exec(ctx, tmax_myr, chi2_max, PGX_MIXED, &n));
+        const double t = ctx->stats.ms_scan;
+        if (ms) ms[v] = t;
+        if (rows0 < 0) rows0 = n;
+        if (n != rows0) return fail(ctx, PGX_E_CUDA, "pgx_tune_screen: shape %d kept %ld pairs, shape 0 %ld", v, n, rows0);
+        if (v == 0 || t < bms) { b = v; bms = t; }
+    }
+    ctx->mixed.scan_variant = b;
+    if (best) *best = b;
+    return 0;
 }
 
 int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const double *ps, const int *steps,

@@ -6,6 +6,10 @@
 // FP32 value with a rigorous error bound.  Only what the bound cannot decide is recomputed with the FP64 path's own
 // functions (pgx_screen_math.cuh), so the rows are the FP64 path's rows bit for bit:
 //
+//   k_block_tables   per star and per cluster and block of 8 track points: the data of the block test
+//   k_mx_scan32_blocks  the filter below with a first level: one test per (pair, block of 8 points) settles the
+//                    block's points at once (most blocks); the blocks it cannot settle are walked point by point
+//                    as below, 32 blocks at a time on full warps.  The default (PHYGAS_SCAN_BLOCKS=0: k_mx_scan32)
 //   k_mx_scan32      FP32 filter, one thread per pair (warp = 32 stars x one cluster).  Per point: a cheap skip
 //                    test (triangle inequality in the M^-1 norm, one FP32 LDL^T) that settles most points; the rest
 //                    are queued per warp for the bounds LB <= chi2_64 <= UB on the FP64 path's value (the
@@ -375,7 +379,9 @@ __device__ __noinline__ bool point_at32_ol(const ScreenTables *T, int s, int c, 
 // have no block data.  A settled block's points all have chi2 >= cut in the FP64 path: they can neither be a kept
 // pair's minimum nor bring a pair under the cut, and they are left out of min ub, which only admits more candidates.
 // six resident blocks per SM asked of the compiler: 24 warps to issue from; the kernel is issue-bound
-__global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32_blocks(const __grid_constant__ ScreenTables T, float cut,
+template <int MINB>
+__global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __grid_constant__ ScreenTables T,
+                                                                      float cut,
                                                              unsigned char *__restrict__ flag,
                                                              float *__restrict__ ubmin,
                                                              unsigned long long *__restrict__ klist) {
@@ -851,6 +857,13 @@ __global__ void k_mx_kept_emit(int np, const PossPair *__restrict__ P, const Pai
 // entries beyond this are screened by the FP64 selection instead (identical rows; bounds the work buffers)
 constexpr long long kMaxEntries = 400000000LL;
 
+// the block filter's launch shapes: resident blocks per SM asked of the compiler (its register cap), in the order
+// pgx_screen_shapes lists them; the screen autotuner picks one per context
+constexpr int kScanVariants = 4;
+constexpr int kScanShapes[kScanVariants] = {6, 5, 7, 8};
+int scan_shapes() { return kScanVariants; }
+int scan_shape(int v) { return kScanShapes[v % kScanVariants]; }
+
 int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &m, cudaEvent_t ev_scan, int *total,
                  PgxStats *stats) {
     std::string &err = m.err;
@@ -870,10 +883,17 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
     }
     dim3 g(nc, (nt + kScanStars - 1) / kScanStars);
     const float cutf = (float)cut;
-    if (T.blk_t && T.blk_c)
-        k_mx_scan32_blocks<<<g, kScanStars, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
-                                                     Pb<unsigned long long>(m.kmin));
-    else
+    if (T.blk_t && T.blk_c) {
+        auto *fl = Pb<unsigned char>(m.flag);
+        auto *ub = Pb<float>(m.ub);
+        auto *km = Pb<unsigned long long>(m.kmin);
+        switch (kScanShapes[m.scan_variant % kScanVariants]) {
+            case 5: k_mx_scan32_blocks<5><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+            case 7: k_mx_scan32_blocks<7><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+            case 8: k_mx_scan32_blocks<8><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+            default: k_mx_scan32_blocks<6><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+        }
+    } else
         k_mx_scan32<<<g, kScanStars, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub),
                                               Pb<unsigned long long>(m.kmin));
     if ((rc = check(cudaGetLastError(), err, "k_mx_scan32"))) return rc;
@@ -1059,27 +1079,19 @@ __device__ __forceinline__ void draw32(const Fin32 &g, uint64_t w, float &x, flo
 
 // The 512 draws of a kept pair, in two phases.  A draw's first coordinate x = mx + l00 z0 depends on its first
 // Gaussian alone, and |x| >= max(r50, rtot) puts the draw outside both spheres whatever z1 and z2 are (r >= |x|, in
-// the FP64 path's arithmetic as well).  Phase 1 settles most draws with one generator output each: level A (below)
-// settles a draw from its u1 alone when even |z0| = sqrt(-2 ln u1) keeps x clear of both radii; the others get z0
-// (level B) and are settled when x, less its error bound (4 eps |mx| + |l00| (4 eps |z0| + e0 (1 + 2 eps)), the x
-// row of draw32's bound), clears the larger radius; with sigma of hundreds of pc against radii of tens, most do.
-// The rest are queued per warp in shared memory with
+// the FP64 path's arithmetic as well).  Phase 1 draws z0 for all 512 and settles the draws whose x, less its error
+// bound (4 eps |mx| + |l00| (4 eps |z0| + e0 (1 + 2 eps)), the x row of draw32's bound), clears the larger radius;
+// with sigma of hundreds of pc against radii of tens, most do.  The rest are queued per warp in shared memory with
 // z0 and its bound, and phase 2 completes them 32 at a time on full warps: z1, z2, the position and its bound as
 // draw32 computes them, and the FP64 recheck of a draw within its bound of a radius -- the counts are the FP64
 // path's, and the same as drawing every draw in full.
 constexpr int kFinWarps = 8, kFinQueue = 64;
-constexpr double kLevelA = 1.5;         // R* from which level A is worth its queue (it settles >= 67.5 % of draws)
-
-// the FP64 recheck of a draw (rare: about one draw in 3e6), kept out of line so the kernel's code stays small
-__device__ __noinline__ int draw_inside64_at(const FinishIn *f, int i) { return draw_inside64(*f, i); }
 
 __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const FinishIn *__restrict__ fin,
                                                                 ScreenRowDev *__restrict__ rows,
                                                                 int *__restrict__ nrecheck) {
     __shared__ int s_i[kFinWarps][kFinQueue];
     __shared__ float s_z[kFinWarps][kFinQueue], s_a[kFinWarps][kFinQueue], s_e[kFinWarps][kFinQueue];
-    __shared__ int s_ia[kFinWarps][kFinQueue];                   // level A: draws left open, and their first output
-    __shared__ uint64_t s_ga[kFinWarps][kFinQueue];
     const int h = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
     if (h >= n) return;                                           // the whole warp: uniform
     const Fin32 g = fin32(fin[h], lane);
@@ -1112,7 +1124,7 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
                 in50 += d50 < 0.f;
                 intot += dt < 0.f;
             } else {
-                const int v = draw_inside64_at(fin + h, i);         // the FP64 path's own draw
+                const int v = draw_inside64(fin[h], i);             // the FP64 path's own draw
                 in50 += v & 1;
                 intot += v >> 1;
                 rechecks++;
@@ -1120,55 +1132,32 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
         }
         __syncwarp();
     };
-    // Level A, before any transcendental: |z0| <= sqrt(-2 ln u1) in the FP64 path, so a draw whose u1 is at least
-    // U* = exp(-R*^2 / 2), R* = (|mx| - max(r50, rtot)) / |l00|, has |x| >= max(r50, rtot) whatever its angle: outside
-    // both spheres.  U* is taken in FP64 once per pair with relative margins of 1e-12 on R* and 1e-10 on R*^2 (far
-    // above the FP64 log's and exp's last-bit errors and the rounding of x = mx + l00 z0), and the test is an integer
-    // compare of u1's 53 bits with ceil(U* 2^53).  It is used for pairs with R* >= kLevelA (then it settles at least
-    // 1 - exp(-kLevelA^2 / 2) of the draws); for the others every draw goes on.  The open draws are queued (index,
-    // first generator output) and get the z0 test above (level B), 32 at a time on full warps.
-    uint64_t kstar = (1ull << 53) + 1;                           // no draw settles at level A
-    {
-        const double mxa = fabs(fin[h].mx), l00a = fabs(fin[h].l00), ro = fmax(fin[h].r50, fin[h].rt);
-        const double R = mxa > ro ? (mxa - ro) / l00a * (1.0 - 1e-12) : 0.0;
-        if (R >= kLevelA) {
-            const double U = exp(-0.5 * R * R * (1.0 - 1e-10)) * (1.0 + 1e-12);
-            if (U < 1.0) kstar = (uint64_t)ceil(U * 9007199254740992.0);
-        }
-    }
-    int qn = 0, an = 0;
-    // level B for level-A queue entries [0, cnt), one per lane: z0 and its bound; the draws still open go to the
-    // phase-2 queue, completed 32 at a time (all of them when `last`)
-    auto level_b = [&](int cnt, bool last) {
-        __syncwarp();
-        bool open = false;
-        int i = 0;
-        float z0 = 0.f, a0 = 0.f, e0 = 0.f;
-        if (lane < cnt) {
-            i = s_ia[wq][lane];
-            const uint64_t w = seed + (uint64_t)(6 * i) * kGolden;
-            gauss32(s_ga[wq][lane], splitmix_mix(w + 2 * kGolden), z0, a0, e0);
-            const float x = fmaf(g.l00, z0, g.mx);
-            const float ex0 = fmaf(eA0, a0, fmaf(eE0, e0, eM0));
-            open = !(fabsf(x) * (1.f - 4.f * kEps32) - ex0 >= rout);
-        }
+    // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden
+    uint64_t w = seed + (uint64_t)(6 * lane) * kGolden;
+    int qn = 0;
+#pragma unroll 1
+    for (int q = 0; q < 16; q++, w += 192 * kGolden) {
+        float z0, a0, e0;
+        gauss32(splitmix_mix(w + kGolden), splitmix_mix(w + 2 * kGolden), z0, a0, e0);
+        const float x = fmaf(g.l00, z0, g.mx);
+        const float ex0 = fmaf(eA0, a0, fmaf(eE0, e0, eM0));
+        const bool open = !(fabsf(x) * (1.f - 4.f * kEps32) - ex0 >= rout);
         const unsigned m = __ballot_sync(0xffffffffu, open);
         if (open) {
             const int at = qn + __popc(m & ((1u << lane) - 1u));
-            s_i[wq][at] = i;
+            s_i[wq][at] = lane + 32 * q;
             s_z[wq][at] = z0;
             s_a[wq][at] = a0;
             s_e[wq][at] = e0;
         }
         qn += __popc(m);
-        while (qn >= 32 || (last && qn > 0)) {
-            const int c = min(qn, 32);
-            complete(c);
-            const int rest = qn - c;
+        if (qn >= 32) {
+            complete(32);
+            const int rest = qn - 32;
             int vi = 0;
             float vz = 0.f, va = 0.f, ve = 0.f;
             if (lane < rest) {
-                vi = s_i[wq][c + lane]; vz = s_z[wq][c + lane]; va = s_a[wq][c + lane]; ve = s_e[wq][c + lane];
+                vi = s_i[wq][32 + lane]; vz = s_z[wq][32 + lane]; va = s_a[wq][32 + lane]; ve = s_e[wq][32 + lane];
             }
             __syncwarp();
             if (lane < rest) {
@@ -1176,38 +1165,8 @@ __global__ void __launch_bounds__(kFinWarps * 32) k_mx_finish32(int n, const Fin
             }
             qn = rest;
         }
-        __syncwarp();
-    };
-    // draw i uses calls 6i+1 .. 6i+6 of the pair's splitmix64 stream, whose state is seed + call * golden; the 17th
-    // pass draws nothing and flushes both queues (one call site for each stage keeps the kernel's code small)
-    uint64_t w = seed + (uint64_t)(6 * lane) * kGolden;
-#pragma unroll 1
-    for (int q = 0; q <= 16; q++, w += 192 * kGolden) {
-        bool open = false;
-        uint64_t ga = 0;
-        if (q < 16) {
-            ga = splitmix_mix(w + kGolden);
-            open = (ga >> 11) < kstar;
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, open);
-        if (open) {
-            const int at = an + __popc(m & ((1u << lane) - 1u));
-            s_ia[wq][at] = lane + 32 * q;
-            s_ga[wq][at] = ga;
-        }
-        an += __popc(m);
-        if (an >= 32 || q == 16) {
-            const int c = min(an, 32);
-            level_b(c, q == 16);
-            const int rest = an - c;
-            int vi = 0;
-            uint64_t vg = 0;
-            if (lane < rest) { vi = s_ia[wq][c + lane]; vg = s_ga[wq][c + lane]; }
-            __syncwarp();
-            if (lane < rest) { s_ia[wq][lane] = vi; s_ga[wq][lane] = vg; }
-            an = rest;
-        }
     }
+    if (qn > 0) complete(qn);
     in50 = __reduce_add_sync(0xffffffffu, in50);
     intot = __reduce_add_sync(0xffffffffu, intot);
     rechecks = __reduce_add_sync(0xffffffffu, rechecks);

@@ -15,7 +15,11 @@ struct DevBuf {
 struct MixedBufs {
     DevBuf order, ub, kmin, flag, cnt, off, total, kept, cand, cand_off, ent, entq, aux, ovf;
     std::string err;
+    int scan_variant = 0;             // the block filter's launch shape (scan_shape), chosen by the screen autotuner
 };
+// the block filter's launch shapes: how many, and shape v's resident blocks per SM asked of the compiler
+int scan_shapes();
+int scan_shape(int v);
 
 void mixed_free(MixedBufs &m);
 // a device buffer of at least `bytes` (grown by a quarter more when it has to grow); a CUDA status as a PGX code
@@ -33,6 +37,18 @@ int mixed_cluster_aux(cudaStream_t st, int nc, int nmax, const int *cn, const do
 // diagonal or none) into blk [ceil(nmax / kBlk)][N][4] float4: what the filter's block test reads
 int block_tables(cudaStream_t st, int N, int nmax, const int *npts, const double *t64, const float *lm,
                  const double *R2, float4 *blk, std::string &err);
+// the draws from the measurement errors on the device (pgx_draws.cu): targets' and clusters' nominal states and
+// covariances (seed[i] = ph_seed("lin", id)), and the clones of pairs (seed[q] = ph_seed(id, name), clone slots
+// slot[q], successful clones m[q]); every pointer is device memory
+int draw_targets_gpu(cudaStream_t st, int n, const PhTarget *t, int n_samp, const uint64_t *seed, double *ps0,
+                     double *sig, std::string &err);
+int draw_clusters_gpu(cudaStream_t st, int n, const PhCluster *c, int n_samp, const uint64_t *seed, double *ps0,
+                      double *sig, std::string &err);
+int draw_pairs_gpu(cudaStream_t st, int n_pairs, const PhTarget *t, const int *ti, const PhCluster *c,
+                   const int *ci, const int *n_clones, const uint64_t *seed, const long long *slot, double *ps,
+                   int *m, std::string &err);
+int compact_pairs_gpu(cudaStream_t st, int n_pairs, const long long *slot, const int *off, const int *m,
+                      const double *src, double *dst, std::string &err);
 // FP32 filter + FP64 recheck: the kept pairs in (star, cluster) order, identical to the FP64 path's
 int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &m, cudaEvent_t ev_scan, int *total,
                  PgxStats *stats);

@@ -168,3 +168,21 @@ def test_block_test_changes_no_row(built):
             os.environ["PHYGAS_SCAN_BLOCKS"] = old
     assert len(rows["1"]) > 1000
     assert rows["1"].tobytes() == rows["0"].tobytes() == rows["fp64"].tobytes()
+
+
+def test_screen_autotuner_keeps_the_rows(built):
+    """pgx_tune_screen times every launch shape of the block filter on the staged chunk and keeps the fastest; the
+    rows after tuning are the rows before."""
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "screen", 512, 1006)
+        clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    tmax = max(c.tmax_myr for c in clusters)
+    with pg.Context(0) as c:
+        c.set_clusters(clusters)
+        draws = pg.draw_targets(stars)
+        before = c.screen(*draws, tmax)
+        c.stage(*draws)
+        best, table = c.tune_screen(tmax)
+        assert 0 <= best < len(table) and all(ms > 0 for _, ms in table)
+        after = c.screen(*draws, tmax)
+    assert before.tobytes() == after.tobytes()

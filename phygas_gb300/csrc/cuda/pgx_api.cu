@@ -73,6 +73,10 @@ struct PgxContext {
     // resident cluster table (original cluster order)
     int nc = 0, ncp = 0;
     Buf c64, c32, clm, cn, cR2, cr50, crt, cname, cblk;
+    // the staged filter (PHYGAS_SCAN_TMA=1 at pgx_open): the cluster table cluster-major, and the wait flag
+    bool scan_tma = false;
+    Buf cblk_cm, c32_cm, clm_cm, werr;
+    int nblk = 0, lm_pitch = 0;
     Buf x_draw, x_draw_ps;                     // device draws: records, seeds and outputs; clone slots
     // the mixed filter's block test (one test settles eight points of a pair); PHYGAS_SCAN_BLOCKS=0 at pgx_open
     // turns it off, and every point is walked (the same rows either way)
@@ -222,6 +226,14 @@ pgx::ScreenTables tables(PgxContext *ctx, TrackSlot &k) {
     if (ctx->scan_blocks && k.blk.p && ctx->cblk.p) {
         T.blk_t = P<float4>(k.blk);
         T.blk_c = P<float4>(ctx->cblk);
+        if (ctx->scan_tma && ctx->cblk_cm.p) {
+            T.blk_cm = P<float4>(ctx->cblk_cm);
+            T.c32_cm = P<float4>(ctx->c32_cm);
+            T.lm_cm = P<float>(ctx->clm_cm);
+            T.nblk = ctx->nblk;
+            T.lm_pitch = ctx->lm_pitch;
+            T.wait_err = P<int>(ctx->werr);
+        }
     }
     return T;
 }
@@ -385,6 +397,11 @@ int screen_slot(PgxContext *ctx, int s, double cut, int precision, long *n_rows,
     }
     CK(cudaEventRecord(ctx->ev[EV_FINISH], ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
+    if (T.wait_err) {
+        int werr = 0;
+        CK(cudaMemcpy(&werr, T.wait_err, 4, cudaMemcpyDeviceToHost));
+        if (werr) return fail(ctx, PGX_E_CUDA, "screen: a bulk copy's wait in the filter ran out");
+    }
     PgxStats &S = ctx->stats;
     S.ms_orbit = elapsed(ctx, EV_START, EV_ORBIT);
     S.ms_cov = elapsed(ctx, EV_ORBIT, EV_COV);
@@ -418,6 +435,7 @@ int pgx_open(int device, PgxContext **out) {
     ctx = new PgxContext();
     ctx->device = device;
     if (const char *e = getenv("PHYGAS_SCAN_BLOCKS")) ctx->scan_blocks = atoi(e) != 0;
+    if (const char *e = getenv("PHYGAS_SCAN_TMA")) ctx->scan_tma = atoi(e) != 0;
     if (const char *e = getenv("PHYGAS_FAIL_ALLOC_AT")) ctx->fail_alloc_at = atol(e);
     int rc = 0;
     {
@@ -454,7 +472,8 @@ void pgx_close(PgxContext *ctx) {
                    &ctx->x_npts,
                    &ctx->x_opos, &ctx->x_ovel, &ctx->x_t64, &ctx->x_t32, &ctx->rows_b[0], &ctx->rows_b[1],
                    &ctx->lab_names, &ctx->lab_kinds, &ctx->lab_age16, &ctx->lab_age84, &ctx->part_in,
-                   &ctx->cblk, &ctx->x_draw, &ctx->x_draw_ps};
+                   &ctx->cblk, &ctx->x_draw, &ctx->x_draw_ps, &ctx->cblk_cm, &ctx->c32_cm, &ctx->clm_cm,
+                   &ctx->werr};
     for (Buf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (ctx->h_part) cudaFreeHost(ctx->h_part);
@@ -927,6 +946,19 @@ int pgx_screen_clusters(PgxContext *ctx, int nc, const double *ps0, const double
     RET(ensure(ctx, ctx->cblk, (size_t)((nmax + pgx::kBlockPoints - 1) / pgx::kBlockPoints) * nc * 64));
     MRET(pgx::block_tables(ctx->st, nc, nmax, P<int>(ctx->cn), P<double>(ctx->c64), P<float>(ctx->clm),
                            P<double>(ctx->cR2), P<float4>(ctx->cblk), ctx->mixed.err));
+    if (ctx->scan_tma) {
+        ctx->nblk = (nmax + pgx::kBlockPoints - 1) / pgx::kBlockPoints;
+        ctx->lm_pitch = (nmax + 3) & ~3;
+        RET(ensure(ctx, ctx->cblk_cm, (size_t)ctx->nblk * nc * 64));
+        RET(ensure(ctx, ctx->c32_cm, (size_t)nmax * nc * 48));
+        RET(ensure(ctx, ctx->clm_cm, (size_t)ctx->lm_pitch * nc * 4));
+        RET(ensure(ctx, ctx->werr, 16));
+        CK(cudaMemsetAsync(ctx->clm_cm.p, 0, (size_t)ctx->lm_pitch * nc * 4, ctx->st));
+        CK(cudaMemsetAsync(ctx->werr.p, 0, 16, ctx->st));
+        MRET(pgx::cluster_major(ctx->st, nc, nmax, ctx->nblk, ctx->lm_pitch, P<float4>(ctx->cblk),
+                                P<float4>(ctx->c32), P<float>(ctx->clm), P<float4>(ctx->cblk_cm),
+                                P<float4>(ctx->c32_cm), P<float>(ctx->clm_cm), ctx->mixed.err));
+    }
     CK(cudaStreamSynchronize(ctx->st));
     return 0;
 }

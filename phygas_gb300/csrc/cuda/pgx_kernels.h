@@ -47,6 +47,13 @@ struct ScreenTables {
     // per object and block of kBlockPoints points, the block test's data ([b][n][4] float4, pgx_bounds32.cuh
     // block_skip32); nullptr: the mixed filter walks every point
     const float4 *blk_t = nullptr, *blk_c = nullptr;
+    // the cluster table cluster-major, for the filter variant that copies a cluster's data into shared memory with
+    // bulk copies (TMA): blk_cm [nc][nblk][4], c32_cm [nc][ncp][3] float4, lm_cm [nc][lm_pitch] (nullptr: not staged);
+    // wait_err: set when a bulk copy's wait ran out (never expected; the host reports it)
+    const float4 *blk_cm = nullptr, *c32_cm = nullptr;
+    const float *lm_cm = nullptr;
+    int nblk = 0, lm_pitch = 0;
+    int *wait_err = nullptr;
     const int *cn;
     const double *R2, *r50, *rtot;
     const char *cname;               // nc * 40 bytes

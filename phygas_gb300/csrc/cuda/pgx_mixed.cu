@@ -209,6 +209,31 @@ int block_tables(cudaStream_t st, int N, int nmax, const int *npts, const double
     return check(cudaGetLastError(), err, "k_block_tables");
 }
 
+// The cluster table cluster-major for the staged filter: one cluster's block-table column, FP32 track and lambda
+// bounds each contiguous (the bulk copies move contiguous ranges), lambda rows padded to lm_pitch (a multiple of 4).
+__global__ void k_cluster_major(int nc, int ncp, int nblk, int lm_pitch, const float4 *__restrict__ blk,
+                                const float4 *__restrict__ c32, const float *__restrict__ lm, float4 *__restrict__ blk_cm,
+                                float4 *__restrict__ c32_cm, float *__restrict__ lm_cm) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int rows = ncp > nblk ? ncp : nblk;
+    if (idx >= (size_t)nc * rows) return;
+    const int c = (int)(idx % nc), k = (int)(idx / nc);
+    if (k < nblk)
+        for (int q = 0; q < 4; q++) blk_cm[((size_t)c * nblk + k) * 4 + q] = blk[((size_t)k * nc + c) * 4 + q];
+    if (k < ncp) {
+        for (int q = 0; q < 3; q++) c32_cm[((size_t)c * ncp + k) * 3 + q] = c32[((size_t)k * nc + c) * 3 + q];
+        lm_cm[(size_t)c * lm_pitch + k] = lm[(size_t)k * nc + c];
+    }
+}
+
+int cluster_major(cudaStream_t st, int nc, int ncp, int nblk, int lm_pitch, const float4 *blk, const float4 *c32,
+                  const float *lm, float4 *blk_cm, float4 *c32_cm, float *lm_cm, std::string &err) {
+    const size_t work = (size_t)nc * (ncp > nblk ? ncp : nblk);
+    k_cluster_major<<<(unsigned)((work + 255) / 256), 256, 0, st>>>(nc, ncp, nblk, lm_pitch, blk, c32, lm, blk_cm,
+                                                                    c32_cm, lm_cm);
+    return check(cudaGetLastError(), err, "k_cluster_major");
+}
+
 // separation of star and cluster at one point from the split FP32 positions
 __device__ __forceinline__ void sep32(const float4 &t0, const float4 &t1, const float4 &c0, const float4 &c1,
                                       float (&m)[3]) {
@@ -361,6 +386,51 @@ __global__ void __launch_bounds__(kScanStars, 6) k_mx_scan32(ScreenTables T, flo
     }
 }
 
+// a cluster value: from shared memory (staged) or through the read-only cache
+template <bool STAGE, class V> __device__ __forceinline__ V ldc(const V *p) {
+    if (STAGE) return *p;
+    return __ldg(p);
+}
+
+// The bulk copies of one cluster's data into shared memory on an mbarrier, and the wait for them.  The wait is
+// bounded: should it ever run out, the CTA records it in T.wait_err (the host turns that into an error), waits once
+// more, bounded too, for its copies in flight, and reports false (the CTA then returns without output).
+__device__ bool stage_cluster(const ScreenTables &T, int c, float4 *sb, float4 *sc, float *sl, uint64_t *bar) {
+    const unsigned ab = (unsigned)__cvta_generic_to_shared(bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(ab) : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int n = T.cn[c];
+        const unsigned b1 = (unsigned)T.nblk * 64u, b2 = (unsigned)n * 48u, b3 = ((unsigned)n * 4u + 15u) & ~15u;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(ab), "r"(b1 + b2 + b3)
+                     : "memory");
+        const void *g1 = T.blk_cm + (size_t)c * T.nblk * 4, *g2 = T.c32_cm + (size_t)c * T.ncp * 3;
+        const void *g3 = T.lm_cm + (size_t)c * T.lm_pitch;
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"((unsigned)__cvta_generic_to_shared(sb)), "l"(g1), "r"(b1), "r"(ab) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"((unsigned)__cvta_generic_to_shared(sc)), "l"(g2), "r"(b2), "r"(ab) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"((unsigned)__cvta_generic_to_shared(sl)), "l"(g3), "r"(b3), "r"(ab) : "memory");
+    }
+    auto wait = [&]() {
+        for (int it = 0; it < (1 << 22); it++) {
+            unsigned ok;
+            asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                         : "=r"(ok) : "r"(ab) : "memory");
+            if (ok) return true;
+        }
+        return false;
+    };
+    if (wait()) return true;
+    if (T.wait_err) atomicExch(T.wait_err, 1);
+    wait();
+    return false;
+}
+
 // the full bounds of a point, out of line (the block kernel's single copy of point_bound32)
 __device__ __noinline__ bool point_at32_ol(const ScreenTables *T, int s, int c, int k, float cut, Bound *b) {
     return point_at32(*T, s, c, k, cut, *b);
@@ -379,12 +449,26 @@ __device__ __noinline__ bool point_at32_ol(const ScreenTables *T, int s, int c, 
 // have no block data.  A settled block's points all have chi2 >= cut in the FP64 path: they can neither be a kept
 // pair's minimum nor bring a pair under the cut, and they are left out of min ub, which only admits more candidates.
 // six resident blocks per SM asked of the compiler: 24 warps to issue from; the kernel is issue-bound
-template <int MINB>
+template <int MINB, bool STAGE>
 __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __grid_constant__ ScreenTables T,
-                                                                      float cut,
-                                                             unsigned char *__restrict__ flag,
-                                                             float *__restrict__ ubmin,
-                                                             unsigned long long *__restrict__ klist) {
+                                                                      float cut, unsigned char *__restrict__ flag,
+                                                                      float *__restrict__ ubmin,
+                                                                      unsigned long long *__restrict__ klist) {
+    // STAGE: this CTA's cluster -- its block-table column, its FP32 track and its lambda bounds, contiguous in the
+    // cluster-major copies -- comes into shared memory by three bulk copies (TMA, cp.async.bulk) on one mbarrier;
+    // the filter then reads the cluster from there instead of through the L1 cache
+    extern __shared__ __align__(128) unsigned char s_dyn[];
+    __shared__ __align__(8) uint64_t s_bar;
+    const float4 *cblk = T.blk_c + (size_t)blockIdx.x * 4, *cc32 = T.c32 + (size_t)blockIdx.x * 3;
+    const float *clm = T.lm_c + blockIdx.x;
+    size_t cbs = (size_t)T.nc * 4, ccs = (size_t)T.nc * 3, cls = T.nc;         // strides between points / blocks
+    if (STAGE) {
+        float4 *sb = reinterpret_cast<float4 *>(s_dyn), *sc = sb + (size_t)T.nblk * 4;
+        float *sl = reinterpret_cast<float *>(sc + (size_t)T.ncp * 3);
+        if (!stage_cluster(T, blockIdx.x, sb, sc, sl, &s_bar)) return;
+        cblk = sb; cc32 = sc; clm = sl;
+        cbs = 4; ccs = 3; cls = 1;
+    }
     __shared__ int s_q[kScanStars / 32][kQueue];                  // points waiting for their full bounds
     __shared__ int s_bq[kScanStars / 32][kQueue];                 // blocks waiting to be walked point by point
     __shared__ float s_lb[kScanStars / 32][32], s_ub[kScanStars / 32][32];
@@ -453,7 +537,7 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
                            const float (&mc)[3], const float (&mn)[3]) {
         const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
         const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
-        const float lmt = T.lm_t[(size_t)k * NT + st], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
+        const float lmt = T.lm_t[(size_t)k * NT + st], lmc = ldc<STAGE>(clm + (size_t)k * cls);
         return !point_skip32(St, Sc, lmt, lmc, mc, mn, cut);
     };
     // ---- level 1: blocks of kBlk points whose position reference km = kBlk b + kBlk/2 lies on the pair's track
@@ -465,13 +549,13 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
             const int e = lane < cnt ? s_bq[w][lane] : 0;
             const int o = e & 31, b = e >> 5, st = s0 + o;
             const int k0 = b * kBlk, k1 = min(k0 + kBlk, n);
-            const float4 *tp = T.t32 + (size_t)st * 3, *cp = T.c32 + (size_t)c * 3;
+            const float4 *tp = T.t32 + (size_t)st * 3;
             float4 t0, t1, t2, c0, c1, c2;
             float mc[3] = {0.f, 0.f, 0.f};
             if (lane < cnt) {
-                const float4 *a = tp + (size_t)k0 * NT * 3, *q = cp + (size_t)k0 * NC * 3;
+                const float4 *a = tp + (size_t)k0 * NT * 3, *q = cc32 + (size_t)k0 * ccs;
                 t0 = a[0]; t1 = a[1]; t2 = a[2];
-                c0 = __ldg(q); c1 = __ldg(q + 1); c2 = __ldg(q + 2);
+                c0 = ldc<STAGE>(q); c1 = ldc<STAGE>(q + 1); c2 = ldc<STAGE>(q + 2);
                 sep32(t0, t1, c0, c1, mc);
             }
             for (int j = 0; j < kBlk; j++) {
@@ -482,9 +566,9 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
                     const float4 T1 = t1, T2 = t2, C1 = c1, C2 = c2;
                     float mn[3] = {mc[0], mc[1], mc[2]};
                     if (k + 1 < n) {
-                        const float4 *a = tp + (size_t)(k + 1) * NT * 3, *q = cp + (size_t)(k + 1) * NC * 3;
+                        const float4 *a = tp + (size_t)(k + 1) * NT * 3, *q = cc32 + (size_t)(k + 1) * ccs;
                         t0 = a[0]; t1 = a[1]; t2 = a[2];
-                        c0 = __ldg(q); c1 = __ldg(q + 1); c2 = __ldg(q + 2);
+                        c0 = ldc<STAGE>(q); c1 = ldc<STAGE>(q + 1); c2 = ldc<STAGE>(q + 2);
                         sep32(t0, t1, c0, c1, mn);
                     }
                     need = point_needs(st, k, T1, T2, C1, C2, mc, mn);
@@ -494,7 +578,7 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
             }
         };
         int bn = 0;
-        const float4 *bt = T.blk_t + (size_t)s * 4, *bc = T.blk_c + (size_t)c * 4;
+        const float4 *bt = T.blk_t + (size_t)s * 4;
         // blocks 0 .. nbt-1 get the test; block nbt, the points after them (fewer than five), is walked untested;
         // the last pass tests nothing and walks what is left (one call site keeps the kernel's code small)
         const int kt = nbt * kBlk, nball = nbt + (kt < n ? 1 : 0);
@@ -502,12 +586,12 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
             bool need = false;
             if (b < nbt && active) {
                 const int km = b * kBlk + kBlk / 2;
-                const float4 *a = bt + (size_t)b * NT * 4, *q = bc + (size_t)b * NC * 4;
+                const float4 *a = bt + (size_t)b * NT * 4, *q = cblk + (size_t)b * cbs;
                 const float4 BT[4] = {a[0], a[1], a[2], a[3]};
-                const float4 BC[4] = {__ldg(q), __ldg(q + 1), __ldg(q + 2), __ldg(q + 3)};
-                const float4 *tm = T.t32 + ((size_t)km * NT + s) * 3, *cm = T.c32 + ((size_t)km * NC + c) * 3;
+                const float4 BC[4] = {ldc<STAGE>(q), ldc<STAGE>(q + 1), ldc<STAGE>(q + 2), ldc<STAGE>(q + 3)};
+                const float4 *tm = T.t32 + ((size_t)km * NT + s) * 3, *cm = cc32 + (size_t)km * ccs;
                 float mref[3];
-                sep32(tm[0], tm[1], __ldg(cm), __ldg(cm + 1), mref);
+                sep32(tm[0], tm[1], ldc<STAGE>(cm), ldc<STAGE>(cm + 1), mref);
                 need = !block_skip32(BT, BC, mref, cut);
             } else if (b < nball) {
                 need = active;
@@ -887,11 +971,16 @@ int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &
         auto *fl = Pb<unsigned char>(m.flag);
         auto *ub = Pb<float>(m.ub);
         auto *km = Pb<unsigned long long>(m.kmin);
-        switch (kScanShapes[m.scan_variant % kScanVariants]) {
-            case 5: k_mx_scan32_blocks<5><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
-            case 7: k_mx_scan32_blocks<7><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
-            case 8: k_mx_scan32_blocks<8><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
-            default: k_mx_scan32_blocks<6><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+        if (T.blk_cm && T.c32_cm && T.lm_cm) {
+            const size_t dyn = (size_t)T.nblk * 64 + (size_t)T.ncp * 48 + (size_t)T.lm_pitch * 4;
+            k_mx_scan32_blocks<6, true><<<g, kScanStars, dyn, st>>>(T, cutf, fl, ub, km);
+        } else {
+            switch (kScanShapes[m.scan_variant % kScanVariants]) {
+                case 5: k_mx_scan32_blocks<5, false><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+                case 7: k_mx_scan32_blocks<7, false><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+                case 8: k_mx_scan32_blocks<8, false><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+                default: k_mx_scan32_blocks<6, false><<<g, kScanStars, 0, st>>>(T, cutf, fl, ub, km); break;
+            }
         }
     } else
         k_mx_scan32<<<g, kScanStars, 0, st>>>(T, cutf, Pb<unsigned char>(m.flag), Pb<float>(m.ub),

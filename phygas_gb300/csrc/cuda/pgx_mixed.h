@@ -49,6 +49,10 @@ int draw_pairs_gpu(cudaStream_t st, int n_pairs, const PhTarget *t, const int *t
                    int *m, std::string &err);
 int compact_pairs_gpu(cudaStream_t st, int n_pairs, const long long *slot, const int *off, const int *m,
                       const double *src, double *dst, std::string &err);
+// the cluster table cluster-major (blk [nblk][nc][4] -> [nc][nblk][4], c32 [ncp][nc][3] -> [nc][ncp][3], lm
+// [ncp][nc] -> [nc][lm_pitch]): the staged filter's bulk copies read contiguous ranges
+int cluster_major(cudaStream_t st, int nc, int ncp, int nblk, int lm_pitch, const float4 *blk, const float4 *c32,
+                  const float *lm, float4 *blk_cm, float4 *c32_cm, float *lm_cm, std::string &err);
 // FP32 filter + FP64 recheck: the kept pairs in (star, cluster) order, identical to the FP64 path's
 int mixed_select(cudaStream_t st, const ScreenTables &T, double cut, MixedBufs &m, cudaEvent_t ev_scan, int *total,
                  PgxStats *stats);

@@ -186,3 +186,28 @@ def test_screen_autotuner_keeps_the_rows(built):
         assert 0 <= best < len(table) and all(ms > 0 for _, ms in table)
         after = c.screen(*draws, tmax)
     assert before.tobytes() == after.tobytes()
+
+
+def test_staged_filter_changes_no_row(built):
+    """The block filter with each cluster's data copied into shared memory by bulk copies (PHYGAS_SCAN_TMA=1): the
+    same rows as the filter reading the cluster table through the cache."""
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "screen", 512, 1007)
+        clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    tmax = max(c.tmax_myr for c in clusters)
+    draws = pg.draw_targets(stars)
+    rows = {}
+    old = os.environ.get("PHYGAS_SCAN_TMA")
+    try:
+        for flag in ("0", "1"):
+            os.environ["PHYGAS_SCAN_TMA"] = flag
+            with pg.Context(0) as c:
+                c.set_clusters(clusters)
+                rows[flag] = c.screen(*draws, tmax, 25.0, pg.PGX_MIXED)
+    finally:
+        if old is None:
+            os.environ.pop("PHYGAS_SCAN_TMA", None)
+        else:
+            os.environ["PHYGAS_SCAN_TMA"] = old
+    assert len(rows["0"]) > 1000
+    assert rows["0"].tobytes() == rows["1"].tobytes()

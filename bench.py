@@ -11,7 +11,7 @@ it).
                 star inputs (nominal state + covariance of the draws) already in HBM; L2 flushed between steps
   e2e           the same metric through the C-ABI call a user makes (pgx_screen_chunks): host star records in, host
                 rows out, host draws and host<->device copies inside the timed region
-  roofline      the step's largest kernel, the FP32 filter k_mx_scan32: the survey's 126 flops per pair-point over
+  roofline      the step's largest kernel, the FP32 block filter: the survey's 126 flops per pair-point over
                 its CUDA-event launch time, against the FP32 FMA peak measured in this run by the library's probe
   cpu_baseline  the oracle (a pinned C restatement of the reference's CPU code) on all host cores, bounded sample;
                 its rows are kept and compared with the GPU's rows of the same stars (parity_vs_oracle)
@@ -67,12 +67,12 @@ FP64_INSTR_PER_CLONE_STEP = 73.3 + 9.3 + 58.9
 # DRAM traffic of one k_stm_orbits launch on the whole chunk (dram__bytes_read.sum + dram__bytes_write.sum, one ncu
 # capture of `bench.py --mode screen --stars 20000 --parts 1`): 6.7 MB read + 711.9 MB of orbit output written
 ORBIT_TRAFFIC_BYTES = 718.6e6
-# DRAM traffic of k_mx_scan32 per pair-point (read + write of one ncu capture of the same command, whole-chunk
-# launch: 1,067 MB for 4.99e9 pair-points); a part's launch moves its share
+# DRAM traffic of the block filter k_mx_scan32_blocks per pair-point (read + write of one ncu capture of one part's
+# launch, `bench.py --mode screen --stars 2500 --parts 1`: 6.30e8 pair-points); a part's launch moves its share
 SCAN_TRAFFIC_PER_PAIR_POINT = 1067e6 / 4.99e9
-# warp instructions k_mx_scan32 issues per pair-point (smsp__inst_executed.sum of the same capture, 4.10e10 for the
-# chunk); its issue bound is 4 warp instructions per clock per SM (one per scheduler)
-SCAN_WARP_INSTR_PER_PAIR_POINT = 4.10e10 / 4.99e9
+# warp instructions the block filter issues per pair-point (smsp__inst_executed.sum of the same capture: 3.84e9 for
+# 6.30e8 pair-points); its issue bound is 4 warp instructions per clock per SM (one per scheduler)
+SCAN_WARP_INSTR_PER_PAIR_POINT = 3.8375e9 / 6.303e8
 ISSUE_PER_CLK_SM = 4
 
 
@@ -488,8 +488,9 @@ def reference_arm(args):
 
 
 def scan_roofline(stats, clocks, pp, fp32_peak, parts):
-    """The step's largest kernel, k_mx_scan32 (one launch per part), against the FP32 FMA peak: the survey's 126
-    flops per pair-point over the launches' CUDA-event time; with it the issue-slot fraction (the bound that
+    """The step's largest kernel, the block filter k_mx_scan32_blocks (one launch per part), against the FP32 FMA
+    peak: the survey's 126 flops per pair-point over the launches' CUDA-event time; with it the issue-slot fraction
+    (the bound that
     applies to its mix of FP32, integer and compare work) from the warp instructions per pair-point of an ncu
     capture, at the SM clock sampled during the steps."""
     import torch
@@ -499,7 +500,7 @@ def scan_roofline(stats, clocks, pp, fp32_peak, parts):
     if not ms:
         return None
     flops = FLOPS_PER_PAIR_POINT * pp
-    out = {"bound": "fp32", "kernel": "k_mx_scan32", "achieved": flops / (ms * 1e-3) / 1e12,
+    out = {"bound": "fp32", "kernel": "k_mx_scan32_blocks", "achieved": flops / (ms * 1e-3) / 1e12,
            "peak": fp32_peak / 1e12, "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / fp32_peak,
            "peak_source": "FP32 FMA probe kernel of this run (pgx_peaks); not in MEASURED_PEAKS.json",
            "traffic": SCAN_TRAFFIC_PER_PAIR_POINT * pp / parts,

@@ -812,13 +812,13 @@ int pgx_check_blocks(PgxContext *ctx, double tmax_myr, double chi2_max, long *co
     if (!ctx->scan_blocks) return fail(ctx, PGX_E_ARG, "pgx_check_blocks: the block test is off (PHYGAS_SCAN_BLOCKS)");
     CK(cudaSetDevice(ctx->device));
     RET(tracks_slot(ctx, ctx->cur, tmax_myr, ctx->st, false));
-    RET(ensure(ctx, ctx->total, 64));
+    RET(ensure(ctx, ctx->total, sizeof(unsigned long long) * pgx::kCheckBlockCounts));
     const pgx::ScreenTables T = tables(ctx, ctx->trk[ctx->cur]);
     MRET(pgx::mixed_check_blocks(ctx->st, T, chi2_max, P<unsigned long long>(ctx->total), ctx->mixed.err));
-    unsigned long long h[4];
+    unsigned long long h[pgx::kCheckBlockCounts];
     CK(cudaMemcpyAsync(h, ctx->total.p, sizeof h, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
-    for (int i = 0; i < 4; i++) counts[i] = (long)h[i];
+    for (int i = 0; i < pgx::kCheckBlockCounts; i++) counts[i] = (long)h[i];
     return 0;
 }
 

@@ -149,7 +149,10 @@ PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float lmt, 
 // adjugate's rounding at M(k) (tr M(k) <= tr N, lambda_min M(k) >= lam_lo_t + lam_lo_c), is >= cut, every point of
 // the block has v >= cut: none can be a kept pair's minimum or bring the pair under the cut.
 constexpr int kBlk = 8;                       // points per block
-constexpr float kBlkTau = 2.0f;               // Myr: the largest |tau| in a block's tube (4 steps of 0.5 Myr)
+#ifndef PGX_BLK_TAU
+#define PGX_BLK_TAU 2.0f                      // (a host test of the bound may build it with another value)
+#endif
+constexpr float kBlkTau = PGX_BLK_TAU;        // Myr: the largest |tau| in a block's tube (4 steps of 0.5 Myr)
 
 PGX_HD bool block_skip32(const float4 (&bt)[4], const float4 (&bc)[4], const float (&mref)[3], float cut) {
     const float N0 = bt[2].x + bc[2].x, N1 = bt[2].y + bc[2].y, N2 = bt[2].z + bc[2].z;

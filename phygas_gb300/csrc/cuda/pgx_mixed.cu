@@ -800,7 +800,9 @@ __device__ __forceinline__ bool point_cand32(const ScreenTables &T, int s, int c
     const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
     const float lmt = T.lm_t[(size_t)k * NT + s], lmc = __ldg(T.lm_c + (size_t)k * NC + c);
     Bound b;
-    return !point_skip32(St, Sc, lmt, lmc, m0, m1, cut) &&
+    // a point whose FP64 value is surely above the pair's min ub (strictly) is not its minimum: no candidate
+    const float thr = fminf(cut, fmaxf(um * (1.f + 1e-6f), 1e-30f));
+    return !point_skip32(St, Sc, lmt, lmc, m0, m1, thr) &&
            point_bound32(St, Sc, lmt, lmc, m0, m1, more, cut, b) && b.lb < cut && b.lb <= um;
 }
 
@@ -1360,6 +1362,11 @@ int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *
 // Self-check of the block test on a staged chunk: every (pair, testable block) gets block_skip32 as the filter runs
 // it, and every point of a block it settles gets the FP64 path's point chi2 (pgx_screen_math.cuh): a point under the
 // cut there is a violation.  cnt: blocks tested, blocks settled, points of settled blocks, violations.
+// The block test against the FP64 path, per (pair, block): counts of blocks tested and settled, the points of the
+// settled blocks and those under the cut (violations, 0 when the bound holds); the blocks whose points are all at or
+// above the cut (what an exact block test would settle) and the blocks of pairs with a point under the cut; and over
+// the points of the blocks the test leaves, those the point test settles, those at or above the cut (what an exact
+// point test would settle), and the point test's violations.
 __global__ void k_mx_check_blocks(ScreenTables T, double cut, unsigned long long *__restrict__ cnt) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t NT = T.nt, NC = T.nc;
@@ -1367,8 +1374,10 @@ __global__ void k_mx_check_blocks(ScreenTables T, double cut, unsigned long long
     const int s = (int)(p % NT), c = (int)(p / NT);
     const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
     const int nbt = n > kBlk / 2 ? (n - kBlk / 2 - 1) / kBlk + 1 : 0;
-    unsigned long long tested = 0, settled = 0, points = 0, bad = 0;
+    unsigned long long k_[kCheckBlockCounts] = {};
     const double R2 = T.R2[c];
+    bool kept = false;
+    unsigned long long nb_pair = 0;
     for (int b = 0; b < nbt; b++) {
         const int km = b * kBlk + kBlk / 2;
         const float4 *a = T.blk_t + ((size_t)b * NT + s) * 4, *q = T.blk_c + ((size_t)b * NC + c) * 4;
@@ -1377,9 +1386,11 @@ __global__ void k_mx_check_blocks(ScreenTables T, double cut, unsigned long long
         const float4 *tm = T.t32 + ((size_t)km * NT + s) * 3, *cm = T.c32 + ((size_t)km * NC + c) * 3;
         float mref[3];
         sep32(tm[0], tm[1], cm[0], cm[1], mref);
-        tested++;
-        if (!block_skip32(BT, BC, mref, (float)cut)) continue;
-        settled++;
+        k_[0]++;
+        nb_pair++;
+        const bool settled = block_skip32(BT, BC, mref, (float)cut);
+        k_[1] += settled;
+        bool all_above = true;
         for (int k = b * kBlk; k < min(b * kBlk + kBlk, n); k++) {
             const double *tk = T.t64 + (size_t)k * 12 * NT + s, *ck = T.c64 + (size_t)k * 12 * NC + c;
             double M[6], m0[3], m1[3], sv;
@@ -1388,14 +1399,37 @@ __global__ void k_mx_check_blocks(ScreenTables T, double cut, unsigned long long
             const bool more = k + 1 < n;
             for (int i = 0; i < 3; i++) m1[i] = more ? tk[(12 + i) * NT] - ck[(12 + i) * NC] : m0[i];
             const double v = point_chi2_64(M, R2, m0, m1, more, cut, sv);
-            points++;
-            bad += v >= 0 && v < cut;
+            const bool under = v >= 0 && v < cut;
+            all_above &= !under;
+            kept |= under;
+            if (settled) {
+                k_[2]++;
+                k_[3] += under;
+            } else {
+                const float4 *t = T.t32 + ((size_t)k * NT + s) * 3, *cc = T.c32 + ((size_t)k * NC + c) * 3;
+                float mc[3], mn[3];
+                sep32(t[0], t[1], cc[0], cc[1], mc);
+                if (more) {
+                    const float4 *t2 = t + NT * 3, *c2 = cc + NC * 3;
+                    sep32(t2[0], t2[1], c2[0], c2[1], mn);
+                } else {
+                    mn[0] = mc[0]; mn[1] = mc[1]; mn[2] = mc[2];
+                }
+                const float St[6] = {t[1].z, t[1].w, t[2].x, t[2].y, t[2].z, t[2].w};
+                const float Sc[6] = {cc[1].z, cc[1].w, cc[2].x, cc[2].y, cc[2].z, cc[2].w};
+                const bool pskip = point_skip32(St, Sc, T.lm_t[(size_t)k * NT + s], T.lm_c[(size_t)k * NC + c], mc,
+                                                mn, (float)cut);
+                k_[6]++;
+                k_[7] += pskip;
+                k_[8] += !under;
+                k_[9] += pskip && under;
+            }
         }
+        k_[4] += all_above;
     }
-    atomicAdd(cnt, tested);
-    atomicAdd(cnt + 1, settled);
-    atomicAdd(cnt + 2, points);
-    atomicAdd(cnt + 3, bad);
+    if (kept) k_[5] += nb_pair;
+    for (int i = 0; i < kCheckBlockCounts; i++)
+        if (k_[i]) atomicAdd(cnt + i, k_[i]);
 }
 
 int mixed_check_blocks(cudaStream_t st, const ScreenTables &T, double cut, unsigned long long *cnt,
@@ -1404,7 +1438,7 @@ int mixed_check_blocks(cudaStream_t st, const ScreenTables &T, double cut, unsig
         err = "no block tables";
         return PGX_E_ARG;
     }
-    int rc = check(cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), st), err, "memset");
+    int rc = check(cudaMemsetAsync(cnt, 0, kCheckBlockCounts * sizeof(unsigned long long), st), err, "memset");
     if (rc) return rc;
     const size_t pairs = (size_t)T.nt * T.nc;
     k_mx_check_blocks<<<(unsigned)((pairs + 127) / 128), 128, 0, st>>>(T, cut, cnt);

@@ -66,6 +66,8 @@ int mixed_check_draws(cudaStream_t st, int n, const FinishIn *fin, double *ratio
 int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *S, const double *R2, double cut,
                        double *v64, float *lb, float *ub, int *rej, std::string &err);
 // self-check of the filter's block test on the staged chunk's tracks (pgx_check_blocks): cnt[4] on the device
+// counters of pgx_check_blocks
+constexpr int kCheckBlockCounts = 10;
 int mixed_check_blocks(cudaStream_t st, const ScreenTables &T, double cut, unsigned long long *cnt, std::string &err);
 
 }  // namespace pgx

@@ -5,8 +5,10 @@ fast reciprocal and reciprocal square root put at either end of their documented
 a block it settles has, at every point the FP64 path evaluates for it, a chi2 >= the cut.  Random blocks, built to
 the block tables' contract (pgx_mixed.cu k_block_tables): dominating matrices N = S_t + S_c from isotropic to
 needle-thin, lambda lower bounds, velocity and acceleration differences, tube radii; separations scaled so that the
-bound lands near the cut.  Each settled block is probed at tube points chosen against it (the tube's offset along
-the direction that lowers the N^-1 norm most, at the ends and the middle of the block) with matrices M(k) <= N."""
+bound lands near the cut, with the relative motion random or along the separation (the closest approach inside the
+block).  Each settled block is probed at tube points chosen against it -- over the block's whole time range, at the
+closest approach of the tube's linear part, each with the tube's offset along the direction that lowers the N^-1
+norm most -- with matrices M(k) <= N."""
 import os
 import subprocess
 import tempfile
@@ -51,14 +53,20 @@ inline float4 make_float4(float x, float y, float z, float w) { return float4{x,
 """
 
 
-@pytest.fixture(scope="module")
-def harness():
+def _build(tau=None):
     d = tempfile.mkdtemp(prefix="phygas_blk_")
     src, exe = os.path.join(d, "h.cpp"), os.path.join(d, "h")
     with open(src, "w") as f:
         f.write(PRELUDE + HARNESS)
-    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", CUDA_SRC, src, "-o", exe], check=True)
+    defs = [] if tau is None else ["-DPGX_BLK_TAU=%sf" % tau]
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off"] + defs + ["-I", CUDA_SRC, src, "-o", exe],
+                   check=True)
     return exe, d
+
+
+@pytest.fixture(scope="module")
+def harness():
+    return _build()
 
 
 def _spd(rng, n, lo, hi, needle):
@@ -79,7 +87,7 @@ def _unpack6(s):
                      np.stack([s[:, 2], s[:, 4], s[:, 5]], -1)], -2)
 
 
-def _blocks(n, seed):
+def _blocks(n, seed, toward=False):
     rng = np.random.default_rng(seed)
     S_t = _pack6(_spd(rng, n, -8, -1, 0.2)).astype(F)              # the stored (dominating) matrices
     S_c = _pack6(_spd(rng, n, -8, -2, 0.1)).astype(F)
@@ -109,6 +117,15 @@ def _blocks(n, seed):
     reach = (2 * np.sqrt(np.einsum("ni,nij,nj->n", dv, Ninv, dv)) + 2 * np.sqrt(np.einsum("ni,nij,nj->n", da, Ninv, da))
              + (e_t.astype(np.float64) + e_c) / np.sqrt(np.linalg.eigvalsh(N)[:, 0]))
     dist = (np.sqrt(cut) + reach) * rng.uniform(0.98, 1.3, n) / np.sqrt(qd)
+    if toward:
+        # the relative motion along the separation, toward or away, so that the tube's linear part comes closest
+        # inside the block or at an end; the distance puts that approach near the cut
+        speed = rng.uniform(0.2, 1.5, n) * dist / 2.0 * np.where(rng.uniform(size=n) < 0.5, 1.0, -1.0)
+        side = rng.normal(size=(n, 3)) * 0.2 * np.abs(speed)[:, None]
+        v_c = (v_t.astype(np.float64) + d * speed[:, None] + side).astype(F)
+        dv = v_t.astype(np.float64) - v_c
+        dvn = np.sqrt(np.einsum("ni,nij,nj->n", dv, Ninv, dv))
+        dist = dist + 2.0 * dvn * rng.uniform(0.0, 1.0, n) / np.sqrt(qd)
     p_c = p_t - d * dist[:, None]
     hi_t, hi_c = p_t.astype(F), p_c.astype(F)
     lo_t_, lo_c_ = (p_t - hi_t).astype(F), (p_c - hi_c).astype(F)
@@ -133,14 +150,19 @@ def _run(harness, rec, err):
     return np.array([c == "1" for c in out])
 
 
-def _min_chi2(info, idx, rng):
+def _min_chi2(info, idx, rng, lo=-2.0, hi=2.0):
     """The smallest chi2 found in the tube of each block idx, with M(k) <= N: tube points at tau = -2, 0, 2 and the
     block's worst direction (e against N^-1 x, the N^-1-norm's steepest descent), matrices shrunk by random PSD parts
     while keeping lambda_min(M) >= the range's lower bound."""
     N, cut = info["N"][idx], info["cut"][idx]
     out = np.full(len(idx), np.inf)
-    for tau in (-2.0, -1.0, 0.0, 1.0, 2.0):
-        x = info["mref"][idx] + info["dv"][idx] * tau + 0.5 * info["da"][idx] * tau * tau
+    m, dv = info["mref"][idx], info["dv"][idx]
+    Nm, Nv = np.linalg.solve(N, m[..., None])[..., 0], np.linalg.solve(N, dv[..., None])[..., 0]
+    t_star = np.clip(-np.einsum("ni,ni->n", dv, Nm) / np.einsum("ni,ni->n", dv, Nv), lo, hi)
+    taus = [np.full(len(idx), t) for t in np.linspace(lo, hi, 17)] + [t_star]
+    for tau in taus:
+        tau = tau[:, None]
+        x = m + dv * tau + 0.5 * info["da"][idx] * tau * tau
         g = np.linalg.solve(N, x[..., None])[..., 0]
         g /= np.linalg.norm(g, axis=1)[:, None]
         x = x - g * info["eps"][idx, None]
@@ -155,9 +177,10 @@ def _min_chi2(info, idx, rng):
     return out
 
 
+@pytest.mark.parametrize("toward", [False, True])
 @pytest.mark.parametrize("err", [0.0, 4 * 5.96e-8, -4 * 5.96e-8])
-def test_settled_blocks_stay_above_the_cut(harness, err):
-    rec, info = _blocks(200_000, 17)
+def test_settled_blocks_stay_above_the_cut(harness, err, toward):
+    rec, info = _blocks(60_000, 17 + toward, toward)
     settled = _run(harness, rec, err)
     idx = np.flatnonzero(settled)
     assert 0.05 * len(rec) < len(idx) < 0.95 * len(rec), len(idx)          # near the boundary, both outcomes
@@ -168,11 +191,21 @@ def test_settled_blocks_stay_above_the_cut(harness, err):
 def test_the_test_is_not_vacuous(harness):
     """With a tube radius far below what the block has (the bound wrong on purpose, on the CPU), the same probes
     find settled blocks under the cut: the probes do reach the bound's weak spots."""
-    rec, info = _blocks(50_000, 23)
+    rec, info = _blocks(30_000, 23)
     rec = rec.copy()
     rec[:, 3] *= F(1e-3)
     rec[:, 19] *= F(1e-3)
     settled = _run(harness, rec, 0.0)
     idx = np.flatnonzero(settled)
     worst = _min_chi2(info, idx, np.random.default_rng(4))
+    assert worst.min() < 1.0
+
+
+def test_the_time_range_matters():
+    """Built for a block of half the time range (|tau| <= 1 Myr, the bound wrong on purpose, on the CPU), the test
+    settles blocks whose tube comes under the cut between 1 and 2 Myr from the middle: the probes reach them."""
+    rec, info = _blocks(30_000, 29, True)
+    settled = _run(_build("1.0"), rec, 0.0)
+    idx = np.flatnonzero(settled)
+    worst = _min_chi2(info, idx, np.random.default_rng(5))
     assert worst.min() < 1.0

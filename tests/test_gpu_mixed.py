@@ -139,8 +139,8 @@ def test_block_test_is_sound(built):
         else:
             os.environ["PHYGAS_SCAN_BLOCKS"] = old
     for cut, r in got.items():
-        assert r["violations"] == 0, (cut, r)
-        assert r["points"] > 0, (cut, r)
+        assert r["violations"] == 0 and r["point_violations"] == 0, (cut, r)
+        assert r["points"] > 0 and r["settled"] <= r["settleable"], (cut, r)
     assert got[25.0]["settled"] > 0.3 * got[25.0]["tested"], got
 
 

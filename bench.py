@@ -382,6 +382,9 @@ def pair_mc_measure(ctx, stars, clusters, cp, rows, want_cpu, fp64_peak):
 # The rate keeps the GPU about 60 % busy with the mixed screen (a pulsar job is ~0.7 s of clone tracing): latency, not
 # a queue that grows without end.
 SERVE_JOBS, SERVE_JOBS_FP64, SERVE_RATE_HZ, SERVE_SLOTS, SERVE_SEED = 200, 40, 2.0, 3, 1004
+# the request loop's clone throughput under a backlog: SERVE_BACKLOG single-pulsar jobs submitted at once (the
+# stream's rate limits the clone-steps/s of the mixed stream above, not the GPU)
+SERVE_BACKLOG = 12
 # chunks of the benchmark's stars per end-to-end run (the pipeline's fill is spread over them)
 E2E_CHUNKS = 8
 
@@ -454,6 +457,15 @@ def serving_measure(cp, tp):
                                       for k in ("screen", "control", "pulsar")}
         s["jobs_by_kind"] = {k: sum(1 for x in jobs if x["kind"] == k) for k in ("screen", "control", "pulsar")}
         out[prec] = s
+    env = dict(os.environ, PHYGAS_SERVE_MIX="pairs")
+    r = subprocess.run([pg.SERVE_CLI, cp, tp, pp, str(SERVE_BACKLOG), "1000", str(SERVE_SLOTS), "mixed",
+                        str(SERVE_SEED + 1)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env)
+    summ = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{") and '"summary"' in x]
+    if r.returncode or not summ:
+        raise RuntimeError("phygas_serve backlog failed: %s" % r.stderr[-400:])
+    out["pair_backlog"] = {"jobs": SERVE_BACKLOG, "how": "single-pulsar jobs submitted at once, %d slots" % SERVE_SLOTS,
+                           "wall_s": summ[0]["wall_s"], "clone_steps_per_s": summ[0]["clone_steps_per_s"],
+                           "latency_p50_s": summ[0]["latency_p50_s"]}
     return out
 
 

@@ -205,6 +205,10 @@ int pgx_pair_targets(PgxContext *ctx, int n_pairs, const PhTarget *t, const int 
 /* The persistent clone kernels of this context on at most blocks_per_sm blocks per SM (0 = as many as fit, the
  * default): leaves registers for other contexts' kernels to run beside them -- the request loop's slots. */
 int pgx_pair_blocks(PgxContext *ctx, int blocks_per_sm);
+/* The same cap, applied only to the launches made while *busy is nonzero (read atomically at each launch of a batch;
+ * busy NULL: always, as pgx_pair_blocks): a caller that runs other work beside the clone kernels sets the flag
+ * while that work runs, and the clone kernels take the whole GPU the rest of the time. */
+int pgx_pair_blocks_while(PgxContext *ctx, int blocks_per_sm, const int *busy);
 
 /* pgx_pair for callers that cannot allocate GPU memory (no counterpart in the reference): code running inside
  * another framework's device memory pool, loops that must not stall on the allocator, hosts that can only hand

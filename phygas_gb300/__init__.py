@@ -110,6 +110,7 @@ SIGNATURES = [
     ("pgx_screen_split", C.c_int, [C.c_void_p, C.c_int]),
     ("pgx_screen_parts", C.c_int, [C.c_void_p, C.c_int]),
     ("pgx_pair_blocks", C.c_int, [C.c_void_p, C.c_int]),
+    ("pgx_pair_blocks_while", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     ("pgx_pair_targets", C.c_int, [C.c_void_p, C.c_int, _P(PhTarget), _P(C.c_int), _P(PhCluster), _P(C.c_int),
                                    _P(C.c_int), C.c_double, C.c_int, C.c_int, C.c_void_p]),
     ("pgx_screen_chunks", C.c_int, [C.c_void_p, _P(PhTarget), C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
@@ -479,6 +480,13 @@ class Context:
     def pair_blocks(self, blocks_per_sm):
         """pgx_pair_blocks: the persistent clone kernels on at most blocks_per_sm blocks per SM (0 = all that fit)."""
         self._check(lib().pgx_pair_blocks(self.h, int(blocks_per_sm)), "pgx_pair_blocks")
+
+    def pair_blocks_while(self, blocks_per_sm, busy):
+        """pgx_pair_blocks_while: the cap only for launches made while the ctypes c_int `busy` is nonzero (the
+        caller keeps `busy` alive while the context uses it; None clears it)."""
+        self._busy = busy
+        ptr = C.cast(C.byref(busy), C.c_void_p) if busy is not None else None
+        self._check(lib().pgx_pair_blocks_while(self.h, int(blocks_per_sm), ptr), "pgx_pair_blocks_while")
 
     def set_split(self, min_stars, parts=None):
         """pgx_screen_split / pgx_screen_parts: stage chunks of at least min_stars stars (0 = never) in `parts`

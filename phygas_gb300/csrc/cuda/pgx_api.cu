@@ -114,9 +114,11 @@ struct PgxContext {
     Buf p_off, p_ps, p_steps, p_dt, p_r50, p_rt, p_items, p_q, p_done, p_cres, p_res, p_params;
     int mc_variant = 0;                        // launch shape of the clone kernel (pgx_tune_pair picks it)
     int mc_blocks_per_sm = 0;                  // > 0: the persistent clone kernels on at most this many blocks per SM
+    const int *mc_busy = nullptr;              // set: the cap applies only while *mc_busy is nonzero at a launch
     double *h_clones[2] = {};                  // pgx_pair_targets: two batches of clones, page-locked, reused
     size_t h_clones_cap[2] = {};
     cudaGraphExec_t mc_exec[16] = {};          // prep + trace + reduce, captured once per shape, replayed
+    cudaGraphExec_t mc_exec_capped[16] = {};   // the same with the grid capped (pgx_pair_blocks_while)
     // one-object helpers of the drop-in API
     Buf x_ps0, x_sig21, x_npts, x_opos, x_ovel, x_t64, x_t32, x_lm;
     PgxStats stats = {};
@@ -491,6 +493,8 @@ void pgx_close(PgxContext *ctx) {
     pgx::prefilter_free(ctx->pre);
     pgx::mixed_free(ctx->mixed);
     for (auto &g : ctx->mc_exec)
+        if (g) cudaGraphExecDestroy(g);
+    for (auto &g : ctx->mc_exec_capped)
         if (g) cudaGraphExecDestroy(g);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -1375,16 +1379,25 @@ void pgx_host_free(void *p) {
 }
 
 namespace {
-// the captured prep + trace + reduce sequence of clone-kernel variant v (parameters read from ctx->p_params)
-int mc_graph(PgxContext *ctx, int v, cudaGraphExec_t &exec) {
-    if (ctx->mc_exec[v]) {
-        exec = ctx->mc_exec[v];
+// the clone kernels' cap on blocks per SM for a launch now (0: none): the static one, or, with a busy flag, the cap
+// while the flag is set
+int mc_cap_now(const PgxContext *ctx) {
+    if (!ctx->mc_busy) return ctx->mc_blocks_per_sm;
+    return __atomic_load_n(ctx->mc_busy, __ATOMIC_ACQUIRE) != 0 ? ctx->mc_blocks_per_sm : 0;
+}
+
+// the captured prep + trace + reduce sequence of clone-kernel variant v (parameters read from ctx->p_params), with the
+// grid capped when `capped` (a live cap keeps one graph of each kind)
+int mc_graph(PgxContext *ctx, int v, bool capped, cudaGraphExec_t &exec) {
+    cudaGraphExec_t &slot = capped ? ctx->mc_exec_capped[v] : ctx->mc_exec[v];
+    if (slot) {
+        exec = slot;
         return 0;
     }
     RET(ensure(ctx, ctx->p_params, sizeof(pgx::McPairs)));
     int grid = 0;
     CK(pgx::mc_variant_grid(v, ctx->sms, grid));
-    if (ctx->mc_blocks_per_sm > 0) grid = std::min(grid, ctx->mc_blocks_per_sm * ctx->sms);
+    if (capped) grid = std::min(grid, ctx->mc_blocks_per_sm * ctx->sms);
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
     const cudaError_t le = pgx::launch_mc(v, grid, ctx->sms * 4, ctx->sms * 8, ctx->st,
@@ -1394,10 +1407,10 @@ int mc_graph(PgxContext *ctx, int v, cudaGraphExec_t &exec) {
         if (g) cudaGraphDestroy(g);
         return fail(ctx, PGX_E_CUDA, "clone graph capture: %s", cudaGetErrorString(le != cudaSuccess ? le : ce));
     }
-    const cudaError_t ie = cudaGraphInstantiate(&ctx->mc_exec[v], g, 0);
+    const cudaError_t ie = cudaGraphInstantiate(&slot, g, 0);
     cudaGraphDestroy(g);
     if (ie != cudaSuccess) return fail(ctx, PGX_E_CUDA, "clone graph instantiate: %s", cudaGetErrorString(ie));
-    exec = ctx->mc_exec[v];
+    exec = slot;
     return 0;
 }
 
@@ -1468,7 +1481,7 @@ int pair_run(PgxContext *ctx, int variant, int n_pairs, const int *clone_off, co
     ctx->stats = PgxStats();
     if (graph) {
         cudaGraphExec_t exec;
-        RET(mc_graph(ctx, variant, exec));
+        RET(mc_graph(ctx, variant, mc_cap_now(ctx) > 0, exec));
         // the parameters travel by copy: the graph's kernels read them from p_params
         CK(cudaMemcpyAsync(ctx->p_params.p, &Pp, sizeof Pp, cudaMemcpyHostToDevice, ctx->st));
         CK(cudaEventRecord(ctx->ev[EV_PAIR0], ctx->st));
@@ -1483,7 +1496,8 @@ int pair_run(PgxContext *ctx, int variant, int n_pairs, const int *clone_off, co
             CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pgx::k_pair_mc, pgx::kMcThreads, 0));
             const int warps_needed = (int)items.size();
             int grid = std::max(1, ctx->sms * std::max(1, per_sm));
-            if (ctx->mc_blocks_per_sm > 0) grid = std::min(grid, ctx->mc_blocks_per_sm * ctx->sms);
+            const int cap = mc_cap_now(ctx);
+            if (cap > 0) grid = std::min(grid, cap * ctx->sms);
             grid = std::min(grid, (warps_needed + pgx::kMcThreads / 32 - 1) / (pgx::kMcThreads / 32));
             pgx::k_pair_mc<<<grid, pgx::kMcThreads, 0, ctx->st>>>(Pp);
             CKL();
@@ -1640,18 +1654,22 @@ int pgx_tune_pair(PgxContext *ctx, int n_pairs, const int *clone_off, const doub
     return 0;
 }
 
-int pgx_pair_blocks(PgxContext *ctx, int blocks_per_sm) {
+int pgx_pair_blocks_while(PgxContext *ctx, int blocks_per_sm, const int *busy) {
     if (!ctx) return PGX_E_ARG;
     if (blocks_per_sm < 0) return fail(ctx, PGX_E_ARG, "pgx_pair_blocks: %d", blocks_per_sm);
     CK(cudaSetDevice(ctx->device));
     ctx->mc_blocks_per_sm = blocks_per_sm;
-    for (auto &g : ctx->mc_exec)                  // captured with the old grid
-        if (g) {
-            cudaGraphExecDestroy(g);
-            g = nullptr;
-        }
+    ctx->mc_busy = busy;
+    for (auto *set : {ctx->mc_exec, ctx->mc_exec_capped})   // captured with the old grid
+        for (int v = 0; v < 16; v++)
+            if (set[v]) {
+                cudaGraphExecDestroy(set[v]);
+                set[v] = nullptr;
+            }
     return 0;
 }
+
+int pgx_pair_blocks(PgxContext *ctx, int blocks_per_sm) { return pgx_pair_blocks_while(ctx, blocks_per_sm, nullptr); }
 
 int pgx_pair_shapes(int n, int *warps, int *clones_per_lane, int *min_blocks) {
     const int nv = pgx::mc_variants();

@@ -67,6 +67,8 @@ struct PgxServer {
     std::map<long, std::unique_ptr<Job>> jobs;
     long next_id = 1, submitted = 0, finished = 0;
     int running = 0, max_running = 0;
+    int screens_running = 0;                   // screen and control jobs on the GPU (atomic access): while any runs,
+                                               // the slots' clone kernels keep to kServeMcBlocksPerSm blocks per SM
     bool stop = false;
     std::vector<std::thread> workers;
     std::chrono::steady_clock::time_point t0;
@@ -170,8 +172,10 @@ void worker(PgxServer *s, int slot) {
             job->out.t_start = s->now();
             job->out.slot = slot;
         }
-        const int rc = job->spec.kind == PGX_JOB_PAIRS ? run_pairs(*s, s->ctx[slot], *job)
-                                                       : run_screen(*s, slot, s->ctx[slot], *job);
+        const bool screen = job->spec.kind != PGX_JOB_PAIRS;
+        if (screen) __atomic_add_fetch(&s->screens_running, 1, __ATOMIC_ACQ_REL);
+        const int rc = screen ? run_screen(*s, slot, s->ctx[slot], *job) : run_pairs(*s, s->ctx[slot], *job);
+        if (screen) __atomic_sub_fetch(&s->screens_running, 1, __ATOMIC_ACQ_REL);
         {
             std::lock_guard<std::mutex> lk(s->mu);
             job->out.status = rc;
@@ -221,9 +225,11 @@ int pgx_server_open(int device, int slots, double hbm_budget_gb, const PhCluster
         s->ctx.push_back(ctx);
         rc = pgx_screen_clusters(ctx, nc, ps0.data(), sig.data(), tm.data(), r50.data(), rt.data(), names.data(),
                                  r_kernel);
-        // a pair job's persistent clone kernel would hold nearly every register of the GPU until it ends, and the
-        // other slots' screens would wait for it: with more than one slot it keeps to kServeMcBlocksPerSm blocks
-        if (rc == 0 && slots > 1) rc = pgx_pair_blocks(ctx, kServeMcBlocksPerSm);
+        // a pair job's persistent clone kernel would hold nearly every register of the GPU until its batch ends,
+        // and the other slots' screens would wait for it: with more than one slot, a batch launched while a screen
+        // or control job runs keeps to kServeMcBlocksPerSm blocks per SM, and one launched while none does takes the
+        // whole GPU (pair jobs beside each other share it as concurrent kernels)
+        if (rc == 0 && slots > 1) rc = pgx_pair_blocks_while(ctx, kServeMcBlocksPerSm, &s->screens_running);
         if (rc) {
             for (PgxContext *x : s->ctx) pgx_close(x);
             return rc;

@@ -9,7 +9,8 @@
  * single-pulsar jobs, a line of pulsars.txt against every cluster that passes the prefilter, 1000 clones at dt
  * 0.05 Myr.  Screen chunks keep the rows with p_r50 >= 0.001, chi2_max 25.  Each job is submitted at its arrival
  * time; its latency is its end minus its arrival.  `plan` prints the stream and exits without touching a GPU.
- * PHYGAS_SERVE_HBM_GB sets the device-memory budget of the running jobs (default 80).
+ * PHYGAS_SERVE_HBM_GB sets the device-memory budget of the running jobs (default 80); PHYGAS_SERVE_MIX=pairs makes
+ * every job a single-pulsar job (for the request loop's clone throughput under a backlog).
  */
 #define _POSIX_C_SOURCE 199309L
 #include <math.h>
@@ -78,13 +79,17 @@ int main(int argc, char **argv) {
     const int nc = ph_read_clusters(argv[1], &cl), ns = ph_read_targets(argv[2], &st), np = ph_read_targets(argv[3], &pu);
     if (nc <= 0 || ns <= 0 || np <= 0) { fprintf(stderr, "phygas_serve: can't read inputs\n"); return 1; }
     Planned *plan = malloc(sizeof(Planned) * jobs);
+    const char *mix = getenv("PHYGAS_SERVE_MIX");
+    const int pairs_only = mix && !strcmp(mix, "pairs");
     double t = 0;
     for (int i = 0; i < jobs; i++) {
         t += -log(1.0 - uni()) / rate;
         const double u = uni();
         Planned *p = &plan[i];
         p->arrive = t;
-        if (u < 0.4 || u >= 0.6) {
+        if (pairs_only) {
+            p->kind = PGX_JOB_PAIRS;
+        } else if (u < 0.4 || u >= 0.6) {
             p->kind = u < 0.4 ? PGX_JOB_SCREEN : PGX_JOB_PAIRS;
         } else {
             p->kind = PGX_JOB_CONTROL;

@@ -188,3 +188,28 @@ def test_pipelined_pair_targets_and_capped_grid_give_the_same_bits(ctx):
         assert ctx.pair_targets(targets, ti, clusters, ci, ncl, 0.05).tobytes() == want.tobytes()
     finally:
         ctx.pair_blocks(0)
+
+
+def test_live_cap_gives_the_same_bits(ctx):
+    """pgx_pair_blocks_while (the request loop's setting): batches launched while the flag is set keep to one block per
+    SM, the others take the whole GPU; the results are the same bits either way, and after the flag changes between
+    calls (both captured graphs in use)."""
+    import ctypes
+    rng = np.random.default_rng(6)
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "pair64", 3, 1001)
+        targets, clusters = pg.read_targets(tp), pg.read_clusters(cp)
+    ti = rng.integers(0, 3, 30).astype(np.int32)
+    ci = rng.integers(0, len(clusters), 30).astype(np.int32)
+    ncl = rng.choice([0, 1, 64, 500, 1024], 30).astype(np.int32)
+    batch = pg.draw_pair_batch(targets, ti, clusters, ci, ncl, 0.05)
+    want = ctx.pair(*batch)
+    busy = ctypes.c_int(1)
+    ctx.pair_blocks_while(1, busy)
+    try:
+        for flag in (1, 0, 1, 0):
+            busy.value = flag
+            assert ctx.pair(*batch).tobytes() == want.tobytes(), flag
+            assert ctx.pair_targets(targets, ti, clusters, ci, ncl, 0.05, batch_pairs=11).tobytes() == want.tobytes()
+    finally:
+        ctx.pair_blocks_while(0, None)

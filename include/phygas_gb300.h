@@ -258,10 +258,11 @@ int pgx_check_bounds(PgxContext *ctx, int n, const double *pos, const double *S,
 /* Self-check of the mixed-precision filter's block test (no counterpart in the reference): on the chunk staged by
  * pgx_screen_stage (unsplit: pgx_screen_split(ctx, 0), or fewer stars than the split threshold), traces its tracks
  * (tmax_myr), runs the block test on every (pair, block of 8 points) as the filter does, and evaluates the FP64 point
- * chi2 of every point: counts[10] = blocks tested, blocks settled, points of settled blocks, violations (points of
+ * chi2 of every point: counts[12] = blocks tested, blocks settled, points of settled blocks, violations (points of
  * settled blocks under chi2_max; 0 when the test's bounds hold), blocks whose points are all at or above chi2_max,
  * blocks of pairs with a point under it, points of the blocks not settled, of those the ones the filter's point test
- * settles, the ones at or above chi2_max, and the point test's violations (0 when its bounds hold). */
+ * settles, the ones at or above chi2_max, and the point tests' violations (0 when their bounds hold); then the ones
+ * the point test against the block's dominating matrix settles, and of those the ones the point test leaves. */
 int pgx_check_blocks(PgxContext *ctx, double tmax_myr, double chi2_max, long *counts);
 
 /* Self-check of the mixed-precision finish's FP32 draws (no counterpart in the reference): for n pairs given by

@@ -321,10 +321,11 @@ class Context:
         """The filter's block test on the staged (unsplit) chunk, every point checked in FP64 (pgx_check_blocks):
         {tested, settled, points, violations, settleable, kept_pair_blocks, walked_points, point_settled,
         point_settleable, point_violations}."""
-        c = (C.c_long * 10)()
+        c = (C.c_long * 12)()
         self._check(lib().pgx_check_blocks(self.h, tmax, chi2_max, c), "pgx_check_blocks")
         return dict(zip(("tested", "settled", "points", "violations", "settleable", "kept_pair_blocks",
-                         "walked_points", "point_settled", "point_settleable", "point_violations"), list(c)))
+                         "walked_points", "point_settled", "point_settleable", "point_violations",
+                         "block_point_settled", "block_point_only"), list(c)))
 
     def check_draws(self, fin11, seeds):
         """Per pair, the FP32 draws' largest error relative to their own bound (see pgx_check_draws)."""

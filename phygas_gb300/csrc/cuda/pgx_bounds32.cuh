@@ -137,8 +137,9 @@ PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float lmt, 
 //            points, so every point the FP64 path evaluates for the block -- m0 at a track point, or its nearest
 //            point on a chord -- lies in the tube p(km) + v tau + a tau^2 / 2 + e, |e| <= eps, |tau| <= 4 h;
 //   S        an FP32 matrix that dominates S(k) (+ R^2 I for a cluster) at every point of the range: S(ke) + delta I,
-//            delta >= the largest eigenvalue of S(k) - S(ke) over the range (0 when the covariance only grows, as it
-//            mostly does going back in time), the FP32 rounding absorbed into delta;
+//            delta >= the largest eigenvalue of S(k) - S(ke) over the range, the FP32 rounding absorbed into delta
+//            (the covariances are needle-thin and turn along the track, so delta is often many times the thin axis:
+//            this domination, not the tube, is what leaves blocks unsettled);
 //   lam      <= lambda_min(S) (the point's FP64 lower bound at ke + delta, rounded down);
 //   lam_lo   <= lambda_min(S(k)) at every point of the range (the point bounds' minimum), for the adjugate's error.
 // For a pair, M(k) = S_t(k) + S_c(k) + R^2 I <= N = S_t + S_c (Loewner order), so x^T M(k)^-1 x >= x^T N^-1 x, and
@@ -153,6 +154,48 @@ constexpr int kBlk = 8;                       // points per block
 #define PGX_BLK_TAU 2.0f                      // (a host test of the bound may build it with another value)
 #endif
 constexpr float kBlkTau = PGX_BLK_TAU;        // Myr: the largest |tau| in a block's tube (4 steps of 0.5 Myr)
+
+// The point test against a block's dominating matrix N = S_t + S_c (the block tables of the point's block) in place of
+// the point's own M(k): M(k) <= N, so every form in M(k)^-1 is at least the form in N^-1; lam <= lambda_min(N), and
+// the FP64 adjugate's rounding at M(k) from tr(N) / lam_lo as in the block test.  Otherwise point_skip32's triangle
+// test on the step's segment.
+PGX_HD bool point_skip32_blk(const float4 (&bt)[4], const float4 (&bc)[4], const float (&m0)[3], const float (&m1)[3],
+                             float cut) {
+    const float N0 = bt[2].x + bc[2].x, N1 = bt[2].y + bc[2].y, N2 = bt[2].z + bc[2].z;
+    const float N3 = bt[2].w + bc[2].w, N4 = bt[3].x + bc[3].x, N5 = bt[3].y + bc[3].y;
+    const float tr = N0 + N3 + N5;
+    const float lam = (bt[1].w + bc[1].w) * (1.f - 16.f * kEps32);
+    const float lam_lo = (bt[3].z + bc[3].z) * (1.f - 16.f * kEps32);
+    if (!(lam > 1e-30f && lam_lo > 1e-30f && N0 > 1e-30f && tr < 1e30f)) return false;
+    const float i1 = fast_rcp(N0);
+    const float l10 = N1 * i1, l20 = N2 * i1;
+    const float D2 = fmaf(-l10, N1, N3);
+    if (!(D2 > 1e-30f)) return false;
+    const float i2 = fast_rcp(D2);
+    const float uu = fmaf(-l20, N1, N4);
+    const float l21 = uu * i2;
+    const float D3 = fmaf(-l21, uu, fmaf(-l20, N2, N5));
+    if (!(D3 > 1e-30f)) return false;
+    const float i3 = fast_rcp(D3);
+    const float tl = tr * fast_rcp(lam) * (1.f + 8.f * kEps32);
+    const float rho = kSkipC1 * kEps32 * tl;
+    if (!(rho <= 0.25f)) return false;
+    const float dx = m1[0] - m0[0], dy = m1[1] - m0[1], dz = m1[2] - m0[2];
+    const float m00 = fmaf(m0[0], m0[0], fmaf(m0[1], m0[1], m0[2] * m0[2]));
+    const float m11 = fmaf(m1[0], m1[0], fmaf(m1[1], m1[1], m1[2] * m1[2]));
+    const float q0 = ldl_form(l10, l20, l21, i1, i2, i3, m0[0], m0[1], m0[2]);
+    const float c = ldl_form(l10, l20, l21, i1, i2, i3, dx, dy, dz);
+    const float r = rho + 12.f * kEps32;
+    const float big2 = fmaxf(fmaxf(m00, m11), 1e-30f);
+    const float big = big2 * fast_rsqrt(big2) * (1.f + 8.f * kEps32);
+    const float qa = fmaxf(q0 * (1.f - r), 1e-30f), ca = fmaxf(c * (1.f + r), 1e-30f);
+    const float d = qa * fast_rsqrt(qa) * (1.f - 8.f * kEps32) - ca * fast_rsqrt(ca) * (1.f + 8.f * kEps32) -
+                    (3.f * kEps32 * big + 1e-12f) * fast_rsqrt(lam) * (1.f + 8.f * kEps32);
+    if (!(d > 0.f)) return false;
+    const float tlo = tr * fast_rcp(lam_lo) * (1.f + 8.f * kEps32);
+    const float r64 = kAdj64 * 3.f * (1.f + 16.f * kEps32) * tlo * tlo;
+    return d * d * (1.f - r64) * (1.f - 8.f * kEps32) >= cut;
+}
 
 PGX_HD bool block_skip32(const float4 (&bt)[4], const float4 (&bc)[4], const float (&mref)[3], float cut) {
     const float N0 = bt[2].x + bc[2].x, N1 = bt[2].y + bc[2].y, N2 = bt[2].z + bc[2].z;

@@ -448,6 +448,8 @@ __device__ __noinline__ bool point_at32_ol(const ScreenTables *T, int s, int c, 
 // last testable block (fewer than five left) are walked by every lane in step, as are all points when the tables
 // have no block data.  A settled block's points all have chi2 >= cut in the FP64 path: they can neither be a kept
 // pair's minimum nor bring a pair under the cut, and they are left out of min ub, which only admits more candidates.
+// Once a pair's min ub is below the cut, blocks and points are settled against it instead (strictly above another
+// point's FP64 value: not the minimum), so a kept pair's points after its minimum mostly need no full bounds.
 // six resident blocks per SM asked of the compiler: 24 warps to issue from; the kernel is issue-bound
 template <int MINB, bool STAGE>
 __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __grid_constant__ ScreenTables T,
@@ -530,15 +532,21 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
             qn = rest;
         }
     };
-    const size_t NT = T.nt, NC = T.nc;
+    // A point or block whose lower bound is >= thr needs nothing more: thr = cut (it can be neither under the cut nor
+    // the minimum of a kept pair), or just above the pair's min ub so far (its FP64 value is then strictly above
+    // another point's: not the minimum, ties included).  Either way it is left out of min ub, which only admits more
+    // candidates.  The pair's min ub falls as its points' full bounds are folded in, so blocks and points walked
+    // after its minimum are mostly settled against it.
+    auto pair_thr = [&]() { return fminf(cut, fmaxf(um * (1.f + 1e-6f), 1e-30f)); };
+    const size_t NT = T.nt;
     const int n = T.ns < T.cn[c] ? T.ns : T.cn[c];
     // the point test of point k of star st's pair (its separations at k and k + 1 in mc / mn), as every walk runs it
     auto point_needs = [&](int st, int k, const float4 &t1, const float4 &t2, const float4 &c1, const float4 &c2,
-                           const float (&mc)[3], const float (&mn)[3]) {
+                           const float (&mc)[3], const float (&mn)[3], float thr) {
         const float St[6] = {t1.z, t1.w, t2.x, t2.y, t2.z, t2.w};
         const float Sc[6] = {c1.z, c1.w, c2.x, c2.y, c2.z, c2.w};
         const float lmt = T.lm_t[(size_t)k * NT + st], lmc = ldc<STAGE>(clm + (size_t)k * cls);
-        return !point_skip32(St, Sc, lmt, lmc, mc, mn, cut);
+        return !point_skip32(St, Sc, lmt, lmc, mc, mn, thr);
     };
     // ---- level 1: blocks of kBlk points whose position reference km = kBlk b + kBlk/2 lies on the pair's track
     const int nbt = n > kBlk / 2 ? (n - kBlk / 2 - 1) / kBlk + 1 : 0;
@@ -548,6 +556,7 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
             __syncwarp();
             const int e = lane < cnt ? s_bq[w][lane] : 0;
             const int o = e & 31, b = e >> 5, st = s0 + o;
+            const float thr = __shfl_sync(0xffffffffu, pair_thr(), o);    // the owner's threshold at this walk
             const int k0 = b * kBlk, k1 = min(k0 + kBlk, n);
             const float4 *tp = T.t32 + (size_t)st * 3;
             float4 t0, t1, t2, c0, c1, c2;
@@ -571,7 +580,7 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
                         c0 = ldc<STAGE>(q); c1 = ldc<STAGE>(q + 1); c2 = ldc<STAGE>(q + 2);
                         sep32(t0, t1, c0, c1, mn);
                     }
-                    need = point_needs(st, k, T1, T2, C1, C2, mc, mn);
+                    need = point_needs(st, k, T1, T2, C1, C2, mc, mn, thr);
                     mc[0] = mn[0]; mc[1] = mn[1]; mc[2] = mn[2];
                 }
                 push_point(need, o | (k << 5));
@@ -592,7 +601,7 @@ __global__ void __launch_bounds__(kScanStars, MINB) k_mx_scan32_blocks(const __g
                 const float4 *tm = T.t32 + ((size_t)km * NT + s) * 3, *cm = cc32 + (size_t)km * ccs;
                 float mref[3];
                 sep32(tm[0], tm[1], ldc<STAGE>(cm), ldc<STAGE>(cm + 1), mref);
-                need = !block_skip32(BT, BC, mref, cut);
+                need = !block_skip32(BT, BC, mref, pair_thr());
             } else if (b < nball) {
                 need = active;
             }
@@ -1366,7 +1375,8 @@ int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *
 // settled blocks and those under the cut (violations, 0 when the bound holds); the blocks whose points are all at or
 // above the cut (what an exact block test would settle) and the blocks of pairs with a point under the cut; and over
 // the points of the blocks the test leaves, those the point test settles, those at or above the cut (what an exact
-// point test would settle), and the point test's violations.
+// point test would settle), and the point test's violations (also of the point test against the block's dominating
+// matrix, whose settled points and those the point test leaves follow).
 __global__ void k_mx_check_blocks(ScreenTables T, double cut, unsigned long long *__restrict__ cnt) {
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t NT = T.nt, NC = T.nc;
@@ -1419,10 +1429,13 @@ __global__ void k_mx_check_blocks(ScreenTables T, double cut, unsigned long long
                 const float Sc[6] = {cc[1].z, cc[1].w, cc[2].x, cc[2].y, cc[2].z, cc[2].w};
                 const bool pskip = point_skip32(St, Sc, T.lm_t[(size_t)k * NT + s], T.lm_c[(size_t)k * NC + c], mc,
                                                 mn, (float)cut);
+                const bool nskip = point_skip32_blk(BT, BC, mc, mn, (float)cut);
                 k_[6]++;
                 k_[7] += pskip;
                 k_[8] += !under;
-                k_[9] += pskip && under;
+                k_[9] += (pskip || nskip) && under;
+                k_[10] += nskip;
+                k_[11] += nskip && !pskip;
             }
         }
         k_[4] += all_above;

@@ -67,7 +67,7 @@ int mixed_check_bounds(cudaStream_t st, int n, const double *pos, const double *
                        double *v64, float *lb, float *ub, int *rej, std::string &err);
 // self-check of the filter's block test on the staged chunk's tracks (pgx_check_blocks): cnt[4] on the device
 // counters of pgx_check_blocks
-constexpr int kCheckBlockCounts = 10;
+constexpr int kCheckBlockCounts = 12;
 int mixed_check_blocks(cudaStream_t st, const ScreenTables &T, double cut, unsigned long long *cnt, std::string &err);
 
 }  // namespace pgx

@@ -12,15 +12,24 @@ namespace pgx {
 constexpr double kInf = __builtin_huge_val();
 
 // m^T M^-1 m for symmetric M = (xx xy xz yy yz zz) by the adjugate; -1 when det <= 0 (reference quad_inv,
-// src/phygas.c:348-356)
+// src/phygas.c:348-356).  The cofactors and the determinant are computed once per matrix and shared by the forms of
+// a point (the same operations on the same operands as evaluating quad_inv for each, so the same bits).
+struct Adj64 {
+    double i00, i01, i02, i11, i12, i22, det;
+    __device__ __forceinline__ explicit Adj64(const double (&M)[6]) {
+        const double a = M[0], b = M[1], c = M[2], d = M[3], e = M[4], f = M[5];
+        i00 = d * f - e * e; i01 = c * e - b * f; i02 = b * e - c * d;
+        det = a * i00 + b * i01 + c * i02;
+        i11 = a * f - c * c; i12 = b * c - a * e; i22 = a * d - b * b;
+    }
+    __device__ __forceinline__ double form(double mx, double my, double mz) const {
+        if (!(det > 0)) return -1.0;
+        return (mx * (i00 * mx + i01 * my + i02 * mz) + my * (i01 * mx + i11 * my + i12 * mz) +
+                mz * (i02 * mx + i12 * my + i22 * mz)) / det;
+    }
+};
 __device__ __forceinline__ double quad_inv64(const double (&M)[6], double mx, double my, double mz) {
-    const double a = M[0], b = M[1], c = M[2], d = M[3], e = M[4], f = M[5];
-    const double i00 = d * f - e * e, i01 = c * e - b * f, i02 = b * e - c * d;
-    const double det = a * i00 + b * i01 + c * i02;
-    if (!(det > 0)) return -1.0;
-    const double i11 = a * f - c * c, i12 = b * c - a * e, i22 = a * d - b * b;
-    return (mx * (i00 * mx + i01 * my + i02 * mz) + my * (i01 * mx + i11 * my + i12 * mz) +
-            mz * (i02 * mx + i12 * my + i22 * mz)) / det;
+    return Adj64(M).form(mx, my, mz);
 }
 
 // chi2 at one track point k of a pair: the form at the point's separation m0 and at the closest point of the step's
@@ -41,7 +50,8 @@ __device__ __forceinline__ double point_chi2_64(double (&M)[6], double R2, const
         else far = (m0[0] * m0[0] + m0[1] * m0[1] + m0[2] * m0[2]) * dd - a * a > thr * dd;
         if (far) return kInf;
     }
-    double q = quad_inv64(M, m0[0], m0[1], m0[2]), s = 0.0;
+    const Adj64 adj(M);
+    double q = adj.form(m0[0], m0[1], m0[2]), s = 0.0;
     if (more) {
         const double dx = m1[0] - m0[0], dy = m1[1] - m0[1], dz = m1[2] - m0[2];
         const double dd = dx * dx + dy * dy + dz * dz;
@@ -49,7 +59,7 @@ __device__ __forceinline__ double point_chi2_64(double (&M)[6], double R2, const
             s = -(m0[0] * dx + m0[1] * dy + m0[2] * dz) / dd;
             if (s < 0) s = 0; else if (s > 1) s = 1;
         }
-        const double qs = quad_inv64(M, m0[0] + dx * s, m0[1] + dy * s, m0[2] + dz * s);
+        const double qs = adj.form(m0[0] + dx * s, m0[1] + dy * s, m0[2] + dz * s);
         if (qs >= 0 && qs < q) q = qs; else s = 0.0;
     }
     s_out = s;

@@ -1054,6 +1054,9 @@ int pgx_screen_exec(PgxContext *ctx, double tmax_myr, double cut, int precision,
         const int s = p & 1;
         if (p + 1 < K) {
             bind_part(ctx, s ^ 1, p + 1);
+            // the second part's orbits start after the first part's: both at once would share the FP64 pipes and
+            // hold back the first screen by the second part's orbits too
+            if (overlap && p == 0) CK(cudaStreamWaitEvent(ctx->side, ctx->ev[EV_COV], 0));
             if (overlap) RET(tracks_slot(ctx, s ^ 1, tmax_myr, ctx->side, false, kSideOrbitBlocksPerSm * ctx->sms));
         }
         // the first part's screen keeps the exec's stats (its orbit and covariance times); later parts' are added

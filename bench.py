@@ -69,10 +69,10 @@ FP64_INSTR_PER_CLONE_STEP = 73.3 + 9.3 + 58.9
 ORBIT_TRAFFIC_BYTES = 718.6e6
 # DRAM traffic of the block filter k_mx_scan32_blocks per pair-point (read + write of one ncu capture of one part's
 # launch, `bench.py --mode screen --stars 2500 --parts 1`: 6.30e8 pair-points); a part's launch moves its share
-SCAN_TRAFFIC_PER_PAIR_POINT = (105.08e6 + 48.26e6) / 6.303e8
-# warp instructions the block filter issues per pair-point (smsp__inst_executed.sum of the same capture: 3.81e9 for
+SCAN_TRAFFIC_PER_PAIR_POINT = (103.69e6 + 47.78e6) / 6.303e8
+# warp instructions the block filter issues per pair-point (smsp__inst_executed.sum of the same capture: 3.57e9 for
 # 6.30e8 pair-points); its issue bound is 4 warp instructions per clock per SM (one per scheduler)
-SCAN_WARP_INSTR_PER_PAIR_POINT = 3.8084e9 / 6.303e8
+SCAN_WARP_INSTR_PER_PAIR_POINT = 3.5741e9 / 6.303e8
 ISSUE_PER_CLK_SM = 4
 
 

@@ -137,10 +137,11 @@ PGX_HD bool point_skip32(const float (&St)[6], const float (&Sc)[6], float lmt, 
 //            points, so every point the FP64 path evaluates for the block -- m0 at a track point, or its nearest
 //            point on a chord -- lies in the tube p(km) + v tau + a tau^2 / 2 + e, |e| <= eps, |tau| <= 4 h;
 //   S        an FP32 matrix that dominates S(k) (+ R^2 I for a cluster) at every point of the range: S(ke) + delta I,
-//            delta >= the largest eigenvalue of S(k) - S(ke) over the range, the FP32 rounding absorbed into delta
-//            (the covariances are needle-thin and turn along the track, so delta is often many times the thin axis:
-//            this domination, not the tube, is what leaves blocks unsettled);
-//   lam      <= lambda_min(S) (the point's FP64 lower bound at ke + delta, rounded down);
+//            delta >= the largest eigenvalue of S(k) - S(ke) over the range, or -- the covariances are needle-thin
+//            and turn along the track, so S(k) - S(ke) is positive mostly along one direction u and delta is often
+//            many times the thin axis -- S(ke) + alpha u u^T + beta I with beta covering the plane orthogonal to u
+//            (k_block_tables derives both); the FP32 rounding absorbed;
+//   lam      <= lambda_min(S) (the point's FP64 lower bound at ke, plus delta or beta, rounded down);
 //   lam_lo   <= lambda_min(S(k)) at every point of the range (the point bounds' minimum), for the adjugate's error.
 // For a pair, M(k) = S_t(k) + S_c(k) + R^2 I <= N = S_t + S_c (Loewner order), so x^T M(k)^-1 x >= x^T N^-1 x, and
 // every evaluated x = m_ref + dv tau + da tau^2 / 2 + e (m_ref = the separation at km, dv and da the differences)

@@ -175,26 +175,115 @@ __global__ void k_block_tables(int N, int nmax, const int *__restrict__ npts, co
     double Se[6];
     for (int q = 0; q < 6; q++) Se[q] = at(ke, 6 + q);
     Se[0] += r2; Se[3] += r2; Se[5] += r2;
+    // delta: a bound on the largest eigenvalue of S(k) - S(ke) over the range (Gershgorin: the largest diagonal entry
+    // plus its row's off-diagonal magnitudes, rounding included), and k*, the point where it is largest
     double delta = 0.0;
+    int kstar = -1;
     float lam_lo = __int_as_float(0x7f800000);
     for (int k = k0; k <= ke; k++) {
         if (k < ke) {
             double D[6];
             for (int q = 0; q < 6; q++) D[q] = at(k, 6 + q) - at(ke, 6 + q);
-            // lambda_max(D) = -lambda_min(-D) <= -(a lower bound on lambda_min(-D))
-            const double up = -sym3_min_eig_lb(-D[0], -D[1], -D[2], -D[3], -D[4], -D[5]);
-            delta = fmax(delta, up);
+            const double g0 = D[0] + fabs(D[1]) + fabs(D[2]), g1 = D[3] + fabs(D[1]) + fabs(D[4]),
+                         g2 = D[5] + fabs(D[2]) + fabs(D[4]);
+            const double up = fmax(g0, fmax(g1, g2)) * (1.0 + 1e-12);
+            if (up > delta) { delta = up; kstar = k; }
         }
         lam_lo = fminf(lam_lo, lm[(size_t)k * NN + i]);
     }
-    // S(ke) + (delta + r) I rounded to FP32: each entry's rounding is within 2^-24 of its magnitude, so the rounding
-    // error E has ||E|| <= 3 * 2^-24 (mx + r) < r: the stored matrix still dominates S(ke) + delta I
+    double mxe = 0.0;
+    for (int q = 0; q < 6; q++) mxe = fmax(mxe, fabs(Se[q]));
+    // or S(ke) + alpha u u^T + beta I: the needle-thin covariances turn and shrink along the track, so S(k) - S(ke)
+    // is positive mostly along one direction u (where the needle was), and delta I inflates the thin axes by many
+    // times their size.  With u the top eigenvector of S(k*) - S(ke) and (u, w1, w2) an orthonormal basis, each
+    // D = S(k) - S(ke) rotated into it: beta >= the largest eigenvalue of its (w1, w2) block over the range, and then
+    // alpha >= the Schur complement's need, b^T C^-1 b - a for B = beta' I - D written as [a b^T; b C], makes
+    // alpha u u^T + B positive semidefinite at every k, so S(ke) + alpha u u^T + beta' I dominates S(k).  Kept when
+    // beta is under half of delta (the thin axes grow by beta instead of delta).  Its FP64 roundings are relative to
+    // the entries, far below the FP32 storage margin r below.
+    bool rank1 = false;
+    double al = 0.0, be = 0.0, u[3] = {0.0, 0.0, 0.0};
+    if (kstar >= 0) {
+        double D[6];
+        for (int q = 0; q < 6; q++) D[q] = at(kstar, 6 + q) - at(ke, 6 + q);
+        const double lt = -sym3_min_eig_lb(-D[0], -D[1], -D[2], -D[3], -D[4], -D[5]);   // ~ its top eigenvalue
+        // the eigenvector: the largest cross product of two rows of D - lt I
+        const double R0[3] = {D[0] - lt, D[1], D[2]}, R1[3] = {D[1], D[3] - lt, D[4]}, R2r[3] = {D[2], D[4], D[5] - lt};
+        auto cross = [](const double *x, const double *y, double *z) {
+            z[0] = x[1] * y[2] - x[2] * y[1]; z[1] = x[2] * y[0] - x[0] * y[2]; z[2] = x[0] * y[1] - x[1] * y[0];
+        };
+        double c0[3], c1[3], c2[3];
+        cross(R0, R1, c0); cross(R0, R2r, c1); cross(R1, R2r, c2);
+        const double n0 = c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2];
+        const double n1 = c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2];
+        const double n2 = c2[0] * c2[0] + c2[1] * c2[1] + c2[2] * c2[2];
+        const double *cb = n0 >= n1 && n0 >= n2 ? c0 : (n1 >= n2 ? c1 : c2);
+        const double nb = fmax(n0, fmax(n1, n2));
+        if (lt > 0.0 && nb > 0.0) {
+            const double inv = 1.0 / sqrt(nb);
+            u[0] = cb[0] * inv; u[1] = cb[1] * inv; u[2] = cb[2] * inv;
+            const double e0[3] = {1.0, 0.0, 0.0}, e1[3] = {0.0, 1.0, 0.0};
+            double w1[3], w2[3];
+            cross(u, fabs(u[0]) < 0.9 ? e0 : e1, w1);
+            const double iw = 1.0 / sqrt(w1[0] * w1[0] + w1[1] * w1[1] + w1[2] * w1[2]);
+            w1[0] *= iw; w1[1] *= iw; w1[2] *= iw;
+            cross(u, w1, w2);
+            // each D rotated into (u, w1, w2): its entries x^T D y
+            double du_[kBlk], dw11[kBlk], dw12[kBlk], dw22[kBlk], duw1[kBlk], duw2[kBlk];
+            const int nk = ke - k0;                       // <= kBlk: ke <= k0 + kBlk
+            for (int j = 0; j < nk; j++) {
+                double Dk[6];
+                for (int q = 0; q < 6; q++) Dk[q] = at(k0 + j, 6 + q) - at(ke, 6 + q);
+                double Du[3], Dw1[3];                     // D u, D w1
+                Du[0] = Dk[0] * u[0] + Dk[1] * u[1] + Dk[2] * u[2];
+                Du[1] = Dk[1] * u[0] + Dk[3] * u[1] + Dk[4] * u[2];
+                Du[2] = Dk[2] * u[0] + Dk[4] * u[1] + Dk[5] * u[2];
+                Dw1[0] = Dk[0] * w1[0] + Dk[1] * w1[1] + Dk[2] * w1[2];
+                Dw1[1] = Dk[1] * w1[0] + Dk[3] * w1[1] + Dk[4] * w1[2];
+                Dw1[2] = Dk[2] * w1[0] + Dk[4] * w1[1] + Dk[5] * w1[2];
+                const double Dw2_2 = Dk[2] * w2[0] + Dk[4] * w2[1] + Dk[5] * w2[2];
+                const double Dw2_0 = Dk[0] * w2[0] + Dk[1] * w2[1] + Dk[2] * w2[2];
+                const double Dw2_1 = Dk[1] * w2[0] + Dk[3] * w2[1] + Dk[4] * w2[2];
+                du_[j] = u[0] * Du[0] + u[1] * Du[1] + u[2] * Du[2];
+                duw1[j] = w1[0] * Du[0] + w1[1] * Du[1] + w1[2] * Du[2];
+                duw2[j] = w2[0] * Du[0] + w2[1] * Du[1] + w2[2] * Du[2];
+                dw11[j] = w1[0] * Dw1[0] + w1[1] * Dw1[1] + w1[2] * Dw1[2];
+                dw12[j] = w2[0] * Dw1[0] + w2[1] * Dw1[1] + w2[2] * Dw1[2];
+                dw22[j] = w2[0] * Dw2_0 + w2[1] * Dw2_1 + w2[2] * Dw2_2;
+                const double h = 0.5 * (dw11[j] - dw22[j]);
+                be = fmax(be, 0.5 * (dw11[j] + dw22[j]) + sqrt(h * h + dw12[j] * dw12[j]));
+            }
+            be = be * (1.0 + 1e-6) + 1e-9 * mxe;
+            bool ok = true;
+            for (int j = 0; j < nk; j++) {
+                // B = be I - D in the basis: a = be - D_uu, b = -D_uw, C = be I - D_ww
+                const double a = be - du_[j], b1 = -duw1[j], b2 = -duw2[j];
+                const double c11 = be - dw11[j], c12 = -dw12[j], c22 = be - dw22[j];
+                const double det = c11 * c22 - c12 * c12;
+                if (!(c11 > 0.0 && det > 0.0)) { ok = false; break; }
+                al = fmax(al, (c22 * b1 * b1 - 2.0 * c12 * b1 * b2 + c11 * b2 * b2) / det - a);
+            }
+            if (ok) {
+                al = al * (1.0 + 1e-6) + 1e-9 * mxe;
+                rank1 = be < 0.5 * delta;
+            }
+        }
+    }
+    // the chosen matrix plus r I, rounded to FP32: each entry's rounding is within 2^-24 of its magnitude, so the
+    // rounding error E has ||E|| <= 3 * 2^-24 (mx + r) < r: the stored matrix still dominates it
+    double Sd[6];
+    if (rank1) {
+        Sd[0] = Se[0] + al * u[0] * u[0] + be; Sd[1] = Se[1] + al * u[0] * u[1]; Sd[2] = Se[2] + al * u[0] * u[2];
+        Sd[3] = Se[3] + al * u[1] * u[1] + be; Sd[4] = Se[4] + al * u[1] * u[2]; Sd[5] = Se[5] + al * u[2] * u[2] + be;
+    } else {
+        Sd[0] = Se[0] + delta; Sd[1] = Se[1]; Sd[2] = Se[2];
+        Sd[3] = Se[3] + delta; Sd[4] = Se[4]; Sd[5] = Se[5] + delta;
+    }
     double mx = 0.0;
-    for (int q = 0; q < 6; q++) mx = fmax(mx, fabs(Se[q]));
-    mx += delta;
+    for (int q = 0; q < 6; q++) mx = fmax(mx, fabs(Sd[q]));
     const double r = 4.0 * 5.9604644775390625e-8 * mx;
-    double Sd[6] = {Se[0] + delta + r, Se[1], Se[2], Se[3] + delta + r, Se[4], Se[5] + delta + r};
-    const float lam = __double2float_rd((double)lm[(size_t)ke * NN + i] + delta);
+    Sd[0] += r; Sd[3] += r; Sd[5] += r;
+    const float lam = __double2float_rd((double)lm[(size_t)ke * NN + i] + (rank1 ? be : delta));
     o[0] = make_float4(v32[0], v32[1], v32[2], __double2float_ru(eps));
     o[1] = make_float4(a32[0], a32[1], a32[2], lam);
     o[2] = make_float4((float)Sd[0], (float)Sd[1], (float)Sd[2], (float)Sd[3]);

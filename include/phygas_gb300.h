@@ -88,7 +88,10 @@ int pgx_screen_into(PgxContext *ctx, int nt, const double *ps0, const double *si
 void *pgx_host_alloc(size_t bytes);
 /* The whole star list t[nt] in chunks of `chunk` stars, pipelined: while the GPU screens chunk i, the draws of chunk
  * i + 1 (ph_lin_target_init's, on `threads` host threads) run, the rows of chunk i - 1 are copied into page-locked
- * memory on a second stream, and emit(arg, first star of chunk i - 1, rows, count) runs on the calling thread.  Star
+ * memory on a second stream, and emit(arg, first star of chunk i - 1, rows, count) runs on the calling thread.  The
+ * first chunks are smaller where `chunk` is larger than round(1e7 / clusters) stars: the first is that many, each
+ * next one s + s / 2 (integer division) after one of s stars, up to `chunk` -- the first chunk's orbits are the only
+ * ones not traced beside another chunk's screen.  Star
  * indices in the rows are relative to the chunk's first star; the pointer is valid until emit returns.  Chunks are
  * emitted in order.  A non-zero return from emit stops the run.  The page-locked and device row buffers (two chunks
  * of each) stay with the context for the next call. */

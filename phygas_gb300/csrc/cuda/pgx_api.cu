@@ -1154,7 +1154,18 @@ int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n
     const bool text = out.text != nullptr;
     CK(cudaSetDevice(ctx->device));
     const int th = threads > 0 ? threads : pgh_default_threads();
-    const int nch = (nt + chunk - 1) / chunk;
+    // Chunk boundaries: `chunk` stars each, except that the first chunks ramp up from about kPartPairs star-cluster
+    // pairs, each half again as large as the last: the first chunk's orbits are the only ones not traced beside
+    // another chunk's screen, and each later chunk's orbits (FP64, at least one warp's 2,000 steps long) stay shorter
+    // than the screen before them.  Measured on 8 chunks of 20,000 stars x 4,087 clusters: 82.5-87.8 against
+    // 87.1-90.6 ms per chunk without the ramp, 84.2-89.6 when doubling.
+    std::vector<int> cfirst;
+    {
+        int s = std::min(chunk, std::max(1, (int)std::lround(kPartPairs / std::max(ctx->nc, 1))));
+        for (int f = 0; f < nt; f += s, s = std::min(chunk, s + std::max(1, s / 2))) cfirst.push_back(f);
+        cfirst.push_back(nt);
+    }
+    const int nch = (int)cfirst.size() - 1;
     struct Draw {
         std::vector<double> ps0, sig;
         std::vector<uint64_t> pre;
@@ -1168,8 +1179,8 @@ int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n
         if (text) b.ids.resize((size_t)40 * chunk);
     }
     auto draw = [&](int c, Draw &b) {
-        b.first = c * chunk;
-        b.n = std::min(chunk, nt - b.first);
+        b.first = cfirst[c];
+        b.n = cfirst[c + 1] - cfirst[c];
         pgh_draw_targets(t + b.first, b.n, n_samp, th, b.ps0.data(), b.sig.data(), b.pre.data());
         for (int i = 0; text && i < b.n; i++) memcpy(&b.ids[(size_t)40 * i], t[b.first + i].id, 40);
     };
@@ -1217,7 +1228,7 @@ int screen_pipeline(PgxContext *ctx, const PhTarget *t, int nt, int chunk, int n
             if (nch > 1) ahead = std::thread(draw, 1, std::ref(buf[1]));
         }
         for (int c = 0; c < nch && wrc == 0; c++) {
-            const int first = c * chunk;
+            const int first = cfirst[c];
             if (c + 1 < nch) {                            // the next chunk's orbits, beside this chunk's screen
                 ahead.join();
                 wrc = start_tracks(c + 1);

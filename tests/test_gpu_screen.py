@@ -172,6 +172,33 @@ def test_screen_chunks_pipeline_matches_one_screen(ctx, golden):
     assert len(ctx.screen(*pg.draw_targets(stars[:40]), tmax)) >= 0      # the context is still usable
 
 
+def test_screen_chunks_ramp_up(ctx):
+    """Against 4,087 clusters a chunk of more than about 1e7 star-cluster pairs is preceded by smaller ones: the first
+    chunk of round(1e7 / 4,087) = 2,447 stars, each next one half again as large (integer halves), up to the chunk
+    size.  The rows, in order and renumbered, equal one screen of the whole list, in both precisions."""
+    from phygas_gb300 import synth
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        cp, tp = synth.write_workload(d, "screen", 9000, 1007)
+        clusters, stars = pg.read_clusters(cp), pg.read_targets(tp)
+    assert len(clusters) == 4087
+    ctx.set_clusters(clusters)
+    tmax = max(c.tmax_myr for c in clusters)
+    for prec in PRECISIONS:
+        want = ctx.screen(*pg.draw_targets(stars), tmax, 25.0, prec)
+        for chunk, firsts_want in ((9000, [0, 2447, 6117]), (4000, [0, 2447, 6117]), (2000, [0, 2000, 4000, 6000, 8000])):
+            got, firsts = [], []
+
+            def emit(first, rows):
+                r = np.array(rows, copy=True)
+                r["star"] += first
+                firsts.append(first)
+                got.append(r)
+            ctx.screen_chunks(stars, chunk, tmax, emit, 25.0, prec)
+            assert firsts == firsts_want, (prec, chunk, firsts)
+            assert np.concatenate(got).tobytes() == want.tobytes(), (prec, chunk)
+
+
 def _lines(rows, stars, clusters, first=0):
     """the reference CLI's line for each row, formatted by Python (exact decimal rounding, as printf)"""
     out = []

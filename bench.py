@@ -517,7 +517,8 @@ def scan_roofline(stats, clocks, pp, fp32_peak, parts):
            "peak_source": "FP32 FMA probe kernel of this run (pgx_peaks); not in MEASURED_PEAKS.json",
            "traffic": SCAN_TRAFFIC_PER_PAIR_POINT * pp / parts,
            "flops_per_pair_point": FLOPS_PER_PAIR_POINT, "pair_points_per_launch": pp / parts,
-           "launches_per_step": parts, "ms_per_launch": ms / parts}
+           "launches_per_step": parts, "ms_per_launch": ms / parts,
+           "per_launch": "means over the step's launches (its parts ramp up in size); achieved and frac from their sum"}
     if mhz:
         out["issue_frac"] = SCAN_WARP_INSTR_PER_PAIR_POINT * pp / (ms * 1e-3) / (ISSUE_PER_CLK_SM * sms * mhz * 1e6)
     return out
@@ -747,8 +748,8 @@ def main():
     g.add_argument("--seed", type=int, default=None)
     g.add_argument("--precision", choices=("mixed", "fp64"), default="mixed")
     g.add_argument("--parts", type=int, default=None,
-                   help="screen: parts of a chunk of at least 8,192 stars (1 = screened whole; default about 1e7 "
-                        "star-cluster pairs a part)")
+                   help="screen: equal parts of a chunk of at least 8,192 stars (1 = screened whole; default parts "
+                        "ramping up from about 1e7 star-cluster pairs)")
     g.add_argument("--repeat", type=int, default=1)
     g.add_argument("--pairs", type=int, default=200)
     g.add_argument("--pulsars", type=int, default=1)

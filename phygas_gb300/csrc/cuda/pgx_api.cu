@@ -47,10 +47,12 @@ enum { EV_START, EV_ORBIT, EV_COV, EV_SCREEN, EV_SCAN, EV_SELECT, EV_FINISH, EV_
 // registers (its FP32 and integer work and the orbits' FP64 work use different pipes), enough to finish first.
 constexpr int kSideOrbitBlocksPerSm = 2;
 // pgx_screen_stage splits chunks of at least this many stars in parts, so that exec can overlap one part's orbits
-// with the previous part's screen: by default parts of about kPartPairs star-cluster pairs (2,447 stars at 4,087
-// clusters).  A part's screen must outlast the next part's orbits, whose 2,000 KDK steps set a latency floor of a few
-// ms: measured on 20,000 x 4,087, 122 ms whole, 103 ms in 5 parts, 100 ms in 8, 104 ms in 12, 116 ms in 16; and 3
-// parts best for 8,192 stars, 5 for 12,000.
+// with the previous part's screen.  A part's screen must outlast the next part's orbits, whose 2,000 KDK steps set a
+// latency floor of a few ms whatever the part's size, so the first part, whose orbits are exposed, is small and the
+// parts then grow: by default the first of about kPartPairs star-cluster pairs (2,447 stars at 4,087 clusters), each
+// next half again as large (20,000 stars: 2,447, 3,670, 5,505 and 8,378).  Measured on 20,000 x 4,087: 89.0 ms a
+// step against 90.0 in 8 equal parts (earlier, before the block filter: 122 ms whole, 103 in 5 equal parts, 100 in 8,
+// 104 in 12, 116 in 16).
 constexpr int kSplitStars = 8192;
 constexpr double kPartPairs = 1.0e7;
 
@@ -88,7 +90,7 @@ struct PgxContext {
     TrackSlot trk[2];
     int cur = 0;
     int split_min = kSplitStars;               // chunks of at least this many stars are split (0: never)
-    int parts = 0;                             // in this many parts (0: about kPartPairs pairs each)
+    int parts = 0;                             // in this many equal parts (0: parts ramping up from kPartPairs pairs)
     // a split chunk: pgx_screen_stage put part p's inputs (ps0[6][n], sig21[21][n], prefix[n]) at part_at[p] in
     // part_in; exec binds the parts to the two track slots in turn
     int nparts = 0;
@@ -978,14 +980,28 @@ int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *s
     if (nt > (1 << 20)) return fail(ctx, PGX_E_LIMIT, "pgx_screen_stage: %d stars in one chunk (limit 2^20)", nt);
     // the parts' inputs, SoA per part, back to back: one page-locked staging buffer and one copy
     const double part_stars = std::max(1.0, kPartPairs / std::max(ctx->nc, 1));
-    const int K = std::min(nt, ctx->parts > 0 ? ctx->parts
-                                              : std::max(2, std::min(64, (int)std::lround(nt / part_stars))));
+    std::vector<int> sizes;
+    if (ctx->parts == 0) {
+        // parts ramping up: the first of about kPartPairs pairs, each next half again as large, a last one under half
+        // of the one before it merged into that one, at least two
+        int s = std::min(nt, (int)std::lround(part_stars));
+        for (int f = 0; f < nt; f += s, s = s + std::max(1, s / 2)) sizes.push_back(std::min(s, nt - f));
+        if (sizes.size() > 2 && 2 * sizes.back() < sizes[sizes.size() - 2]) {
+            sizes[sizes.size() - 2] += sizes.back();
+            sizes.pop_back();
+        }
+        if (sizes.size() < 2) sizes = {nt / 2, nt - nt / 2};
+    } else {
+        const int K0 = std::min(nt, ctx->parts);                    // pgx_screen_parts: K equal parts
+        for (int p = 0; p < K0; p++) sizes.push_back(nt / K0 + (p < nt % K0 ? 1 : 0));
+    }
+    const int K = (int)sizes.size();
     ctx->part_n.assign(K, 0);
     ctx->part_off.assign(K, 0);
     ctx->part_at.assign(K, 0);
     size_t bytes = 0;
     for (int p = 0, off = 0; p < K; p++) {
-        ctx->part_n[p] = nt / K + (p < nt % K ? 1 : 0);
+        ctx->part_n[p] = sizes[p];
         ctx->part_off[p] = off;
         ctx->part_at[p] = bytes;
         off += ctx->part_n[p];

@@ -175,7 +175,8 @@ def test_screen_chunks_pipeline_matches_one_screen(ctx, golden):
 def test_screen_chunks_ramp_up(ctx):
     """Against 4,087 clusters a chunk of more than about 1e7 star-cluster pairs is preceded by smaller ones: the first
     chunk of round(1e7 / 4,087) = 2,447 stars, each next one half again as large (integer halves), up to the chunk
-    size.  The rows, in order and renumbered, equal one screen of the whole list, in both precisions."""
+    size.  A staged chunk of 9,000 stars is screened in parts that ramp up the same way (2,447, 3,670, 2,883).  The
+    rows, in order and renumbered, equal one screen of the whole list unsplit, in both precisions."""
     from phygas_gb300 import synth
     import tempfile
     with tempfile.TemporaryDirectory() as d:
@@ -184,8 +185,16 @@ def test_screen_chunks_ramp_up(ctx):
     assert len(clusters) == 4087
     ctx.set_clusters(clusters)
     tmax = max(c.tmax_myr for c in clusters)
+    draws = pg.draw_targets(stars)
     for prec in PRECISIONS:
-        want = ctx.screen(*pg.draw_targets(stars), tmax, 25.0, prec)
+        try:
+            ctx.set_split(0)
+            whole = ctx.screen(*draws, tmax, 25.0, prec)
+        finally:
+            ctx.set_split(8192)
+        want = ctx.screen(*draws, tmax, 25.0, prec)
+        assert ctx.stats()["parts"] == 3
+        assert want.tobytes() == whole.tobytes(), prec
         for chunk, firsts_want in ((9000, [0, 2447, 6117]), (4000, [0, 2447, 6117]), (2000, [0, 2000, 4000, 6000, 8000])):
             got, firsts = [], []
 

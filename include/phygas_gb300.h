@@ -78,8 +78,9 @@ int pgx_screen_fetch(PgxContext *ctx, PgxScreenRow *rows, long n);
 /* Chunks of at least min_stars stars (default 8192; 0 = never) are staged in parts, and exec traces each part's orbits
  * beside the previous part's screen (the mixed path; the FP64 path screens the parts in turn).  pgx_screen_parts(ctx,
  * K) fixes K equal parts (2 to 64); its default 0 ramps them up: the first of round(1e7 / clusters) stars, each next
- * s + s / 2 after one of s stars, a last part under half of the one before merged into that one, at least 2 (20,000
- * stars at 4,087 clusters: 2,447, 3,670, 5,505, 8,378).  The rows are the same either way. */
+ * s + 3s / 4 after one of s stars (integer division), a last part under half of the one before merged into that one
+ * where the two together are at most 1.75 times the part before them, at least 2 (20,000 stars at 4,087 clusters:
+ * 2,447, 4,282, 7,493, 5,778).  The rows are the same either way. */
 int pgx_screen_split(PgxContext *ctx, int min_stars);
 int pgx_screen_parts(PgxContext *ctx, int parts);
 /* pgx_screen writing into the caller's rows[cap] (no allocation); *n_rows = the kept pairs, PGX_E_LIMIT (rows kept on

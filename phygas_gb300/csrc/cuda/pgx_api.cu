@@ -50,9 +50,10 @@ constexpr int kSideOrbitBlocksPerSm = 2;
 // with the previous part's screen.  A part's screen must outlast the next part's orbits, whose 2,000 KDK steps set a
 // latency floor of a few ms whatever the part's size, so the first part, whose orbits are exposed, is small and the
 // parts then grow: by default the first of about kPartPairs star-cluster pairs (2,447 stars at 4,087 clusters), each
-// next half again as large (20,000 stars: 2,447, 3,670, 5,505 and 8,378).  Measured on 20,000 x 4,087: 89.0 ms a
-// step against 90.0 in 8 equal parts (earlier, before the block filter: 122 ms whole, 103 in 5 equal parts, 100 in 8,
-// 104 in 12, 116 in 16).
+// next 1.75 times the last (20,000 stars: 2,447, 4,282, 7,493 and 5,778).  Measured on 20,000 x 4,087: 87.9 ms a
+// step, against 90.1, 88.5, 91.0 and 95.8 ms growing by 1.6, 1.7, 1.8 and 1.9, 89.0 by 1.5, 90.0 in 8 equal parts;
+// beside the screens the orbits take 2 blocks per SM (1 block: 98.7 ms, 3: 89.8).  Earlier, before the block filter:
+// 122 ms whole, 103 in 5 equal parts, 100 in 8, 104 in 12, 116 in 16.
 constexpr int kSplitStars = 8192;
 constexpr double kPartPairs = 1.0e7;
 
@@ -982,12 +983,14 @@ int pgx_screen_stage(PgxContext *ctx, int nt, const double *ps0, const double *s
     const double part_stars = std::max(1.0, kPartPairs / std::max(ctx->nc, 1));
     std::vector<int> sizes;
     if (ctx->parts == 0) {
-        // parts ramping up: the first of about kPartPairs pairs, each next half again as large, a last one under half
-        // of the one before it merged into that one, at least two
+        // parts ramping up: the first of about kPartPairs pairs, each next s + 3s/4 after one of s, a last part under
+        // half of the one before merged into that one where the two together stay within that growth, at least two
         int s = std::min(nt, (int)std::lround(part_stars));
-        for (int f = 0; f < nt; f += s, s = s + std::max(1, s / 2)) sizes.push_back(std::min(s, nt - f));
-        if (sizes.size() > 2 && 2 * sizes.back() < sizes[sizes.size() - 2]) {
-            sizes[sizes.size() - 2] += sizes.back();
+        for (int f = 0; f < nt; f += s, s = s + std::max(1, 3 * s / 4)) sizes.push_back(std::min(s, nt - f));
+        const size_t k = sizes.size();
+        if (k > 2 && 2 * sizes[k - 1] < sizes[k - 2] &&
+            sizes[k - 2] + sizes[k - 1] <= sizes[k - 3] + 3 * sizes[k - 3] / 4) {
+            sizes[k - 2] += sizes[k - 1];
             sizes.pop_back();
         }
         if (sizes.size() < 2) sizes = {nt / 2, nt - nt / 2};

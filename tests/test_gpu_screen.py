@@ -175,7 +175,7 @@ def test_screen_chunks_pipeline_matches_one_screen(ctx, golden):
 def test_screen_chunks_ramp_up(ctx):
     """Against 4,087 clusters a chunk of more than about 1e7 star-cluster pairs is preceded by smaller ones: the first
     chunk of round(1e7 / 4,087) = 2,447 stars, each next one half again as large (integer halves), up to the chunk
-    size.  A staged chunk of 9,000 stars is screened in parts that ramp up the same way (2,447, 3,670, 2,883).  The
+    size.  A staged chunk of 9,000 stars is screened in parts that ramp up too (2,447, 4,282, 2,271).  The
     rows, in order and renumbered, equal one screen of the whole list unsplit, in both precisions."""
     from phygas_gb300 import synth
     import tempfile

@@ -195,7 +195,8 @@ def test_screen_chunks_ramp_up(ctx):
         want = ctx.screen(*draws, tmax, 25.0, prec)
         assert ctx.stats()["parts"] == 3
         assert want.tobytes() == whole.tobytes(), prec
-        for chunk, firsts_want in ((9000, [0, 2447, 6117]), (4000, [0, 2447, 6117]), (2000, [0, 2000, 4000, 6000, 8000])):
+        for chunk, firsts_want in ((9000, [0, 2447, 6117]), (4000, [0, 2447, 6117]),
+                                   (2000, [0, 2000, 4000, 6000, 8000])):
             got, firsts = [], []
 
             def emit(first, rows):
